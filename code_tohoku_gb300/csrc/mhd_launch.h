@@ -1,0 +1,35 @@
+// mhd_launch.h — host-side launchers shared by the two precision
+// translation units (mhd_fp64.cu, mhd_fp32.cu) and the C-ABI layer.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mhd_kernels.cuh"
+
+namespace mhd {
+
+// largest pencil batch P in {4,2,1} that divides the batching direction
+// and fits the shared-memory budget
+int sweep_batch(const Grid &g, int dir);
+size_t sweep_smem_bytes(const Grid &g, int dir, int P);
+
+// plain form (every operation FP64, no contraction)
+cudaError_t sweep_fp64(int dir, const SweepArgs &a, cudaStream_t s);
+cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s);
+// chosen form (FP32 reconstruction / Riemann / characteristics)
+cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s);
+cudaError_t emf_fp32(int e, const CTArgs &a, cudaStream_t s);
+
+// precision-independent FP64 kernels (built in the FP64 unit)
+cudaError_t ghost_fill(const Grid &g, const FillArgs &f, int dir, int nol, int species, cudaStream_t s);
+cudaError_t face_velocity(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
+cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const double *ex, const double *ey, double dt,
+                   cudaStream_t s);
+cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s);
+cudaError_t source_pass(const SourceArgs &a, cudaStream_t s);
+cudaError_t dt_reduce(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
+                      cudaStream_t s);
+cudaError_t divv(const Grid &g, const Fields &f, double *d, cudaStream_t s);
+cudaError_t dissip(const Grid &g, const Fields &f, const double *d, int e, cudaStream_t s);
+cudaError_t diag(const Grid &g, const Phys &ph, const Fields &f, double *part, int *nblocks, cudaStream_t s);
+
+}  // namespace mhd

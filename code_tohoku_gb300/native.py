@@ -1,0 +1,219 @@
+"""ctypes binding of libmhd_gb300.so (the C ABI of include/mhd_gb300.h).
+
+This is the Python face of the same entry points a Fortran driver binds
+with iso_c_binding.  There is no CPU fallback: if the CUDA library cannot
+be loaded or no GPU is present, every constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from .problems import MhdParams, MhdState
+
+MHD_OK = 0
+ERRORS = {1: "MHD_ERR_ARG", 2: "MHD_ERR_CUDA", 3: "MHD_ERR_NONFINITE", 4: "MHD_ERR_DT",
+          5: "MHD_ERR_STATE", 6: "MHD_ERR_NO_DEVICE"}
+PREC_FP64, PREC_FP32 = 0, 1
+COOL_EXACT, COOL_SURROGATE = 0, 1
+
+# every symbol the header declares (checked by the CPU test suite)
+EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_timestep", "mhd_source",
+           "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_evolve", "mhd_get_time",
+           "mhd_set_time", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
+           "mhd_kernel_launches")
+
+
+class MhdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("cfl", ctypes.c_double), ("facdep", ctypes.c_double), ("tfinal", ctypes.c_double),
+                ("bc", ctypes.c_int * 6),
+                ("pmin", ctypes.c_double), ("pmax", ctypes.c_double), ("rmin", ctypes.c_double),
+                ("kb", ctypes.c_double), ("kcond", ctypes.c_double),
+                ("ifthrm", ctypes.c_int), ("dissip", ctypes.c_int), ("precision", ctypes.c_int),
+                ("cooling", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class _Diag(ctypes.Structure):
+    _fields_ = [("mass", ctypes.c_double), ("momentum", ctypes.c_double * 3), ("energy", ctypes.c_double),
+                ("divb_max", ctypes.c_double), ("time", ctypes.c_double), ("steps", ctypes.c_longlong),
+                ("imc_cells", ctypes.c_longlong), ("surrogate_cells", ctypes.c_longlong),
+                ("fallback_cells", ctypes.c_longlong)]
+
+
+_lib = None
+_P = ctypes.POINTER(ctypes.c_double)
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libmhd_gb300.so, compiling it first when it is missing or stale."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError(f"{_build.LIB} is missing; run code_tohoku_gb300.build.build()")
+    L = ctypes.CDLL(_build.LIB)
+    H = ctypes.c_void_p
+    sig = {
+        "mhd_create": [ctypes.POINTER(_Params), ctypes.POINTER(H)],
+        "mhd_destroy": [H],
+        "mhd_upload": [H, _P, _P, _P, _P, _P, _P, _P, _P],
+        "mhd_download": [H, _P, _P, _P],
+        "mhd_timestep": [H, _P, ctypes.POINTER(ctypes.c_int)],
+        "mhd_source": [H, ctypes.c_double],
+        "mhd_sweep": [H, ctypes.c_int, ctypes.c_double],
+        "mhd_ct": [H, ctypes.c_double],
+        "mhd_dissip": [H],
+        "mhd_advance": [H, ctypes.c_double],
+        "mhd_step": [H, ctypes.c_double, _P, ctypes.POINTER(ctypes.c_int)],
+        "mhd_evolve": [H, ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int)],
+        "mhd_get_time": [H, _P, ctypes.POINTER(ctypes.c_int)],
+        "mhd_set_time": [H, ctypes.c_double, ctypes.c_int],
+        "mhd_diagnostics": [H, ctypes.POINTER(_Diag)],
+        "mhd_synchronize": [H],
+        "mhd_set_stream": [H, ctypes.c_void_p],
+        "mhd_last_error": [H, ctypes.c_char_p, ctypes.c_int],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    L.mhd_kernel_launches.argtypes = [H]
+    L.mhd_kernel_launches.restype = ctypes.c_longlong
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P)
+
+
+def params_struct(p: MhdParams, precision=PREC_FP64, cooling=COOL_EXACT, device=0):
+    s = _Params()
+    s.nx, s.ny, s.nz = p.nx, p.ny, p.nz
+    s.cfl, s.facdep, s.tfinal = p.cfl, p.facdep, p.tfinal
+    for q in range(6):
+        s.bc[q] = p.bc[q]
+    s.pmin, s.pmax, s.rmin = p.pmin, p.pmax, p.rmin
+    s.kb, s.kcond = p.kb, p.kcond
+    s.ifthrm, s.dissip = p.ifthrm, p.dissip
+    s.precision, s.cooling, s.device = precision, cooling, device
+    return s
+
+
+class Mhd3D:
+    """GPU-resident 3D MHD + KI cooling state driven through the C ABI."""
+
+    def __init__(self, params: MhdParams, precision=PREC_FP64, cooling=COOL_EXACT, device=0):
+        self.L = load()
+        self.params = params
+        self.shape = (params.nz + 4, params.ny + 4, params.nx + 4)
+        self.h = ctypes.c_void_p()
+        ps = params_struct(params, precision, cooling, device)
+        r = self.L.mhd_create(ctypes.byref(ps), ctypes.byref(self.h))
+        if r != MHD_OK:
+            raise MhdError(r, "mhd_create failed")
+
+    def _ck(self, r):
+        if r != MHD_OK:
+            buf = ctypes.create_string_buffer(512)
+            self.L.mhd_last_error(self.h, buf, 512)
+            raise MhdError(r, buf.value.decode(errors="replace"))
+
+    def upload(self, st: MhdState):
+        U = np.ascontiguousarray(st.U, dtype=np.float64)
+        sp = np.ascontiguousarray(st.species, dtype=np.float64)
+        co = [np.ascontiguousarray(a, dtype=np.float64) for a in (st.x, st.dx, st.y, st.dy, st.z, st.dz)]
+        self._ck(self.L.mhd_upload(self.h, _ptr(U), _ptr(sp), *[_ptr(c) for c in co]))
+
+    def download(self, with_bcc=True):
+        U = np.empty((8,) + self.shape)
+        sp = np.empty((8,) + self.shape)
+        bcc = np.empty((3,) + self.shape) if with_bcc else None
+        self._ck(self.L.mhd_download(self.h, _ptr(U), _ptr(sp), _ptr(bcc) if with_bcc else None))
+        return U, sp, bcc
+
+    def timestep(self):
+        dt = ctypes.c_double()
+        st = ctypes.c_int()
+        self._ck(self.L.mhd_timestep(self.h, ctypes.byref(dt), ctypes.byref(st)))
+        return dt.value, st.value
+
+    def source(self, dt):
+        self._ck(self.L.mhd_source(self.h, dt))
+
+    def sweep(self, d, dt):
+        self._ck(self.L.mhd_sweep(self.h, d, dt))
+
+    def ct(self, dt):
+        self._ck(self.L.mhd_ct(self.h, dt))
+
+    def dissip(self):
+        self._ck(self.L.mhd_dissip(self.h))
+
+    def advance(self, dt):
+        self._ck(self.L.mhd_advance(self.h, dt))
+
+    def step(self, tsave=1e30):
+        dt = ctypes.c_double()
+        st = ctypes.c_int()
+        self._ck(self.L.mhd_step(self.h, tsave, ctypes.byref(dt), ctypes.byref(st)))
+        return dt.value, st.value
+
+    def evolve(self, nsteps, tsave=1e30):
+        n = ctypes.c_int()
+        self._ck(self.L.mhd_evolve(self.h, nsteps, tsave, ctypes.byref(n)))
+        return n.value
+
+    def set_time(self, time, ifevo=1):
+        self._ck(self.L.mhd_set_time(self.h, time, ifevo))
+
+    @property
+    def time(self):
+        t = ctypes.c_double()
+        o = ctypes.c_int()
+        self._ck(self.L.mhd_get_time(self.h, ctypes.byref(t), ctypes.byref(o)))
+        return t.value
+
+    def diagnostics(self):
+        d = _Diag()
+        self._ck(self.L.mhd_diagnostics(self.h, ctypes.byref(d)))
+        return dict(mass=d.mass, momentum=tuple(d.momentum), energy=d.energy, divb_max=d.divb_max,
+                    time=d.time, steps=d.steps, imc_cells=d.imc_cells, surrogate_cells=d.surrogate_cells,
+                    fallback_cells=d.fallback_cells)
+
+    def synchronize(self):
+        self._ck(self.L.mhd_synchronize(self.h))
+
+    def set_stream(self, stream_ptr):
+        self._ck(self.L.mhd_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    @property
+    def kernel_launches(self):
+        return self.L.mhd_kernel_launches(self.h)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.mhd_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,128 @@
+/* mhd_gb300.h — C ABI of the GB300 MHD + Koyama–Inutsuka cooling step.
+ *
+ * The reference program (3DMHD-CfCA/MCF3DSGincfca3.f90) advances its state
+ * inside EVOLVE (:562-657) by calling Fortran subroutines on module arrays.
+ * Each entry point below replaces one of those calls, so the Fortran driver,
+ * its decks (INPUT3D.DAT) and its output writers stay as they are and a
+ * bind(C) interface module routes the calls here:
+ *
+ *   mhd_timestep      Couran :1912-1930 + Stblty :2784-2822 + the dt
+ *                     gather/min/bcast of EVOLVE :569-599
+ *   mhd_source        SOURCE(dt) thermal branch :2477-2572 with the KI
+ *                     Fcool of KIcool/1DMHDwCC3.f90:1148-1173 and IMC
+ *   mhd_sweep         MHD(xelr,dxelr,dt) :1264-1324 (RHS, RIEMAN, MOC,
+ *                     CHAREQ, REMAP, VLIMIT) for one direction
+ *   mhd_ct            CC(1), CC(2)+CCT ×3, CC(3), CC(4) :639-649, :2115-2445
+ *   mhd_dissip        DISSIP :3143-3173
+ *   mhd_advance       one in20 iteration after dt is known :606-656
+ *   mhd_step          the whole in20 iteration including dt :569-656
+ *   mhd_upload/download  the module arrays U(-1:ndx,-1:ndy,-1:ndz,8), the
+ *                     species ndH..ndCO and the coordinates (INITIA, SAVEU)
+ *
+ * All arrays are plain host pointers in the reference's Fortran layout:
+ * U is U(-1:nx+2,-1:ny+2,-1:nz+2,8) column-major (x fastest, then y, z,
+ * then field), i.e. 8 consecutive blocks of (nx+4)(ny+4)(nz+4) doubles.
+ * U(:,:,:,1)=rho, 2..4 = velocity, 5 = pressure, 6..8 = face-centred B
+ * (U(i,j,k,6) is Bx on the x-face i-1/2).  Species use the same block
+ * layout in the order ndH, ndp, ndH2, ndHe, ndHep, ndC, ndCp, ndCO.
+ * Coordinates are x(-1:nx+2) and dx(-1:nx+2), likewise y and z.
+ *
+ * The state lives on the GPU between calls; host copies happen only in
+ * upload/download.  A handle is bound to one device and one CUDA stream and
+ * is not safe for concurrent use from several threads.  Every function
+ * returns MHD_OK (0) or one of the error codes below; mhd_last_error()
+ * gives the message.  Device kernels never spin or trap: numerical failures
+ * (NaN/Inf in the state, a non-positive dt) are recorded in a device error
+ * word that the host reads after each call.
+ */
+#ifndef MHD_GB300_H
+#define MHD_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MHD_OK 0
+#define MHD_ERR_ARG 1          /* invalid argument or unsupported option   */
+#define MHD_ERR_CUDA 2         /* CUDA runtime error (allocation, launch)   */
+#define MHD_ERR_NONFINITE 3    /* NaN or Inf appeared in the state          */
+#define MHD_ERR_DT 4           /* dt <= 0 or not finite ('err at Couran')   */
+#define MHD_ERR_STATE 5        /* call out of order (e.g. no upload yet)    */
+#define MHD_ERR_NO_DEVICE 6    /* no CUDA device / kernels not loadable     */
+
+#define MHD_PREC_FP64 0        /* plain form: every operation in FP64       */
+#define MHD_PREC_FP32 1        /* FP32 reconstruction/flux, FP64 accumulate */
+
+#define MHD_COOL_EXACT 0       /* explicit step or IMC bisection (reference) */
+#define MHD_COOL_SURROGATE 1   /* MLP surrogate with exact fallback          */
+
+typedef struct mhd_params {
+  int nx, ny, nz;              /* interior cells (Ncellx, Ncelly, Ncellz)   */
+  double cfl, facdep, tfinal;  /* INPUT3D.DAT rows 13-14                    */
+  int bc[6];                   /* BCx1,BCx2,BCy1,BCy2,BCz1,BCz2: 1 = free
+                                  (zero-gradient), 3 = periodic              */
+  double pmin, pmax, rmin;     /* floors, MCF3DSGincfca3.f90:173-176        */
+  double kb, kcond;            /* 8.63359, 1.6384e-2                        */
+  int ifthrm;                  /* 2: KI source and thermal dt limit; 0: off */
+  int dissip;                  /* 1: DISSIP edge damping after each step    */
+  int precision;               /* MHD_PREC_FP64 or MHD_PREC_FP32            */
+  int cooling;                 /* MHD_COOL_EXACT or MHD_COOL_SURROGATE      */
+  int device;                  /* CUDA device ordinal                       */
+} mhd_params;
+
+typedef struct mhd_diag {
+  double mass, momentum[3], energy;   /* sums over interior cells × volume  */
+  double divb_max;                    /* max |div B| over interior cells    */
+  double time;
+  long long steps;
+  long long imc_cells;                /* cells that took the implicit path  */
+  long long surrogate_cells;          /* cells solved by the surrogate      */
+  long long fallback_cells;           /* surrogate cells sent back to IMC   */
+} mhd_diag;
+
+typedef struct mhd_handle mhd_handle;
+
+/* Allocates the resident state for p on p->device.  No data yet. */
+int mhd_create(const mhd_params *p, mhd_handle **out);
+int mhd_destroy(mhd_handle *h);
+
+/* INITIA/restart read: copies the full arrays (ghosts included) and runs
+ * CC(4) (MCF3DSGincfca3.f90:470) to form the cell-centred field. */
+int mhd_upload(mhd_handle *h, const double *U, const double *species,
+               const double *x, const double *dx, const double *y,
+               const double *dy, const double *z, const double *dz);
+/* SAVEU: copies U and species back (bcc may be NULL; else 3 blocks). */
+int mhd_download(mhd_handle *h, double *U, double *species, double *bcc);
+
+/* Couran + Stblty + min (EVOLVE:569-599 for the whole grid).  *dt is
+ * min(tfinal, CFL*tCFL, tLMT); *st is 1 (FastSpd) or 2 (Conduct). */
+int mhd_timestep(mhd_handle *h, double *dt, int *st);
+int mhd_source(mhd_handle *h, double dt);             /* SOURCE(dt)        */
+int mhd_sweep(mhd_handle *h, int dir, double dt);     /* dir 0=x,1=y,2=z   */
+int mhd_ct(mhd_handle *h, double dt);
+int mhd_dissip(mhd_handle *h);
+/* SOURCE(dt/2), three sweeps in the order ifEVO (1..6, :611-634), CT,
+ * SOURCE(dt/2), DISSIP, time += dt.  Advances ifEVO like the reference. */
+int mhd_advance(mhd_handle *h, double dt);
+/* Full iteration: dt from mhd_timestep clipped at tfinal and tsave
+ * (:603-604), then mhd_advance.  Returns the dt used and the limiter. */
+int mhd_step(mhd_handle *h, double tsave, double *dt, int *st);
+/* nsteps iterations of mhd_step; stops early at tfinal or tsave. */
+int mhd_evolve(mhd_handle *h, int nsteps, double tsave, int *steps_done);
+
+int mhd_get_time(mhd_handle *h, double *time, int *ifevo);
+int mhd_set_time(mhd_handle *h, double time, int ifevo);
+int mhd_diagnostics(mhd_handle *h, mhd_diag *out);
+/* Blocks until all work queued on the handle's stream has finished. */
+int mhd_synchronize(mhd_handle *h);
+/* Use an existing CUDA stream (cudaStream_t passed as void*); NULL = own. */
+int mhd_set_stream(mhd_handle *h, void *stream);
+/* Copies the last error message (NUL-terminated) into buf. */
+int mhd_last_error(mhd_handle *h, char *buf, int len);
+/* Number of kernels launched by this handle since creation. */
+long long mhd_kernel_launches(mhd_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MHD_GB300_H */

@@ -1,0 +1,952 @@
+// oracle/mhd3d.cpp — TEST INFRASTRUCTURE ONLY (the oracle; never shipped,
+// never on the product path).
+//
+// CPU restatement of one time step of the reference's 3D ideal-MHD code
+// 3DMHD-CfCA/MCF3DSGincfca3.f90 (EVOLVE:562-657) with the Koyama–Inutsuka
+// cooling function spliced in from KIcool/1DMHDwCC3.f90:1148-1173 and the
+// free (outflow) x boundary taken from
+// 3DMHD-feedback/MCF3DSGincfca3-feedback.f90:1217-1221 and siblings.
+//
+// The reference runs one MPI rank per 64^3 block; here the whole grid is one
+// block and every MPI_SENDRECV halo exchange becomes the ghost copy it
+// implies: a periodic wrap (the reference's neighbour ring, :78-83) or the
+// zero-gradient copy of the free boundary.  The exchanges are issued at the
+// same points, on the same fields and directions, as BC_MPI / BC_MPI_OT
+// calls in the reference, so every ghost value read has the same meaning
+// (including the reference's habit of reading a ghost that was filled
+// before the interior changed).  Loops, operation order and floating-point
+// expressions follow the Fortran line by line; build with -ffp-contract=off.
+// exp/log10/10**x come from detmath.h, shared with the GPU kernels.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../code_tohoku_gb300/csrc/detmath.h"
+
+namespace {
+
+using detmath::fmax2;
+using detmath::fmin2;
+using detmath::fsign;
+
+// species slots, in the order of the reference's VLIMIT_OT / REMAP G(:,1..8)
+enum { SH = 0, SP = 1, SH2 = 2, SHE = 3, SHEP = 4, SC = 5, SCP = 6, SCO = 7 };
+
+struct Params {
+  int nx, ny, nz;
+  double CFL, facdep, tfinal;
+  int bc[6];          // BCx1,BCx2,BCy1,BCy2,BCz1,BCz2: 1 = free, otherwise periodic
+  double pmin, pmax, rmin;
+  double kb, Kcond;
+  int ifthrm;         // 2: KI source + thermal dt limit; 0: neither
+  int dissip;         // 1: DISSIP edge damping (MCF3DSGincfca3.f90:3143-3173)
+  int nspecies;       // 8 (all species carried)
+};
+
+struct Mhd3D {
+  Params P;
+  int Nx, Ny, Nz, sx, sy, sz;   // sx = Nx+4 ...
+  size_t ncell;
+  double time = 0;
+  int ifEVO = 1;
+  std::vector<double> xc[3], dxc[3];   // x(-1..N+2), dx(-1..N+2) per direction
+  std::vector<double> U[9];            // fields 1..8
+  std::vector<double> sp[8];
+  std::vector<double> Bcc[4], Blg[3], Vfc[4], EMF[4];
+  std::vector<double> dnc, xlag, dxlagM;
+  double ndmin[8];
+
+  size_t id(int i, int j, int k) const {
+    return (size_t)(i + 1) + (size_t)sx * ((size_t)(j + 1) + (size_t)sy * (size_t)(k + 1));
+  }
+  double &X(int d, int i) { return xc[d][i + 1]; }
+  double &DX(int d, int i) { return dxc[d][i + 1]; }
+  int Nd(int d) const { return d == 0 ? Nx : (d == 1 ? Ny : Nz); }
+
+  void init(const Params &p) {
+    P = p;
+    Nx = p.nx; Ny = p.ny; Nz = p.nz;
+    sx = Nx + 4; sy = Ny + 4; sz = Nz + 4;
+    ncell = (size_t)sx * sy * sz;
+    for (int f = 1; f <= 8; f++) U[f].assign(ncell, 0.0);
+    for (int s = 0; s < 8; s++) sp[s].assign(ncell, 0.0);
+    for (int c = 1; c <= 3; c++) { Bcc[c].assign(ncell, 0.0); Vfc[c].assign(ncell, 0.0); EMF[c].assign(ncell, 0.0); }
+    for (int c = 1; c <= 2; c++) Blg[c].assign(ncell, 0.0);
+    dnc.assign(ncell, 0.0); xlag.assign(ncell, 0.0); dxlagM.assign(ncell, 0.0);
+    for (int d = 0; d < 3; d++) { xc[d].assign(Nd(d) + 4, 0.0); dxc[d].assign(Nd(d) + 4, 0.0); }
+    // MCF3DSGincfca3.f90:178-179
+    ndmin[SH] = p.rmin * 0.91; ndmin[SP] = 1e-20; ndmin[SH2] = 1e-20; ndmin[SHE] = p.rmin * 0.09;
+    ndmin[SHEP] = 1e-20; ndmin[SCP] = 1e-20; ndmin[SC] = 1e-20; ndmin[SCO] = 1e-20;
+  }
+
+  // ---------------------------------------------------------------- ghosts
+  // One direction of BC_MPI / BC_MPI_OT for one array: periodic wrap (the
+  // reference's neighbour ring) or, for BC=1, the free-boundary copy of the
+  // first/last interior cell (…-feedback.f90:1217-1221, 1261-1265).  The
+  // exchange covers every index of the two other directions, ghosts
+  // included, like the MPI_TYPE_VECTOR strides (:812, :892, :910).
+  // 'interior_only_transverse' reproduces the species copy of the free
+  // boundary, which the reference restricts to JY,KZ = 1..N (:1057).
+  void fill_dir(std::vector<double> &a, int d, int nol, bool species = false) {
+    int N = Nd(d);
+    int b1 = P.bc[2 * d], b2 = P.bc[2 * d + 1];
+    int ext[3] = {sx, sy, sz};
+    int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+    for (int q2 = -1; q2 < ext[o2] - 1; q2++)
+      for (int q1 = -1; q1 < ext[o1] - 1; q1++) {
+        int c[3];
+        c[o1] = q1; c[o2] = q2;
+        auto at = [&](int i) -> double & {
+          c[d] = i;
+          return a[id(c[0], c[1], c[2])];
+        };
+        bool tr_in = (q1 >= 1 && q1 <= Nd(o1) && q2 >= 1 && q2 <= Nd(o2));
+        // left side (periodic part first, as the SENDRECV happens first)
+        for (int g = 1 - nol; g <= 0; g++) at(g) = at(g + N);
+        if (b1 == 1 && (!species || tr_in))
+          for (int g = 1 - nol; g <= 0; g++) at(g) = at(1);
+        for (int g = N + 1; g <= N + nol; g++) at(g) = at(g - N);
+        if (b2 == 1 && (!species || tr_in))
+          for (int g = N + 1; g <= N + nol; g++) at(g) = at(N);
+      }
+  }
+  // dirs: bit0 = x, bit1 = y, bit2 = z, applied in x, y, z order
+  void fill(std::vector<double> &a, int dirs, int nol, bool species = false) {
+    for (int d = 0; d < 3; d++)
+      if (dirs & (1 << d)) fill_dir(a, d, nol, species);
+  }
+  void fill_species(int dirs, int nol) {
+    for (int s = 0; s < 8; s++) fill(sp[s], dirs, nol, true);
+  }
+
+  // ---------------------------------------------------------------- helpers
+  double gam_of(size_t c) {
+    double g = 3.0 * (sp[SH][c] + sp[SP][c] + sp[SHE][c] + sp[SHEP][c]) + 5.0 * sp[SH2][c];
+    return (5.0 * (sp[SH][c] + sp[SP][c] + sp[SHE][c] + sp[SHEP][c]) + 7.0 * sp[SH2][c]) / g;
+  }
+  double gmi1_of(size_t c) {
+    double g = 3.0 * (sp[SH][c] + sp[SP][c] + sp[SHE][c] + sp[SHEP][c]) + 5.0 * sp[SH2][c];
+    return (2.0 * (sp[SH][c] + sp[SP][c] + sp[SHE][c] + sp[SHEP][c]) + 2.0 * sp[SH2][c]) / g;
+  }
+  static double posmask(double q, double fallback) {
+    return (0.5 - fsign(0.5, -q)) * q + (0.5 + fsign(0.5, -q)) * fallback;
+  }
+  // index of sweep position i on pencil (Mnum, Lnum) for direction d
+  // (MCF3DSGincfca3.f90:1370-1372)
+  size_t pidx(int d, int i, int Mnum, int Lnum) const {
+    if (d == 0) return id(i, Mnum, Lnum);
+    if (d == 1) return id(Lnum, i, Mnum);
+    return id(Mnum, Lnum, i);
+  }
+
+  // VLIMIT, one field on one pencil (MCF3DSGincfca3.f90:1692-1804) for
+  // i = 0..N+1; q(i) reads the limited field, T uses U(:,5)/U(:,1) in place.
+  template <class Q>
+  void vlimit(int d, int Mnum, int Lnum, const double *dxx, Q q, double *grd) {
+    const double eps = 1e-10;
+    int N = Nd(d);
+    for (int i = 0; i <= N + 1; i++) {
+      double qp = q(i + 1), q0 = q(i), qm = q(i - 1);
+      double delp = qp - q0;
+      double delm = q0 - qm;
+      double flmt = fmax2(0.0, (2.0 * delp * delm + eps) / (delp * delp + delm * delm + eps));
+      double g = flmt * (qp - qm) / (dxx[i + 1] + 0.5 * dxx[i] + 0.5 * dxx[i + 2]);
+      size_t c = pidx(d, i, Mnum, Lnum);
+      double T = 1.27 * U[5][c] / (P.kb * U[1][c]);
+      delp = 2.0 * delp / (dxx[i + 1] + dxx[i + 2]);
+      delm = 2.0 * delm / (dxx[i + 1] + dxx[i]);
+      double gmm = (0.5 + fsign(0.5, delp * delm)) * fsign(1.0, delp) *
+                   fmin2(std::fabs(delp), std::fabs(delm));
+      grd[i + 1] = g * (0.5 - fsign(0.5, T - 3.0)) + gmm * (0.5 + fsign(0.5, T - 3.0));
+    }
+  }
+
+  static void CHAREQ(double QL1, double QL2, double QL3, double QR1, double QR2, double QR3,
+                     double &Bay, double &Vay) {
+    double vyp = QL1, vym = QR1, Byp = QL2, Bym = QR2;
+    double sqdyp = std::sqrt(QL3), sqdym = std::sqrt(QR3);
+    Vay = (sqdyp * vyp + sqdym * vym + Bym - Byp) / (sqdyp + sqdym);
+    Bay = (sqdyp * sqdym * (vym - vyp) + sqdyp * Bym + sqdym * Byp) / (sqdyp + sqdym);
+  }
+
+  // ------------------------------------------------------------ the sweep
+  // MHD (MCF3DSGincfca3.f90:1264-1324) → RHS, MOC, REMAP, wrapper
+  void MHD(int d, double dt) {
+    int N = Nd(d);
+    int Ncm = (d == 0) ? Ny : (d == 1 ? Nz : Nx);
+    int Ncl = (d == 0) ? Nz : (d == 1 ? Nx : Ny);
+    int dirbit = 1 << d;
+    const double *xelr = xc[d].data();      // xelr(i) at [i+1]
+    const double *dxelr = dxc[d].data();
+    // xlag = xelr along the sweep (:1275-1278)
+    for (int k = -1; k <= Nz + 2; k++)
+      for (int j = -1; j <= Ny + 2; j++)
+        for (int i = -1; i <= Nx + 2; i++) {
+          int ix = (d == 0) ? i : (d == 1 ? j : k);
+          xlag[id(i, j, k)] = xelr[ix + 1];
+        }
+    int VN = 2 + d;                          // normal velocity field
+    int BT1 = (d == 0) ? 2 : (d == 1 ? 3 : 1);
+    int BT2 = (d == 0) ? 3 : (d == 1 ? 1 : 2);
+    int VT1 = (d == 0) ? 3 : (d == 1 ? 4 : 2);
+    int VT2 = (d == 0) ? 4 : (d == 1 ? 2 : 3);
+    int BN = 6 + d;
+
+    // ===== RHS (:1330-1467)
+    fill(U[1], dirbit, 2); fill(U[VN], dirbit, 2); fill(U[5], dirbit, 2);   // BC_MPI(2,1) :1355
+    fill_species(dirbit, 2);                                                  // :1357
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int Lnum = 1; Lnum <= Ncl; Lnum++)
+      for (int Mnum = 1; Mnum <= Ncm; Mnum++) {
+        std::vector<double> g1(N + 4), gVN(N + 4), g5(N + 4), gB1(N + 4), gB2(N + 4);
+        std::vector<double> Pa(N + 4), Va(N + 4), dm(N + 4);
+        auto P_ = [&](int i) { return pidx(d, i, Mnum, Lnum); };
+        vlimit(d, Mnum, Lnum, dxelr, [&](int i) { return U[1][P_(i)]; }, g1.data());
+        vlimit(d, Mnum, Lnum, dxelr, [&](int i) { return U[VN][P_(i)]; }, gVN.data());
+        vlimit(d, Mnum, Lnum, dxelr, [&](int i) { return U[5][P_(i)]; }, g5.data());
+        vlimit(d, Mnum, Lnum, dxelr, [&](int i) { return Bcc[BT1][P_(i)]; }, gB1.data());
+        vlimit(d, Mnum, Lnum, dxelr, [&](int i) { return Bcc[BT2][P_(i)]; }, gB2.data());
+        // gamma factors are per interface (module variables in the reference)
+        double lg1, lg2, lg3, lp1, lp3;
+        for (int i = 0; i <= N; i++) {
+          size_t a = P_(i), b = P_(i + 1);
+          double gam = gam_of(a);
+          double cm = std::sqrt((gam * U[5][a] + Bcc[BT1][a] * Bcc[BT1][a] + Bcc[BT2][a] * Bcc[BT2][a]) / U[1][a]);
+          double depend1 = 0.5 * (dxelr[i + 1] - cm * dt) * P.facdep;
+          depend1 = fmax2(0.0, depend1);
+          gam = gam_of(b);
+          cm = std::sqrt((gam * U[5][b] + Bcc[BT1][b] * Bcc[BT1][b] + Bcc[BT2][b] * Bcc[BT2][b]) / U[1][b]);
+          double depend2 = 0.5 * (dxelr[i + 2] - cm * dt) * P.facdep;
+          depend2 = fmax2(0.0, depend2);
+          double QL1 = U[1][a] + depend1 * g1[i + 1];
+          QL1 = posmask(QL1, U[1][a]);
+          double QR1 = U[1][b] - depend2 * g1[i + 2];
+          QR1 = posmask(QR1, U[1][b]);
+          double QL2 = U[VN][a] + depend1 * gVN[i + 1];
+          double QR2 = U[VN][b] - depend2 * gVN[i + 2];
+          double QL3 = U[5][a] + depend1 * g5[i + 1];
+          QL3 = posmask(QL3, U[5][a]);
+          double QR3 = U[5][b] - depend2 * g5[i + 2];
+          QR3 = posmask(QR3, U[5][b]);
+          double l1 = Bcc[BT1][a] + depend1 * gB1[i + 1], l2 = Bcc[BT2][a] + depend1 * gB2[i + 1];
+          double QL4 = l1 * l1 + l2 * l2;
+          double r1 = Bcc[BT1][b] - depend2 * gB1[i + 2], r2 = Bcc[BT2][b] - depend2 * gB2[i + 2];
+          double QR4 = r1 * r1 + r2 * r2;
+          double ndHm = 0.5 * (sp[SH][a] + sp[SH][b]), ndpm = 0.5 * (sp[SP][a] + sp[SP][b]);
+          double ndHem = 0.5 * (sp[SHE][a] + sp[SHE][b]), ndHepm = 0.5 * (sp[SHEP][a] + sp[SHEP][b]);
+          double ndH2m = 0.5 * (sp[SH2][a] + sp[SH2][b]);
+          double gamma = (5.0 * (ndHm + ndpm + ndHem + ndHepm) + 7.0 * ndH2m) /
+                         (3.0 * (ndHm + ndpm + ndHem + ndHepm) + 5.0 * ndH2m);
+          lg1 = gamma - 1.0; lg2 = gamma - 2.0; lg3 = gamma - 3.0; lp1 = gamma + 1.0; lp3 = gamma + 3.0;
+          riemann_local(lg1, lg2, lg3, lp1, lp3, QL1, QL2, QL3, QL4, QR1, QR2, QR3, QR4, Pa[i + 1], Va[i + 1]);
+        }
+        for (int i = 0; i <= N; i++) {
+          size_t a = P_(i);
+          dm[i + 1] = dxelr[i + 1] * U[1][a];
+          xlag[a] = xlag[a] + Va[i + 1] * dt;
+        }
+        for (int i = 1; i <= N; i++) {
+          size_t a = P_(i), am = P_(i - 1);
+          double g1c = gmi1_of(a);
+          U[5][a] = U[5][a] / (U[1][a] * g1c) +
+                    0.5 * (U[2][a] * U[2][a] + U[3][a] * U[3][a] + U[4][a] * U[4][a]) +
+                    0.5 * (Bcc[1][a] * Bcc[1][a] + Bcc[2][a] * Bcc[2][a] + Bcc[3][a] * Bcc[3][a]) / U[1][a];
+          U[1][a] = dm[i + 1] / (xlag[a] - xlag[am]);
+          U[VN][a] = U[VN][a] - dt / dm[i + 1] * (Pa[i + 1] - Pa[i]);
+          U[5][a] = U[5][a] - dt / dm[i + 1] * (Pa[i + 1] * Va[i + 1] - Pa[i] * Va[i]);
+          Blg[1][a] = Bcc[BT1][a] * dxelr[i + 1] / (xlag[a] - xlag[am]);
+          Blg[2][a] = Bcc[BT2][a] * dxelr[i + 1] / (xlag[a] - xlag[am]);
+          for (int s = 0; s < 8; s++) sp[s][a] = dxelr[i + 1] * sp[s][a] / (xlag[a] - xlag[am]);
+        }
+        for (int i = 1; i <= N + 1; i++) Vfc[1][P_(i)] = Va[i];   // Va(i-1)
+      }
+
+    // ===== MOC (:1939-2098)
+    fill(U[1], dirbit, 2); fill(U[VT1], dirbit, 2); fill(U[VT2], dirbit, 2); fill(U[BN], dirbit, 2);  // :1960
+    for (int Lnum = 1; Lnum <= Ncl; Lnum++)
+      for (int Mnum = 1; Mnum <= Ncm; Mnum++)
+        for (int i = 1; i <= N; i++)
+          dxlagM[pidx(d, i, Mnum, Lnum)] = xlag[pidx(d, i, Mnum, Lnum)] - xlag[pidx(d, i - 1, Mnum, Lnum)];
+    fill(dxlagM, dirbit, 2); fill(Blg[1], dirbit, 2); fill(Blg[2], dirbit, 2);   // :1974
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int Lnum = 1; Lnum <= Ncl; Lnum++)
+      for (int Mnum = 1; Mnum <= Ncm; Mnum++) {
+        auto P_ = [&](int i) { return pidx(d, i, Mnum, Lnum); };
+        std::vector<double> dxlag(N + 4), g1(N + 4), gT1(N + 4), gT2(N + 4), gL1(N + 4), gL2(N + 4);
+        std::vector<double> Vay(N + 4), Bay(N + 4), Vaz(N + 4), Baz(N + 4);
+        for (int i = -1; i <= N + 2; i++) dxlag[i + 1] = dxlagM[P_(i)];
+        vlimit(d, Mnum, Lnum, dxlag.data(), [&](int i) { return U[1][P_(i)]; }, g1.data());
+        vlimit(d, Mnum, Lnum, dxlag.data(), [&](int i) { return U[VT1][P_(i)]; }, gT1.data());
+        vlimit(d, Mnum, Lnum, dxlag.data(), [&](int i) { return U[VT2][P_(i)]; }, gT2.data());
+        vlimit(d, Mnum, Lnum, dxlag.data(), [&](int i) { return Blg[1][P_(i)]; }, gL1.data());
+        vlimit(d, Mnum, Lnum, dxlag.data(), [&](int i) { return Blg[2][P_(i)]; }, gL2.data());
+        auto DL = [&](int i) { return dxlag[i + 1]; };
+        auto XE = [&](int i) { return xelr[i + 1]; };
+        for (int i = 0; i <= N; i++) {
+          size_t a = P_(i), b = P_(i + 1), c2 = P_(i + 2);
+          double Bnap = U[BN][b] + (xlag[a] - XE(i)) * (U[BN][c2] - U[BN][a]) / (XE(i + 1) - XE(i - 1));
+          double deni = std::sqrt((DL(i) + DL(i + 1)) / (DL(i) * U[1][b] + DL(i + 1) * U[1][a]));
+          double QL11, QR11, QL12, QR12, QL13, QR13, QL21, QR21, QL22, QR22;
+          if (Bnap > 0.0) {
+            double ca = std::fabs(Bnap * deni) * 0.5 * dt;
+            ca = fmin2(DL(i), ca);
+            double depend1 = (0.5 * DL(i) - ca) * P.facdep;
+            ca = std::fabs(Bnap * deni) * 0.5 * dt;
+            ca = fmin2(DL(i + 1), ca);
+            double depend2 = (0.5 * DL(i + 1) - ca) * P.facdep;
+            QL11 = U[VT1][a] + depend1 * gT1[i + 1];
+            QR11 = U[VT1][b] - depend2 * gT1[i + 2];
+            QL12 = Blg[1][a] + depend1 * gL1[i + 1];
+            QR12 = Blg[1][b] - depend2 * gL1[i + 2];
+            QL13 = U[1][a] + depend1 * g1[i + 1];
+            QL13 = posmask(QL13, U[1][a]);
+            QR13 = U[1][b] - depend2 * g1[i + 2];
+            QR13 = posmask(QR13, U[1][b]);
+            QL21 = U[VT2][a] + depend1 * gT2[i + 1];
+            QR21 = U[VT2][b] - depend2 * gT2[i + 2];
+            QL22 = Blg[2][a] + depend1 * gL2[i + 1];
+            QR22 = Blg[2][b] - depend2 * gL2[i + 2];
+          } else {
+            double ca = std::fabs(Bnap * deni) * 0.5 * dt;
+            ca = fmin2(DL(i + 1), ca);
+            double depend1 = (0.5 * DL(i + 1) - ca) * P.facdep;
+            ca = std::fabs(Bnap * deni) * 0.5 * dt;
+            ca = fmin2(DL(i), ca);
+            double depend2 = (0.5 * DL(i) - ca) * P.facdep;
+            QL11 = U[VT1][b] - depend1 * gT1[i + 2];
+            QR11 = U[VT1][a] + depend2 * gT1[i + 1];
+            QL12 = Blg[1][b] - depend1 * gL1[i + 2];
+            QR12 = Blg[1][a] + depend2 * gL1[i + 1];
+            QL13 = U[1][b] - depend1 * g1[i + 2];
+            QL13 = posmask(QL13, U[1][b]);
+            QR13 = U[1][a] + depend2 * g1[i + 1];
+            QR13 = posmask(QR13, U[1][a]);
+            QL21 = U[VT2][b] - depend1 * gT2[i + 2];
+            QR21 = U[VT2][a] + depend2 * gT2[i + 1];
+            QL22 = Blg[2][b] - depend1 * gL2[i + 2];
+            QR22 = Blg[2][a] + depend2 * gL2[i + 1];
+          }
+          CHAREQ(QL11, QL12, QL13, QR11, QR12, QR13, Bay[i + 1], Vay[i + 1]);
+          CHAREQ(QL21, QL22, QL13, QR21, QR22, QR13, Baz[i + 1], Vaz[i + 1]);
+        }
+        for (int i = 1; i <= N; i++) {
+          size_t am = P_(i - 1), a = P_(i), b = P_(i + 1), c2 = P_(i + 2);
+          double Bnap = U[BN][b] + (xlag[a] - XE(i)) * (U[BN][c2] - U[BN][a]) / (XE(i + 1) - XE(i - 1));
+          double Bnam = U[BN][a] + (xlag[am] - XE(i - 1)) * (U[BN][b] - U[BN][am]) / (XE(i) - XE(i - 2));
+          double Vnap = Vfc[1][b];
+          double Vnam = Vfc[1][a];
+          U[VN][a] = U[VN][a] * U[1][a] + dt / DL(i) * 0.5 * (Bnap * Bnap - Bnam * Bnam);
+          U[VT1][a] = U[VT1][a] * U[1][a] + dt / DL(i) * (Bnap * Bay[i + 1] - Bnam * Bay[i]);
+          U[VT2][a] = U[VT2][a] * U[1][a] + dt / DL(i) * (Bnap * Baz[i + 1] - Bnam * Baz[i]);
+          U[5][a] = U[5][a] * U[1][a] + dt / DL(i) *
+                    ((0.5 * Bnap * Vnap + Bay[i + 1] * Vay[i + 1] + Baz[i + 1] * Vaz[i + 1]) * Bnap -
+                     (0.5 * Bnam * Vnam + Bay[i] * Vay[i] + Baz[i] * Vaz[i]) * Bnam);
+          Blg[1][a] = Blg[1][a] + dt / DL(i) * (Bnap * Vay[i + 1] - Bnam * Vay[i]);
+          Blg[2][a] = Blg[2][a] + dt / DL(i) * (Bnap * Vaz[i + 1] - Bnam * Vaz[i]);
+        }
+      }
+
+    // ===== REMAP (:1556-1686)
+    fill(Blg[1], dirbit, 2); fill(Blg[2], dirbit, 2);                         // :1572 (mode 2)
+    for (int f = 1; f <= 5; f++) fill(U[f], dirbit, 2);                       // :1581 (mode 2)
+    fill_species(dirbit, 2);                                                  // :1594
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int Lnum = 1; Lnum <= Ncl; Lnum++)
+      for (int Mnum = 1; Mnum <= Ncm; Mnum++) {
+        auto P_ = [&](int i) { return pidx(d, i, Mnum, Lnum); };
+        std::vector<double> dxlag(N + 4);
+        for (int i = -1; i <= N + 2; i++) dxlag[i + 1] = dxlagM[P_(i)];
+        // columns: U1..U5, Blg1, Blg2, then the 8 species
+        std::vector<double> *cols[15] = {&U[1], &U[2], &U[3], &U[4], &U[5], &Blg[1], &Blg[2],
+                                         &sp[SH], &sp[SP], &sp[SH2], &sp[SHE], &sp[SHEP], &sp[SC], &sp[SCP], &sp[SCO]};
+        std::vector<std::vector<double>> grd(15, std::vector<double>(N + 4)), F(15, std::vector<double>(N + 4));
+        for (int c = 0; c < 15; c++)
+          vlimit(d, Mnum, Lnum, dxlag.data(), [&](int i) { return (*cols[c])[P_(i)]; }, grd[c].data());
+        for (int i = 0; i <= N; i++) {
+          size_t a = P_(i), b = P_(i + 1);
+          double vadt = Vfc[1][b] * dt;
+          if (vadt <= 0.0) {
+            double depend = 0.5 * (dxlag[i + 2] + vadt) * P.facdep;
+            for (int c = 0; c < 15; c++) F[c][i + 1] = -vadt * ((*cols[c])[b] - depend * grd[c][i + 2]);
+          } else {
+            double depend = 0.5 * (dxlag[i + 1] - vadt) * P.facdep;
+            for (int c = 0; c < 15; c++) F[c][i + 1] = -vadt * ((*cols[c])[a] + depend * grd[c][i + 1]);
+          }
+        }
+        for (int i = 1; i <= N; i++) {
+          size_t a = P_(i);
+          for (int c = 0; c < 15; c++)
+            (*cols[c])[a] = ((*cols[c])[a] * dxlag[i + 1] + F[c][i + 1] - F[c][i]) / (xelr[i + 1] - xelr[i]);
+        }
+      }
+
+    // ===== wrapper (:1291-1321)
+    int iBcc = d + 1;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny; j++)
+        for (int i = 1; i <= Nx; i++) {
+          size_t a = id(i, j, k);
+          U[1][a] = fmax2(1.27 * P.rmin, U[1][a]);
+          double invd = 1.0 / U[1][a];
+          U[2][a] = U[2][a] * invd;
+          U[3][a] = U[3][a] * invd;
+          U[4][a] = U[4][a] * invd;
+          double g1c = gmi1_of(a);
+          double ekin = 0.5 * (U[2][a] * U[2][a] + U[3][a] * U[3][a] + U[4][a] * U[4][a]) * U[1][a];
+          double emag = 0.5 * (Bcc[iBcc][a] * Bcc[iBcc][a] + Blg[1][a] * Blg[1][a] + Blg[2][a] * Blg[2][a]);
+          U[5][a] = (U[5][a] - ekin - emag) * g1c;
+          U[5][a] = fmax2(P.pmin, U[5][a]);
+          U[5][a] = fmin2(P.pmax, U[5][a]);
+          for (int s = 0; s < 8; s++) sp[s][a] = fmax2(ndmin[s], sp[s][a]);
+        }
+  }
+
+  // RIEMAN with gamma factors passed in (the reference keeps them in module
+  // variables; passing them keeps the OpenMP pencil loop race-free).
+  static void riemann_local(double g1, double g2, double g3, double p1, double p3, double uLi1,
+                            double uLi2, double uLi3, double uLi4, double uRi1, double uRi2,
+                            double uRi3, double uRi4, double &Pai, double &Vai) {
+    double D1i = uLi1, V1i = uLi2, P1i = uLi3, B1i = 0.5 * uLi4;
+    double D2i = uRi1, V2i = uRi2, P2i = uRi3, B2i = 0.5 * uRi4;
+    P1i = P1i + B1i;
+    P2i = P2i + B2i;
+    double GP1i = g1 * P1i, GP2i = g1 * P2i;
+    double GP1B1i = g3 * P1i - g2 * B1i * 2.0;
+    double GP2B2i = g3 * P2i - g2 * B2i * 2.0;
+    Pai = (P1i + P2i) * 0.5;
+    double qM1i = 0, qM2i = 0;
+    for (int loop = 0; loop < 4; loop++) {   // :1500-1546, four unrolled copies
+      double pp1i = p3 * Pai + GP1B1i;
+      double qM1sqi = pp1i + std::sqrt(pp1i * pp1i - 8.0 * (Pai - P1i) * (p1 * Pai + GP1i));
+      qM1i = std::sqrt(qM1sqi * D1i) * 0.5;
+      double pp2i = p3 * Pai + GP2B2i;
+      double qM2sqi = pp2i + std::sqrt(pp2i * pp2i - 8.0 * (Pai - P2i) * (p1 * Pai + GP2i));
+      qM2i = std::sqrt(qM2sqi * D2i) * 0.5;
+      double PaOLDi = Pai;
+      Pai = qM2i * P1i + qM1i * P2i + qM2i * qM1i * (V1i - V2i);
+      Pai = Pai / (qM2i + qM1i);
+      if (Pai <= 0.0) Pai = 0.1 * PaOLDi;
+    }
+    Vai = qM1i * V1i + qM2i * V2i + P1i - P2i;
+    Vai = Vai / (qM2i + qM1i);
+  }
+
+  // ------------------------------------------------------------- CT
+  // CC(mode) (MCF3DSGincfca3.f90:2115-2183) and CCT (:2186-2445)
+  void CC1() {
+    fill(U[2], 1, 2); fill(U[7], 1, 2); fill(U[8], 1, 2);     // :2123
+    fill(U[3], 2, 2); fill(U[6], 2, 2); fill(U[8], 2, 2);     // :2124
+    fill(U[4], 4, 2); fill(U[6], 4, 2); fill(U[7], 4, 2);     // :2125
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny; j++)
+        for (int i = 1; i <= Nx + 1; i++)
+          Vfc[1][id(i, j, k)] = (DX(0, i - 1) * U[2][id(i, j, k)] + DX(0, i) * U[2][id(i - 1, j, k)]) /
+                                (DX(0, i - 1) + DX(0, i));
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny + 1; j++)
+        for (int i = 1; i <= Nx; i++)
+          Vfc[2][id(i, j, k)] = (DX(1, j - 1) * U[3][id(i, j, k)] + DX(1, j) * U[3][id(i, j - 1, k)]) /
+                                (DX(1, j - 1) + DX(1, j));
+    for (int k = 1; k <= Nz + 1; k++)
+      for (int j = 1; j <= Ny; j++)
+        for (int i = 1; i <= Nx; i++)
+          Vfc[3][id(i, j, k)] = (DX(2, k - 1) * U[4][id(i, j, k)] + DX(2, k) * U[4][id(i, j, k - 1)]) /
+                                (DX(2, k - 1) + DX(2, k));
+    // BC_MPI_OT(2,1) with N_MPI(13)=1 and iwx=iwy=iwz=1 (:2135, :1018-1036,
+    // :1127-1135, :1205-1213): x moves Vfc2,3; y moves Vfc1,3; z moves Vfc1,2
+    fill_dir(Vfc[2], 0, 2); fill_dir(Vfc[3], 0, 2);
+    fill_dir(Vfc[1], 1, 2); fill_dir(Vfc[3], 1, 2);
+    fill_dir(Vfc[1], 2, 2); fill_dir(Vfc[2], 2, 2);
+    fill(U[5], 7, 2);                                           // :2137
+  }
+
+  // VLIMIT on a face array (branches 14-16, 6-8) along direction d for the
+  // pencil through (c0,c1,c2) — returns grd at sweep positions 0..N+1.
+  // The T switch reads U(:,5)/U(:,1) at the cell of the same index.
+  void vlimit_line(int d, int i0, int j0, int k0, const double *dxx, const std::vector<double> &q,
+                   std::vector<double> &grd) {
+    int N = Nd(d);
+    const double eps = 1e-10;
+    auto at = [&](int i) {
+      int c[3] = {i0, j0, k0};
+      c[d] = i;
+      return id(c[0], c[1], c[2]);
+    };
+    for (int i = 0; i <= N + 1; i++) {
+      double qp = q[at(i + 1)], q0 = q[at(i)], qm = q[at(i - 1)];
+      double delp = qp - q0;
+      double delm = q0 - qm;
+      double flmt = fmax2(0.0, (2.0 * delp * delm + eps) / (delp * delp + delm * delm + eps));
+      double g = flmt * (qp - qm) / (dxx[i + 1] + 0.5 * dxx[i] + 0.5 * dxx[i + 2]);
+      size_t c = at(i);
+      double T = 1.27 * U[5][c] / (P.kb * U[1][c]);
+      delp = 2.0 * delp / (dxx[i + 1] + dxx[i + 2]);
+      delm = 2.0 * delm / (dxx[i + 1] + dxx[i]);
+      double gmm = (0.5 + fsign(0.5, delp * delm)) * fsign(1.0, delp) *
+                   fmin2(std::fabs(delp), std::fabs(delm));
+      grd[i + 1] = g * (0.5 - fsign(0.5, T - 3.0)) + gmm * (0.5 + fsign(0.5, T - 3.0));
+    }
+  }
+
+  // CC(2) + CCT for one edge direction e (0: Ez from x/y, 1: Ex from y/z,
+  // 2: Ey from z/x), :2140-2157 and :2186-2445.
+  void CCT(int e, double dt) {
+    if (e == 0) fill(U[1], 7, 2);   // :2142, only in the iwx branch
+    // dnc, edge density
+    if (e == 0) {
+      for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny + 1; j++) for (int i = 1; i <= Nx + 1; i++)
+        dnc[id(i, j, k)] = 0.25 * (U[1][id(i, j, k)] + U[1][id(i - 1, j, k)] + U[1][id(i, j - 1, k)] + U[1][id(i - 1, j - 1, k)]);
+    } else if (e == 1) {
+      for (int k = 1; k <= Nz + 1; k++) for (int j = 1; j <= Ny + 1; j++) for (int i = 1; i <= Nx; i++)
+        dnc[id(i, j, k)] = 0.25 * (U[1][id(i, j, k)] + U[1][id(i, j - 1, k)] + U[1][id(i, j, k - 1)] + U[1][id(i, j - 1, k - 1)]);
+    } else {
+      for (int k = 1; k <= Nz + 1; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx + 1; i++)
+        dnc[id(i, j, k)] = 0.25 * (U[1][id(i, j, k)] + U[1][id(i - 1, j, k)] + U[1][id(i, j, k - 1)] + U[1][id(i - 1, j, k - 1)]);
+    }
+    // local "x" (a) and "y" (b) directions of the edge, velocities and fields
+    int da = e, db = (e + 1) % 3;
+    int Vx = 1 + da, Vy = 1 + db, Bx = 6 + da, By = 6 + db;
+    const double *dxe = dxc[da].data(), *dye = dxc[db].data();
+    // dQ(:,1) = slope of Vfc(Vx) along b, dQ(:,3) = slope of U(Bx) along b,
+    // dQ(:,2) = slope of Vfc(Vy) along a, dQ(:,4) = slope of U(By) along a
+    std::vector<double> dQ1(ncell, 0.0), dQ2(ncell, 0.0), dQ3(ncell, 0.0), dQ4(ncell, 0.0);
+    int Na = Nd(da), Nb = Nd(db), dc = (e + 2) % 3, Nc = Nd(dc);
+    // slopes along a: positions a=0..Na+1, b=1..Nb+1, c=1..Nc  (:2206-2213 etc.)
+    for (int cc = 1; cc <= Nc; cc++)
+      for (int bb = 1; bb <= Nb + 1; bb++) {
+        int c3[3];
+        c3[db] = bb; c3[dc] = cc; c3[da] = 0;
+        std::vector<double> gv(Na + 4), gb(Na + 4);
+        vlimit_line(da, c3[0], c3[1], c3[2], dxe, Vfc[Vy], gv);
+        vlimit_line(da, c3[0], c3[1], c3[2], dxe, U[By], gb);
+        for (int aa = 0; aa <= Na + 1; aa++) {
+          c3[da] = aa;
+          size_t p = id(c3[0], c3[1], c3[2]);
+          dQ2[p] = gv[aa + 1];
+          dQ4[p] = gb[aa + 1];
+        }
+      }
+    // slopes along b: positions a=1..Na+1, b=0..Nb+1, c=1..Nc (:2215-2222 etc.)
+    for (int cc = 1; cc <= Nc; cc++)
+      for (int aa = 1; aa <= Na + 1; aa++) {
+        int c3[3];
+        c3[da] = aa; c3[dc] = cc; c3[db] = 0;
+        std::vector<double> gv(Nb + 4), gb(Nb + 4);
+        vlimit_line(db, c3[0], c3[1], c3[2], dye, Vfc[Vx], gv);
+        vlimit_line(db, c3[0], c3[1], c3[2], dye, U[Bx], gb);
+        for (int bb = 0; bb <= Nb + 1; bb++) {
+          c3[db] = bb;
+          size_t p = id(c3[0], c3[1], c3[2]);
+          dQ1[p] = gv[bb + 1];
+          dQ3[p] = gb[bb + 1];
+        }
+      }
+    double facm = P.facdep * 0.5;
+    int Ez = (e == 0) ? 3 : (e == 1 ? 1 : 2);
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int cc = 1; cc <= Nc; cc++)
+      for (int bb = 1; bb <= Nb + 1; bb++)
+        for (int aa = 1; aa <= Na + 1; aa++) {
+          auto pos = [&](int a_, int b_) {
+            int c3[3];
+            c3[da] = a_; c3[db] = b_; c3[dc] = cc;
+            return id(c3[0], c3[1], c3[2]);
+          };
+          size_t p0 = pos(aa, bb);
+          double dsqinv = 1.0 / std::sqrt(dnc[p0]);
+          double a1p, a1m, da1p, da1m, a2m, a2p, da2m, da2p;
+          auto load1 = [&](size_t p) {
+            a1p = Vfc[Vx][p] + U[Bx][p] * dsqinv;
+            da1p = (dQ1[p] + dQ3[p] * dsqinv) * facm;
+            a1m = Vfc[Vx][p] - U[Bx][p] * dsqinv;
+            da1m = (dQ1[p] - dQ3[p] * dsqinv) * facm;
+          };
+          auto load2 = [&](size_t p) {
+            a2m = Vfc[Vy][p] - U[By][p] * dsqinv;
+            da2m = (dQ2[p] - dQ4[p] * dsqinv) * facm;
+            a2p = Vfc[Vy][p] + U[By][p] * dsqinv;
+            da2p = (dQ2[p] + dQ4[p] * dsqinv) * facm;
+          };
+          double dxm = dxe[aa], dx0 = dxe[aa + 1], dym = dye[bb], dy0 = dye[bb + 1];
+          double S1, S2;
+          // C1 > 0, C2 > 0
+          S1 = 1.0; S2 = 1.0;
+          load1(pos(aa, bb - 1));
+          load2(pos(aa - 1, bb));
+          double C1pLL = a1p + da1p * dym * S1 - da1p * (a2m + da2m * dxm * S2) * dt;
+          C1pLL = C1pLL / (1.0 - da1p * da2m * dt * dt);
+          double C2mLL = a2m + da2m * dxm * S2 - da2m * (a1p + da1p * dym * S1) * dt;
+          C2mLL = C2mLL / (1.0 - da1p * da2m * dt * dt);
+          double C1mLL = a1m + da1m * dym * S1 - da1m * (a2p + da2p * dxm * S2) * dt;
+          C1mLL = C1mLL / (1.0 - da1m * da2p * dt * dt);
+          double C2pLL = a2p + da2p * dxm * S2 - da2p * (a1m + da1m * dym * S1) * dt;
+          C2pLL = C2pLL / (1.0 - da1m * da2p * dt * dt);
+          // C1 > 0, C2 < 0
+          S1 = -1.0; S2 = 1.0;
+          load1(pos(aa, bb));
+          load2(pos(aa - 1, bb));
+          double C1pRL = a1p + da1p * dy0 * S1 - da1p * (a2m + da2m * dxm * S2) * dt;
+          C1pRL = C1pRL / (1.0 - da1p * da2m * dt * dt);
+          double C2mRL = a2m + da2m * dxm * S2 - da2m * (a1p + da1p * dy0 * S1) * dt;
+          C2mRL = C2mRL / (1.0 - da1p * da2m * dt * dt);
+          double C1mRL = a1m + da1m * dy0 * S1 - da1m * (a2p + da2p * dxm * S2) * dt;
+          C1mRL = C1mRL / (1.0 - da1m * da2p * dt * dt);
+          double C2pRL = a2p + da2p * dxm * S2 - da2p * (a1m + da1m * dy0 * S1) * dt;
+          C2pRL = C2pRL / (1.0 - da1m * da2p * dt * dt);
+          // C1 < 0, C2 > 0
+          S1 = 1.0; S2 = -1.0;
+          load1(pos(aa, bb - 1));
+          load2(pos(aa, bb));
+          double C1pLR = a1p + da1p * dym * S1 - da1p * (a2m + da2m * dx0 * S2) * dt;
+          C1pLR = C1pLR / (1.0 - da1p * da2m * dt * dt);
+          double C2mLR = a2m + da2m * dx0 * S2 - da2m * (a1p + da1p * dym * S1) * dt;
+          C2mLR = C2mLR / (1.0 - da1p * da2m * dt * dt);
+          double C1mLR = a1m + da1m * dym * S1 - da1m * (a2p + da2p * dx0 * S2) * dt;
+          C1mLR = C1mLR / (1.0 - da1m * da2p * dt * dt);
+          double C2pLR = a2p + da2p * dx0 * S2 - da2p * (a1m + da1m * dym * S1) * dt;
+          C2pLR = C2pLR / (1.0 - da1m * da2p * dt * dt);
+          // C1 < 0, C2 < 0
+          S1 = -1.0; S2 = -1.0;
+          load1(pos(aa, bb));
+          load2(pos(aa, bb));
+          double C1pRR = a1p + da1p * dy0 * S1 - da1p * (a2m + da2m * dx0 * S2) * dt;
+          C1pRR = C1pRR / (1.0 - da1p * da2m * dt * dt);
+          double C2mRR = a2m + da2m * dx0 * S2 - da2m * (a1p + da1p * dy0 * S1) * dt;
+          C2mRR = C2mRR / (1.0 - da1p * da2m * dt * dt);
+          double C1mRR = a1m + da1m * dy0 * S1 - da1m * (a2p + da2p * dx0 * S2) * dt;
+          C1mRR = C1mRR / (1.0 - da1m * da2p * dt * dt);
+          double C2pRR = a2p + da2p * dx0 * S2 - da2p * (a1m + da1m * dy0 * S1) * dt;
+          C2pRR = C2pRR / (1.0 - da1m * da2p * dt * dt);
+
+          int ifW11 = 0, ifW21 = 0, ifW31 = 0, ifW41 = 0, ifW12 = 0, ifW22 = 0, ifW32 = 0, ifW42 = 0;
+          if (C1pLL > 0.0 && C2mLL > 0.0) ifW11 = 1;
+          if (C1mLL > 0.0 && C2pLL > 0.0) ifW12 = 1;
+          if (C1pRL > 0.0 && C2mRL < 0.0) ifW21 = 1;
+          if (C1mRL > 0.0 && C2pRL < 0.0) ifW22 = 1;
+          if (C1pLR < 0.0 && C2mLR > 0.0) ifW31 = 1;
+          if (C1mLR < 0.0 && C2pLR > 0.0) ifW32 = 1;
+          if (C1pRR < 0.0 && C2mRR < 0.0) ifW41 = 1;
+          if (C1mRR < 0.0 && C2pRR < 0.0) ifW42 = 1;
+          auto boost = [](int a1, int a2) {   // dble(int(0.51*a1 + 0.51*a2))
+            return (double)(int)(0.51 * (double)a1 + 0.51 * (double)a2);
+          };
+          double W11 = (double)ifW11 + (1.e13 - 1.0) * boost(ifW11, ifW12);
+          double W12 = (double)ifW12 + (1.e13 - 1.0) * boost(ifW11, ifW12);
+          double W21 = (double)ifW21 + (1.e13 - 1.0) * boost(ifW21, ifW22);
+          double W22 = (double)ifW22 + (1.e13 - 1.0) * boost(ifW21, ifW22);
+          double W31 = (double)ifW31 + (1.e13 - 1.0) * boost(ifW31, ifW32);
+          double W32 = (double)ifW32 + (1.e13 - 1.0) * boost(ifW31, ifW32);
+          double W41 = (double)ifW41 + (1.e13 - 1.0) * boost(ifW41, ifW42);
+          double W42 = (double)ifW42 + (1.e13 - 1.0) * boost(ifW41, ifW42);
+          double C1p = 0.0, C2m = 0.0;
+          if (ifW11 + ifW21 + ifW31 + ifW41 != 0) {
+            C1p = W11 * std::fabs(C2mLL) * C1pLL + W21 * std::fabs(C2mRL) * C1pRL +
+                  W31 * std::fabs(C2mLR) * C1pLR + W41 * std::fabs(C2mRR) * C1pRR;
+            C1p = C1p / (W11 * std::fabs(C2mLL) + W21 * std::fabs(C2mRL) + W31 * std::fabs(C2mLR) +
+                         W41 * std::fabs(C2mRR));
+            C2m = W11 * std::fabs(C1pLL) * C2mLL + W21 * std::fabs(C1pRL) * C2mRL +
+                  W31 * std::fabs(C1pLR) * C2mLR + W41 * std::fabs(C1pRR) * C2mRR;
+            C2m = C2m / (W11 * std::fabs(C1pLL) + W21 * std::fabs(C1pRL) + W31 * std::fabs(C1pLR) +
+                         W41 * std::fabs(C1pRR));
+          }
+          double C1m = 0.0, C2p = 0.0;
+          if (ifW12 + ifW22 + ifW32 + ifW42 != 0) {
+            C1m = W12 * std::fabs(C2pLL) * C1mLL + W22 * std::fabs(C2pRL) * C1mRL +
+                  W32 * std::fabs(C2pLR) * C1mLR + W42 * std::fabs(C2pRR) * C1mRR;
+            C1m = C1m / (W12 * std::fabs(C2pLL) + W22 * std::fabs(C2pRL) + W32 * std::fabs(C2pLR) +
+                         W42 * std::fabs(C2pRR));
+            C2p = W12 * std::fabs(C1mLL) * C2pLL + W22 * std::fabs(C1mRL) * C2pRL +
+                  W32 * std::fabs(C1mLR) * C2pLR + W42 * std::fabs(C1mRR) * C2pRR;
+            C2p = C2p / (W12 * std::fabs(C1mLL) + W22 * std::fabs(C1mRL) + W32 * std::fabs(C1mLR) +
+                         W42 * std::fabs(C1mRR));
+          }
+          double v1a = C1p + C1m, v2a = C2p + C2m, B1a = C1p - C1m, B2a = C2p - C2m;
+          EMF[Ez][p0] = 0.25 * (v1a * B2a - v2a * B1a) * std::sqrt(dnc[p0]);
+        }
+  }
+
+  void CC3(double dt) {   // :2159-2169
+    for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx + 1; i++) {
+      size_t a = id(i, j, k);
+      U[6][a] = U[6][a] + dt / DX(1, j) * (EMF[3][id(i, j + 1, k)] - EMF[3][a]) -
+                dt / DX(2, k) * (EMF[2][id(i, j, k + 1)] - EMF[2][a]);
+    }
+    for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny + 1; j++) for (int i = 1; i <= Nx; i++) {
+      size_t a = id(i, j, k);
+      U[7][a] = U[7][a] + dt / DX(2, k) * (EMF[1][id(i, j, k + 1)] - EMF[1][a]) -
+                dt / DX(0, i) * (EMF[3][id(i + 1, j, k)] - EMF[3][a]);
+    }
+    for (int k = 1; k <= Nz + 1; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx; i++) {
+      size_t a = id(i, j, k);
+      U[8][a] = U[8][a] + dt / DX(0, i) * (EMF[2][id(i + 1, j, k)] - EMF[2][a]) -
+                dt / DX(1, j) * (EMF[1][id(i, j + 1, k)] - EMF[1][a]);
+    }
+  }
+
+  void CC4() {   // :2171-2181
+    for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx; i++) {
+      size_t a = id(i, j, k);
+      Bcc[1][a] = 0.5 * (U[6][a] + U[6][id(i + 1, j, k)]);
+      Bcc[2][a] = 0.5 * (U[7][a] + U[7][id(i, j + 1, k)]);
+      Bcc[3][a] = 0.5 * (U[8][a] + U[8][id(i, j, k + 1)]);
+    }
+    for (int c = 1; c <= 3; c++) fill(Bcc[c], 7, 2);
+  }
+
+  void CT(double dt) {   // EVOLVE:639-649
+    CC1();
+    CCT(0, dt);
+    CCT(1, dt);
+    CCT(2, dt);
+    CC3(dt);
+    CC4();
+  }
+
+  // ---------------------------------------------------------- source
+  double Fcool(double T, size_t c) {   // KI form, KIcool/1DMHDwCC3.f90:1166-1173
+    double NN = U[1][c] / 1.27;
+    double AbsL = 3.94656e1, T0 = 1.0e3;
+    double Laml = 1.0e7 * detmath::exp(-1.184e5 / (T * T0 + 1.0e3));
+    Laml = fmin2(Laml, 5.e3);
+    double Lamc = 1.4e-2 * std::sqrt(T * T0) * detmath::exp(-9.2e1 / (T * T0));
+    return (NN * NN * (Laml + Lamc) - NN) * AbsL;
+  }
+
+  void IMC(double &Pv, double n, double dt, double g1c, size_t c) {   // :2898-2921
+    double Pu = 1.e10, Pd = 1.e-10, Pm = 1.e1, Pmold = -1.0;
+    double nkbi = 1.0 / (P.kb * n);
+    for (int kkk = 1; kkk <= 30; kkk++) {
+      double T = Pm * nkbi;
+      double CooL = Fcool(T, c);
+      double fev = Pm + CooL * dt * g1c - Pv;
+      double iud = fsign(1.0, fev);
+      Pd = fmax2(-iud * Pm, Pd);
+      Pu = fmin2(2.0 * Pm / (iud + 1.0 + 1.e-10), Pu);
+      Pm = detmath::exp10(0.5 * (detmath::log10(Pu) + detmath::log10(Pd)));
+      if (std::fabs(Pm - Pmold) < 1.e-5) break;
+      Pmold = Pm;
+    }
+    Pv = Pm;
+  }
+
+  void SOURCE(double dt) {   // thermal branch ifthrm=2, :2477-2572
+    if (P.ifthrm != 2) return;
+    fill(U[1], 7, 1); fill(U[5], 7, 1);                              // :2484
+    fill_species(7, 1);                                              // :2486
+    std::vector<double> Tn(ncell), Pn(ncell), Qx(ncell), Qy(ncell), Qz(ncell);
+    auto ntot = [&](size_t c) { return sp[SP][c] + sp[SH][c] + sp[SH2][c] + sp[SHE][c] + sp[SHEP][c]; };
+    auto nimc = [&](size_t c) { return sp[SH][c] + sp[SP][c] + sp[SHE][c] + sp[SHEP][c] + sp[SH2][c]; };
+    auto temps = [&]() {
+      for (int k = 0; k <= Nz + 1; k++) for (int j = 0; j <= Ny + 1; j++) for (int i = 0; i <= Nx + 1; i++) {
+        size_t a = id(i, j, k);
+        Tn[a] = U[5][a] / (P.kb * ntot(a));
+      }
+    };
+    auto fluxes = [&]() {
+      for (int k = 0; k <= Nz; k++) for (int j = 0; j <= Ny; j++) for (int i = 0; i <= Nx; i++) {
+        size_t a = id(i, j, k);
+        double rtTx = std::sqrt((DX(0, i) * Tn[id(i + 1, j, k)] + DX(0, i + 1) * Tn[a]) / (DX(0, i) + DX(0, i + 1)));
+        double rtTy = std::sqrt((DX(1, j) * Tn[id(i, j + 1, k)] + DX(1, j + 1) * Tn[a]) / (DX(1, j) + DX(1, j + 1)));
+        double rtTz = std::sqrt((DX(2, k) * Tn[id(i, j, k + 1)] + DX(2, k + 1) * Tn[a]) / (DX(2, k) + DX(2, k + 1)));
+        Qx[a] = P.Kcond * fmin2(rtTx, 3.873) * (Tn[id(i + 1, j, k)] - Tn[a]) * 2.0 / (DX(0, i) + DX(0, i + 1));
+        Qy[a] = P.Kcond * fmin2(rtTy, 3.873) * (Tn[id(i, j + 1, k)] - Tn[a]) * 2.0 / (DX(1, j) + DX(1, j + 1));
+        Qz[a] = P.Kcond * fmin2(rtTz, 3.873) * (Tn[id(i, j, k + 1)] - Tn[a]) * 2.0 / (DX(2, k) + DX(2, k + 1));
+      }
+    };
+    temps();
+    for (size_t a = 0; a < ncell; a++) Pn[a] = U[5][a];
+    fluxes();
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == 1) {
+        fill(U[5], 7, 1);                                           // :2528
+        temps();
+        fluxes();
+      }
+#pragma omp parallel for collapse(2) schedule(dynamic, 1)
+      for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx; i++) {
+        size_t a = id(i, j, k);
+        double CooL = Fcool(Tn[a], a);
+        double g1c = gmi1_of(a);
+        if (pass == 0) {
+          if (dt <= 0.2 * Pn[a] / (g1c * std::fabs(CooL))) {
+            U[5][a] = U[5][a] - g1c * CooL * dt * 0.5;
+          } else {
+            IMC(U[5][a], nimc(a), dt * 0.5, g1c, a);
+          }
+        } else {
+          if (dt <= 0.2 * Pn[a] / (g1c * std::fabs(CooL))) {
+            U[5][a] = Pn[a] - g1c * CooL * dt;
+          } else {
+            double pv = Pn[a];
+            IMC(pv, nimc(a), dt, g1c, a);
+            U[5][a] = pv;
+          }
+        }
+        double tcd = g1c * P.Kcond * std::sqrt(Tn[a]);
+        tcd = 0.49 * nimc(a) * P.kb / tcd * (DX(0, i) * DX(0, i));
+        tcd = fsign(0.5, tcd - dt);
+        double div = (Qx[a] - Qx[id(i - 1, j, k)]) / DX(0, i) + (Qy[a] - Qy[id(i, j - 1, k)]) / DX(1, j) +
+                     (Qz[a] - Qz[id(i, j, k - 1)]) / DX(2, k);
+        if (pass == 0)
+          U[5][a] = U[5][a] + (tcd + 0.5) * g1c * dt * 0.5 * div;
+        else
+          U[5][a] = U[5][a] + (tcd + 0.5) * g1c * dt * div;
+        U[5][a] = fmax2(U[5][a], P.pmin);
+        U[5][a] = fmin2(U[5][a], P.pmax);
+      }
+    }
+  }
+
+  // ------------------------------------------------------------ dt
+  double Couran() {   // :1912-1930
+    double tCFL = P.tfinal;
+    for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx; i++) {
+      size_t a = id(i, j, k);
+      double gam = gam_of(a);
+      double c2 = (gam * U[5][a] + Bcc[1][a] * Bcc[1][a] + Bcc[2][a] * Bcc[2][a] + Bcc[3][a] * Bcc[3][a]) / U[1][a];
+      tCFL = fmin2(tCFL, DX(0, i) / (std::sqrt(c2) + std::fabs(U[2][a])));
+      tCFL = fmin2(tCFL, DX(1, j) / (std::sqrt(c2) + std::fabs(U[3][a])));
+      tCFL = fmin2(tCFL, DX(2, k) / (std::sqrt(c2) + std::fabs(U[4][a])));
+    }
+    return tCFL;
+  }
+  double Stblty() {   // :2784-2822 with the KI Fcool
+    double tLMT = P.tfinal;
+    for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx; i++) {
+      size_t a = id(i, j, k);
+      double Nn = sp[SP][a] + sp[SH][a] + sp[SH2][a] + sp[SHE][a] + sp[SHEP][a];
+      double Tn = U[5][a] / (P.kb * Nn);
+      double dl = fmin2(fmin2(DX(0, i), DX(1, j)), DX(2, k));
+      double g1c = gmi1_of(a);
+      double alpha = g1c * P.Kcond * std::sqrt(fmin2(Tn, 15.0));
+      alpha = 0.4 * Nn * P.kb / alpha * (dl * dl);
+      double CooL = Fcool(Tn, a);
+      double tauC = U[5][a] / g1c / std::fabs(CooL);
+      tauC = fmax2(0.2 * tauC, 2.5e-4);
+      tLMT = fmin2(tLMT, tauC);
+      tLMT = fmin2(tLMT, alpha);
+    }
+    return tLMT;
+  }
+  // EVOLVE:569-580 for one rank: returns dt and the limiter id st
+  double timestep(int &st) {
+    double dtm = P.tfinal;
+    dtm = fmin2(dtm, P.CFL * Couran());
+    st = 1;
+    if (P.ifthrm == 2) {
+      double stt = dtm;
+      dtm = fmin2(dtm, Stblty());
+      if (dtm < stt) st = 2;
+    }
+    return fmin2(P.tfinal, dtm);   // :590-596 with one rank
+  }
+
+  // ------------------------------------------------------------ DISSIP
+  // :3143-3173; the reference damps the first and last ten x-cells on the
+  // edge ranks.  Both edges are damped here, each from the pre-damping
+  // velocities, which is what any run with NSPLTx >= 2 does.
+  void DISSIP() {
+    fill(U[2], 7, 2); fill(U[3], 7, 2); fill(U[4], 7, 2);
+    int offs[2] = {0, Nx - 10};
+    std::vector<double> divv[2];
+    for (int e = 0; e < 2; e++) {
+      divv[e].assign((size_t)12 * (Ny + 2) * (Nz + 2), 0.0);
+      for (int k = 0; k <= Nz + 1; k++) for (int j = 0; j <= Ny + 1; j++) for (int i = 0; i <= 11; i++) {
+        int ix = i + offs[e];
+        divv[e][(size_t)i + 12 * ((size_t)j + (Ny + 2) * (size_t)k)] =
+            (U[2][id(ix + 1, j, k)] - U[2][id(ix - 1, j, k)] + U[3][id(ix, j + 1, k)] - U[3][id(ix, j - 1, k)] +
+             U[4][id(ix, j, k + 1)] - U[4][id(ix, j, k - 1)]) * 0.25;
+      }
+    }
+    for (int e = 0; e < 2; e++) {
+      auto dv = [&](int i, int j, int k) { return divv[e][(size_t)i + 12 * ((size_t)j + (Ny + 2) * (size_t)k)]; };
+      for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= 10; i++) {
+        size_t a = id(i + offs[e], j, k);
+        U[2][a] = U[2][a] + 0.1 * (dv(i + 1, j, k) - dv(i - 1, j, k));
+        U[3][a] = U[3][a] + 0.1 * (dv(i, j + 1, k) - dv(i, j - 1, k));
+        U[4][a] = U[4][a] + 0.1 * (dv(i, j, k + 1) - dv(i, j, k - 1));
+      }
+    }
+  }
+
+  // one in20 iteration of EVOLVE after dt is known (:606-656)
+  void advance(double dt) {
+    SOURCE(0.5 * dt);
+    static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
+    for (int s = 0; s < 3; s++) MHD(orders[ifEVO - 1][s], dt);
+    ifEVO = ifEVO % 6 + 1;
+    CT(dt);
+    SOURCE(0.5 * dt);
+    if (P.dissip) DISSIP();
+    time = time + dt;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+// params (doubles): nx,ny,nz, CFL,facdep,tfinal, bc[6], pmin,pmax,rmin, kb,Kcond, ifthrm, dissip
+void *o3d_create(const double *p) {
+  Params P{};
+  P.nx = (int)p[0]; P.ny = (int)p[1]; P.nz = (int)p[2];
+  P.CFL = p[3]; P.facdep = p[4]; P.tfinal = p[5];
+  for (int q = 0; q < 6; q++) P.bc[q] = (int)p[6 + q];
+  P.pmin = p[12]; P.pmax = p[13]; P.rmin = p[14];
+  P.kb = p[15]; P.Kcond = p[16];
+  P.ifthrm = (int)p[17]; P.dissip = (int)p[18];
+  P.nspecies = 8;
+  Mhd3D *m = new Mhd3D();
+  m->init(P);
+  return m;
+}
+
+// U: 8 fields of (nz+4)(ny+4)(nx+4) doubles (Fortran U(-1:ndx,-1:ndy,-1:ndz,8)),
+// species: 8 such arrays in the order ndH,ndp,ndH2,ndHe,ndHep,ndC,ndCp,ndCO,
+// coords: x,dx,y,dy,z,dz each (-1..N+2).  Runs CC(4) like INITIA:470.
+void o3d_upload(void *h, const double *U, const double *sp, const double *coords) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  for (int f = 1; f <= 8; f++) memcpy(m->U[f].data(), U + (f - 1) * m->ncell, m->ncell * sizeof(double));
+  for (int s = 0; s < 8; s++) memcpy(m->sp[s].data(), sp + s * m->ncell, m->ncell * sizeof(double));
+  size_t off = 0;
+  for (int d = 0; d < 3; d++) {
+    int n = m->Nd(d) + 4;
+    memcpy(m->xc[d].data(), coords + off, n * sizeof(double)); off += n;
+    memcpy(m->dxc[d].data(), coords + off, n * sizeof(double)); off += n;
+  }
+  m->CC4();
+}
+
+void o3d_download(void *h, double *U, double *sp, double *bcc) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  for (int f = 1; f <= 8; f++) memcpy(U + (f - 1) * m->ncell, m->U[f].data(), m->ncell * sizeof(double));
+  if (sp) for (int s = 0; s < 8; s++) memcpy(sp + s * m->ncell, m->sp[s].data(), m->ncell * sizeof(double));
+  if (bcc) for (int c = 1; c <= 3; c++) memcpy(bcc + (c - 1) * m->ncell, m->Bcc[c].data(), m->ncell * sizeof(double));
+}
+
+double o3d_timestep(void *h, int *st) { return static_cast<Mhd3D *>(h)->timestep(*st); }
+void o3d_source(void *h, double dt) { static_cast<Mhd3D *>(h)->SOURCE(dt); }
+void o3d_sweep(void *h, int dir, double dt) { static_cast<Mhd3D *>(h)->MHD(dir, dt); }
+void o3d_ct(void *h, double dt) { static_cast<Mhd3D *>(h)->CT(dt); }
+void o3d_dissip(void *h) { static_cast<Mhd3D *>(h)->DISSIP(); }
+void o3d_advance(void *h, double dt) { static_cast<Mhd3D *>(h)->advance(dt); }
+double o3d_time(void *h) { return static_cast<Mhd3D *>(h)->time; }
+void o3d_set_order(void *h, int ifEVO) { static_cast<Mhd3D *>(h)->ifEVO = ifEVO; }
+
+// full EVOLVE iteration: dt from Couran/Stblty, clipped at tfinal and tsave
+// (:569-604), then advance.  Returns dt; *st is the limiter (1 FastSpd, 2 Conduct).
+double o3d_step(void *h, double tsave, int *st) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  double dt = m->timestep(*st);
+  if (m->time + dt > m->P.tfinal) dt = m->P.tfinal - m->time;
+  if (m->time + dt > tsave) dt = tsave - m->time;
+  m->advance(dt);
+  return dt;
+}
+
+void o3d_destroy(void *h) { delete static_cast<Mhd3D *>(h); }
+
+}  // extern "C"

@@ -1,0 +1,160 @@
+"""ctypes wrapper of the oracle library (test infrastructure only).
+
+The oracle is the CPU restatement of the reference algorithm; tests, the
+smoke check and the CPU-baseline leg of bench.py load it as the checker.
+Nothing on the product path imports this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_P = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force=False):
+    """Compile oracle/_build/liboracle.so with the committed Makefile."""
+    srcs = [os.path.join(_HERE, f) for f in ("mhd1d.cpp", "mhd3d.cpp")]
+    if not force and os.path.exists(_LIB) and all(
+            os.path.getmtime(_LIB) >= os.path.getmtime(s) for s in srcs):
+        return _LIB
+    subprocess.run(["make", "-C", _HERE, "-B" if force else "all"], check=True,
+                   stdout=subprocess.DEVNULL)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB)
+        L.o1d_create.restype = ctypes.c_void_p
+        L.o1d_create.argtypes = [_P]
+        L.o1d_ncell.argtypes = [ctypes.c_void_p]
+        L.o1d_time.restype = ctypes.c_double
+        L.o1d_time.argtypes = [ctypes.c_void_p]
+        L.o1d_step.restype = ctypes.c_double
+        L.o1d_step.argtypes = [ctypes.c_void_p]
+        L.o1d_run_trace.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
+        L.o1d_state.argtypes = [ctypes.c_void_p, _P]
+        L.o1d_destroy.argtypes = [ctypes.c_void_p]
+        L.o3d_create.restype = ctypes.c_void_p
+        L.o3d_create.argtypes = [_P]
+        L.o3d_upload.argtypes = [ctypes.c_void_p, _P, _P, _P]
+        L.o3d_download.argtypes = [ctypes.c_void_p, _P, _P, _P]
+        L.o3d_timestep.restype = ctypes.c_double
+        L.o3d_timestep.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        for n in ("o3d_source", "o3d_ct", "o3d_advance"):
+            getattr(L, n).argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.o3d_sweep.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+        L.o3d_dissip.argtypes = [ctypes.c_void_p]
+        L.o3d_time.restype = ctypes.c_double
+        L.o3d_time.argtypes = [ctypes.c_void_p]
+        L.o3d_set_order.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.o3d_step.restype = ctypes.c_double
+        L.o3d_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
+        L.o3d_destroy.argtypes = [ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P)
+
+
+class Oracle1D:
+    """KIcool/1DMHDwCC3.f90 (or the Brio-Wu variant) on the CPU."""
+
+    def __init__(self, deck_vector):
+        d = np.ascontiguousarray(deck_vector, dtype=np.float64)
+        self.h = lib().o1d_create(_ptr(d))
+        self.ncell = lib().o1d_ncell(self.h)
+
+    def run_trace(self, nsteps, probe_n=512, probe_b=510):
+        tr = np.zeros((nsteps, 4))
+        lib().o1d_run_trace(self.h, nsteps, probe_n, probe_b, _ptr(tr))
+        return tr
+
+    def step(self):
+        return lib().o1d_step(self.h)
+
+    @property
+    def time(self):
+        return lib().o1d_time(self.h)
+
+    def state(self):
+        out = np.zeros((self.ncell, 17))
+        lib().o1d_state(self.h, _ptr(out))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().o1d_destroy(self.h)
+            self.h = None
+
+
+class Oracle3D:
+    """One-block restatement of the 3D step (MCF3DSGincfca3.f90 + KI cooling)."""
+
+    def __init__(self, params):
+        p = params
+        v = [p.nx, p.ny, p.nz, p.cfl, p.facdep, p.tfinal, *p.bc, p.pmin, p.pmax, p.rmin,
+             p.kb, p.kcond, p.ifthrm, p.dissip]
+        self.params = p
+        self.shape = (p.nz + 4, p.ny + 4, p.nx + 4)
+        self.h = lib().o3d_create(_ptr(np.array(v, dtype=np.float64)))
+
+    def upload(self, state):
+        U = np.ascontiguousarray(state.U, dtype=np.float64)
+        sp = np.ascontiguousarray(state.species, dtype=np.float64)
+        co = np.ascontiguousarray(state.coords_vector(), dtype=np.float64)
+        lib().o3d_upload(self.h, _ptr(U), _ptr(sp), _ptr(co))
+
+    def download(self):
+        U = np.zeros((8,) + self.shape)
+        sp = np.zeros((8,) + self.shape)
+        bcc = np.zeros((3,) + self.shape)
+        lib().o3d_download(self.h, _ptr(U), _ptr(sp), _ptr(bcc))
+        return U, sp, bcc
+
+    def timestep(self):
+        st = ctypes.c_int(0)
+        dt = lib().o3d_timestep(self.h, ctypes.byref(st))
+        return dt, st.value
+
+    def source(self, dt):
+        lib().o3d_source(self.h, dt)
+
+    def sweep(self, d, dt):
+        lib().o3d_sweep(self.h, d, dt)
+
+    def ct(self, dt):
+        lib().o3d_ct(self.h, dt)
+
+    def dissip(self):
+        lib().o3d_dissip(self.h)
+
+    def advance(self, dt):
+        lib().o3d_advance(self.h, dt)
+
+    def step(self, tsave=1e30):
+        st = ctypes.c_int(0)
+        dt = lib().o3d_step(self.h, tsave, ctypes.byref(st))
+        return dt, st.value
+
+    def set_order(self, ifevo):
+        lib().o3d_set_order(self.h, ifevo)
+
+    @property
+    def time(self):
+        return lib().o3d_time(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().o3d_destroy(self.h)
+            self.h = None
