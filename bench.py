@@ -1,0 +1,349 @@
+"""Benchmark of the GB300 MHD + KI cooling step (one JSON line on rank 0).
+
+Workload: the 256^3 colliding warm-neutral-medium flows with KI cooling
+(20 pc box, n0 = 1 cm^-3, T0 = 6000 K, lognormal density rms 0.1 with a
+k^-11/3 spectrum from ran0 seed 1, vx = +-20 km/s converging at the
+mid-plane, |B| = 3 uG at 45 deg in x-y, free x and periodic y/z
+boundaries, DISSIP on).  A "step" is one EVOLVE iteration: dt from
+Couran+Stblty, SOURCE(dt/2), three sweeps, constrained transport,
+SOURCE(dt/2), DISSIP.  The grid (16 FP64 arrays of 260^3 plus scratch,
+~3.7 GB) is far larger than the 129 MB L2, so no flush is needed between
+steps.
+
+`value` is the chosen form (FP32 reconstruction/flux, FP64 accumulation);
+`plain_fp64` is the plain FP64 path timed the same way; `l1_error` compares
+the two after the run (same dt sequence).  `e2e` times the same step
+through the C ABI with the state uploaded from pinned host memory and
+downloaded again every step.  `roofline` is for the dominant kernel (the
+fused sweep), with algorithmic bytes from the per-zone budget of the step.
+`cpu_baseline` is the CPU restatement (oracle, C++ with OpenMP) timed on a
+bounded sample on the host cores.
+
+`--impl reference` times that CPU restatement alone (the reference itself is
+Fortran + MPI and no Fortran compiler exists on this machine; the restatement
+reproduces its golden outputs) on a 64^3 sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_ALG_STEP = 552.0      # algorithmic bytes per zone-update of the whole step
+B_ALG_SWEEP = 104.0     # per sweep: read rho, v3, p, face-B3 (64) + write rho, v3, p (40)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--sur-steps", type=int, default=2000)
+    ap.add_argument("--sur-data", type=int, default=1 << 24)
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per zone of one sweep launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "sweep_fp32_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_zone_fp32_sweep="):
+                return float(line.split("=")[1])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks during the timed region (one sample / 200 ms)."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        import statistics
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(n=64, steps=2):
+    """The oracle (C++ restatement, OpenMP over host cores) on a 64^3 sample
+    of the same workload: zone-updates/s."""
+    from code_tohoku_gb300 import problems
+    from oracle.pyoracle import Oracle3D
+    st = problems.colliding_flows(n)
+    o = Oracle3D(st.params)
+    o.upload(st)
+    o.step()   # first-touch and thread start-up
+    t = time.perf_counter()
+    for _ in range(steps):
+        o.step()
+    el = time.perf_counter() - t
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": n ** 3 * steps / el, "unit": "zone-updates/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} steps of the {n}^3 colliding-flow problem (same physics, seed, box)"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    from code_tohoku_gb300 import problems
+    from oracle.pyoracle import Oracle3D
+    n = 64
+    st = problems.colliding_flows(n)
+    o = Oracle3D(st.params)
+    o.upload(st)
+    for _ in range(max(args.warmup, 0)):
+        o.step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        o.step()
+    el = time.perf_counter() - t
+    v = n ** 3 * args.steps / el
+    line = {"metric": "zone-updates/s, 256^3 MHD+KI cool: FP32+surrogate vs plain FP64 at stated L1 err",
+            "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "colliding WNM flows with KI cooling, 64^3 sample of the 256^3 problem",
+                       "n": n, "precision": "fp64"},
+            "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port",
+                             "sample": f"{args.steps} steps of the {n}^3 problem; C++ restatement of "
+                                       "MCF3DSGincfca3.f90 (no Fortran compiler on the box)"},
+            "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import numpy as np
+    import torch
+
+    from code_tohoku_gb300 import native, problems, replicas
+    torch.cuda.set_device(local)
+    replicas.init("nccl")
+    dev = local
+    # a dedicated stream: the kernels, the CUDA events and the copies all go here
+    stream = torch.cuda.Stream()
+
+    st = problems.colliding_flows(args.n)
+    n3 = args.n ** 3
+
+    # the learned part: train the KI-cooling surrogate on this GPU first
+    from code_tohoku_gb300 import surrogate
+    t0 = time.perf_counter()
+    sur_params, hist = surrogate.train(n_data=args.sur_data, batch=65536, steps=args.sur_steps, lr=1e-3,
+                                       seed=1, device=dev)
+    sur_train_s = time.perf_counter() - t0
+
+    def make(prec, cooling=native.COOL_EXACT):
+        g = native.Mhd3D(st.params, precision=prec, cooling=cooling, device=dev)
+        g.set_stream(stream.cuda_stream)
+        if cooling == native.COOL_SURROGATE:
+            g.surrogate_load(sur_params, 1e-3)
+        g.upload(st)
+        return g
+
+    def barrier():
+        replicas.barrier()
+        torch.cuda.synchronize()
+
+    def step_timed(g, ev):
+        """One EVOLVE iteration through the C ABI, with events around the sweeps."""
+        dt, _ = g.timestep()
+        g.source(0.5 * dt)
+        order = ((0, 1, 2), (1, 2, 0), (2, 0, 1), (0, 2, 1), (1, 0, 2), (2, 1, 0))[g.ifevo - 1]
+        for d in order:
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            g.sweep(d, dt)
+            b.record(stream)
+            ev.append((a, b))
+        g.ifevo = g.ifevo % 6 + 1
+        g.ct(dt)
+        g.source(0.5 * dt)
+        if st.params.dissip:
+            g.dissip()
+        g.set_time(g.time + dt, g.ifevo)
+        return dt
+
+    def timed_run(prec, cooling=native.COOL_EXACT):
+        g = make(prec, cooling)
+        g.ifevo = 1
+        for _ in range(args.warmup):
+            step_timed(g, [])
+        ev = []
+        barrier()
+        launches0 = g.kernel_launches
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(dev) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                step_timed(g, ev)
+            e1.record(stream)
+            barrier()
+        ms = e0.elapsed_time(e1)
+        sweep_ms = [a.elapsed_time(b) for a, b in ev]
+        launches = g.kernel_launches - launches0
+        return g, ms, sweep_ms, launches, clk.summary()
+
+    # chosen form: FP32 reconstruction/flux + FP64 accumulation + surrogate
+    g32, ms32, sw32, launches32, clocks = timed_run(native.PREC_FP32, native.COOL_SURROGATE)
+    d32 = g32.diagnostics()
+    ms32 = replicas.max_over_ranks(ms32)
+    value = world * n3 * args.steps / (ms32 * 1e-3)
+    # ablation: the same FP32 form with the exact cooling integrator
+    gx, msx, _, _, _ = timed_run(native.PREC_FP32, native.COOL_EXACT)
+    dx_ = gx.diagnostics()
+    del gx
+
+    # plain FP64 form, same workload
+    fp64 = None
+    l1 = None
+    if not args.no_fp64:
+        g64, ms64, sw64, launches64, _ = timed_run(native.PREC_FP64)
+        fp64 = {"value": n3 * args.steps / (ms64 * 1e-3), "unit": "zone-updates/s",
+                "ms_per_step": ms64 / args.steps, "sweep_ms": sum(sw64) / len(sw64)}
+        # L1 error of the chosen form against FP64 after the same number of
+        # steps from the same state (each form takes its own dt, like a run)
+        U32, s32, b32 = g32.download()
+        U64, s64, b64 = g64.download()
+        c = (slice(2, -2),) * 3
+
+        def l1rel(a, b):
+            return float(np.abs(a - b).mean() / np.abs(b).mean())
+        n32 = s32[0][c] + s32[1][c] + s32[2][c] + s32[3][c] + s32[4][c]
+        n64 = s64[0][c] + s64[1][c] + s64[2][c] + s64[3][c] + s64[4][c]
+        l1 = {"rho": l1rel(U32[0][c], U64[0][c]), "T": l1rel(U32[4][c] / n32, U64[4][c] / n64),
+              "B": l1rel(b32[(slice(None),) + c], b64[(slice(None),) + c]),
+              "steps": args.warmup + args.steps}
+        del g64
+
+    # e2e through the C ABI with host buffers (pinned), one upload + step +
+    # download per step
+    pin_U = torch.empty((8,) + tuple(st.U.shape[1:]), dtype=torch.float64, pin_memory=True).numpy()
+    pin_S = torch.empty((8,) + tuple(st.U.shape[1:]), dtype=torch.float64, pin_memory=True).numpy()
+    pin_U[...] = st.U
+    pin_S[...] = st.species
+    g = g32
+    host_state = problems.MhdState(st.params, pin_U, pin_S, st.x, st.dx, st.y, st.dy, st.z, st.dz)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(2, min(args.steps, 5))
+    for _ in range(e2e_steps):
+        g.upload(host_state)
+        g.step()
+        U, S, _ = g.download(with_bcc=False)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    nb = 8 * pin_U.size
+    e2e = {"value": world * n3 / e2e_s, "unit": "zone-updates/s", "h2d_bytes_per_step": 2 * nb,
+           "d2h_bytes_per_step": 2 * nb}
+
+    if rank != 0:
+        return
+    hbm, which = peaks()
+    sweep_ms = sum(sw32) / len(sw32)
+    achieved = B_ALG_SWEEP * n3 / (sweep_ms * 1e-3) / 1e9
+    tr = ncu_traffic()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": tr * n3 if tr else None, "kernel": "sweep_kernel<float> (fused RHS+MOC+REMAP)",
+            "peak_source": f"{which} (MEASURED_PEAKS.json hbm_gbs)" if which == "measured" else which,
+            "algorithmic_bytes_per_zone": B_ALG_SWEEP}
+    line = {"metric": "zone-updates/s, 256^3 MHD+KI cool: FP32+surrogate vs plain FP64 at stated L1 err",
+            "value": value, "unit": "zone-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 recon/flux + f64 accumulation",
+            "data": "synthetic",
+            "config": {"workload": f"colliding WNM flows with KI cooling, {args.n}^3, free x / periodic y,z",
+                       "n": args.n, "precision": "fp32 reconstruction+flux, fp64 accumulation",
+                       "cooling": "KI surrogate MLP (BF16 tensor cores) + Newton polish, IMC fallback",
+                       "l2": "inputs larger than L2 (3.7 GB)",
+                       "parallelism": f"replicas x{world}"},
+            "plain_fp64": fp64, "l1_error": l1, "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
+            "fp32_exact_cooling": {"value": n3 * args.steps / (msx * 1e-3), "unit": "zone-updates/s",
+                                   "imc_cells": dx_["imc_cells"]},
+            "surrogate": {"train_s": sur_train_s, "steps": args.sur_steps, "n_data": args.sur_data,
+                          "batch": 65536, "final_mse": float(np.mean(hist[-20:])) if len(hist) else None,
+                          "surrogate_cells": d32["surrogate_cells"], "fallback_cells": d32["fallback_cells"],
+                          "imc_cells": d32["imc_cells"],
+                          "fallback_fraction": (d32["fallback_cells"] / max(1, d32["fallback_cells"] + d32["surrogate_cells"]))},
+            "step_zone_updates_roof": hbm * 1e9 / B_ALG_STEP,
+            "e2e": e2e, "gpu_launches": launches32, "roofline": roof, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

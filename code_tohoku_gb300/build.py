@@ -5,6 +5,8 @@ one shared library next to this file:
   csrc/mhd_fp64.cu  plain FP64 kernels, --fmad=false (bit-exact arithmetic)
   csrc/mhd_fp32.cu  FP32 reconstruction/flux kernels (contraction allowed)
   csrc/mhd_capi.cu  the extern "C" boundary of include/mhd_gb300.h
+  csrc/mhd_surrogate.cu  surrogate data, training and evaluation kernels
+                    (--fmad=false: its FP64 labels match the CPU IMC bit for bit)
 """
 import os
 import shutil
@@ -22,7 +24,7 @@ UNITS = {
     "mhd_fp64.cu": ["--fmad=false"],
     "mhd_fp32.cu": ["--fmad=true"],
     "mhd_capi.cu": ["--fmad=false"],
-    "mhd_surrogate.cu": ["--fmad=true"],
+    "mhd_surrogate.cu": ["--fmad=false"],
 }
 
 

@@ -33,7 +33,10 @@ struct mhd_handle {
   double *pnew = nullptr;
   double *divv = nullptr;
   double *diag_part = nullptr;
-  unsigned long long *dtred = nullptr;   // [0] tCFL bits, [1] tLMT bits, [2] IMC count
+  unsigned long long *dtred = nullptr;   // [0] tCFL, [1] tLMT bits, [2] IMC, [3] surrogate, [4] fallback
+  float *sur_master = nullptr;           // FP32 surrogate parameters (device)
+  SurNet *sur_net = nullptr;             // packed BF16 network (device)
+  float sur_tol = 1e-3f;
   int *err = nullptr;
   unsigned long long *h_small = nullptr; // pinned readback
   double time = 0.0;
@@ -42,6 +45,7 @@ struct mhd_handle {
   long long launches = 0;
   long long imc_cells = 0;
   bool uploaded = false;
+  std::vector<double> rdx_host;
   std::string msg;
 };
 
@@ -112,7 +116,8 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   for (int q = 0; q < 6; q++)
     if (!valid_bc(p->bc[q])) return MHD_ERR_ARG;   // codes 1 (free) and 3 (periodic)
   if (p->precision != MHD_PREC_FP64 && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
-  if (p->cooling != MHD_COOL_EXACT) return MHD_ERR_ARG;   // surrogate: see mhd_surrogate.cu
+  if (p->cooling != MHD_COOL_EXACT && p->cooling != MHD_COOL_SURROGATE) return MHD_ERR_ARG;
+  if (p->cooling == MHD_COOL_SURROGATE && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
   if (p->dissip && p->nx < 11) return MHD_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device) return MHD_ERR_NO_DEVICE;
@@ -148,13 +153,13 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   for (int c = 0; c < 3; c++) { h->vf[c] = q; q += g.ncell; }
   for (int c = 0; c < 3; c++) { h->emf[c] = q; q += g.ncell; }
   h->pnew = q;
-  size_t ncoord = 2 * (size_t)(g.s[0] + g.s[1] + g.s[2]);
+  size_t ncoord = 3 * (size_t)(g.s[0] + g.s[1] + g.s[2]);
   size_t ndivv = 2 * 12 * (size_t)(g.n[1] + 2) * (g.n[2] + 2);
   size_t ndiag = 6 * (size_t)((g.n[0] * (long long)g.n[1] * g.n[2] + 255) / 256);
   bool ok = cudaMalloc(&h->coords, ncoord * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&h->divv, ndivv * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&h->diag_part, ndiag * sizeof(double)) == cudaSuccess &&
-            cudaMalloc(&h->dtred, 4 * sizeof(unsigned long long)) == cudaSuccess &&
+            cudaMalloc(&h->dtred, 8 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaMalloc(&h->err, sizeof(int)) == cudaSuccess &&
             cudaMallocHost(&h->h_small, 8 * sizeof(unsigned long long)) == cudaSuccess &&
             cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
@@ -166,9 +171,13 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   h->own_stream = true;
   cudaMemsetAsync(h->block, 0, bytes, h->stream);
   cudaMemsetAsync(h->err, 0, sizeof(int), h->stream);
-  cudaMemsetAsync(h->dtred, 0, 4 * sizeof(unsigned long long), h->stream);
+  cudaMemsetAsync(h->dtred, 0, 8 * sizeof(unsigned long long), h->stream);
   double *c = h->coords;
-  for (int d = 0; d < 3; d++) { g.x[d] = c; c += g.s[d]; g.dx[d] = c; c += g.s[d]; }
+  for (int d = 0; d < 3; d++) {
+    g.x[d] = c; c += g.s[d];
+    g.dx[d] = c; c += g.s[d];
+    g.rdx[d] = c; c += g.s[d];
+  }
   *out = h;
   return MHD_OK;
 }
@@ -183,6 +192,8 @@ int mhd_destroy(mhd_handle *h) {
   cudaFree(h->diag_part);
   cudaFree(h->dtred);
   cudaFree(h->err);
+  cudaFree(h->sur_master);
+  cudaFree(h->sur_net);
   if (h->h_small) cudaFreeHost(h->h_small);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -213,9 +224,18 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
   for (int s = 0; s < 8; s++)
     CKR(cudaMemcpyAsync(h->f.sp[s], species + (size_t)s * g.ncell, nb, cudaMemcpyHostToDevice, h->stream));
   const double *src[6] = {x, dx, y, dy, z, dz};
+  h->rdx_host.resize((size_t)(g.s[0] + g.s[1] + g.s[2]));
+  size_t off = 0;
   for (int d = 0; d < 3; d++) {
     CKR(cudaMemcpyAsync((void *)g.x[d], src[2 * d], g.s[d] * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CKR(cudaMemcpyAsync((void *)g.dx[d], src[2 * d + 1], g.s[d] * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    // reciprocal Euler widths for the chosen form's remap: 1/(x(i)-x(i-1))
+    double *r = h->rdx_host.data() + off;
+    const double *xx = src[2 * d];
+    r[0] = 1.0 / src[2 * d + 1][0];
+    for (int i = 1; i < g.s[d]; i++) r[i] = 1.0 / (xx[i] - xx[i - 1]);
+    CKR(cudaMemcpyAsync((void *)g.rdx[d], r, g.s[d] * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    off += g.s[d];
   }
   // CC(4) as INITIA:470
   CK(cell_b(h->g, h->f, h->stream));
@@ -278,6 +298,22 @@ int mhd_source(mhd_handle *h, double dt) {
   // SOURCE :2481-2486 — rho, p and the species, one ghost layer, x y z
   TRY(fill(h, {h->f.U[0], h->f.U[4]}, 7, 1));
   TRY(fill(h, {h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]}, 7, 1, 1));
+  if (h->p.precision == MHD_PREC_FP32) {
+    if (h->p.cooling == MHD_COOL_SURROGATE && !h->sur_net)
+      return fail(h, MHD_ERR_STATE, "surrogate cooling selected but no network loaded (mhd_surrogate_load)");
+    Source32Args a{};
+    a.g = h->g; a.ph = h->ph; a.f = h->f;
+    a.dt = dt; a.err = h->err;
+    a.imc_count = h->dtred + 2; a.sur_count = h->dtred + 3; a.fb_count = h->dtred + 4;
+    a.W = (h->p.cooling == MHD_COOL_SURROGATE) ? h->sur_net : nullptr;
+    a.tol = h->sur_tol;
+    a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
+    CK(source_fp32(a, h->stream));
+    TRY(fill(h, {h->pnew}, 7, 1));
+    a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
+    CK(source_fp32(a, h->stream));
+    return MHD_OK;
+  }
   SourceArgs a{};
   a.g = h->g; a.ph = h->ph; a.f = h->f;
   a.dt = dt; a.err = h->err; a.imc_count = h->dtred + 2; a.skip = nullptr;
@@ -409,7 +445,7 @@ int mhd_diagnostics(mhd_handle *h, mhd_diag *out) {
   CK(diag(h->g, h->ph, h->f, h->diag_part, &nb, h->stream));
   std::vector<double> part((size_t)nb * 6);
   CKR(cudaMemcpyAsync(part.data(), h->diag_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CKR(cudaMemcpyAsync(h->h_small + 2, h->dtred + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+  CKR(cudaMemcpyAsync(h->h_small + 2, h->dtred + 2, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
   CKR(cudaStreamSynchronize(h->stream));
   memset(out, 0, sizeof *out);
   // fixed-order sum of the block partials (compensated)
@@ -431,6 +467,8 @@ int mhd_diagnostics(mhd_handle *h, mhd_diag *out) {
   out->time = h->time;
   out->steps = h->steps;
   out->imc_cells = (long long)h->h_small[2];
+  out->surrogate_cells = (long long)h->h_small[3];
+  out->fallback_cells = (long long)h->h_small[4];
   return check_err(h);
 }
 
@@ -448,5 +486,26 @@ int mhd_last_error(mhd_handle *h, char *buf, int len) {
 }
 
 long long mhd_kernel_launches(mhd_handle *h) { return h ? h->launches : 0; }
+
+int mhd_surrogate_load(mhd_handle *h, const float *params, float tol) {
+  if (!h || !params || !(tol > 0.0f)) return MHD_ERR_ARG;
+  if (h->p.cooling != MHD_COOL_SURROGATE) return fail(h, MHD_ERR_ARG, "handle was created without surrogate cooling");
+  CKR(cudaSetDevice(h->p.device));
+  if (!h->sur_master) {
+    CKR(cudaMalloc(&h->sur_master, SUR_NPARAM * sizeof(float)));
+    CKR(cudaMalloc(&h->sur_net, sizeof(SurNet)));
+  }
+  CKR(cudaMemcpyAsync(h->sur_master, params, SUR_NPARAM * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  CK(surrogate_pack(h->sur_master, h->sur_net, h->stream));
+  CKR(cudaStreamSynchronize(h->stream));
+  h->sur_tol = tol;
+  return MHD_OK;
+}
+
+int mhd_reset_counters(mhd_handle *h) {
+  if (!h) return MHD_ERR_ARG;
+  CKR(cudaMemsetAsync(h->dtred + 2, 0, 3 * sizeof(unsigned long long), h->stream));
+  return MHD_OK;
+}
 
 }  // extern "C"

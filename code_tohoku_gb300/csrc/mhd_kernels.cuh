@@ -36,6 +36,7 @@ struct Grid {
   int bcl[3], bcr[3];       // 1 = free boundary, otherwise periodic
   const double *x[3];       // coordinates x(-1..n+2) per direction
   const double *dx[3];      // spacings dx(-1..n+2)
+  const double *rdx[3];     // 1/(x(i)-x(i-1)), i = -1..n+2 (chosen form)
 };
 
 struct Phys {
@@ -85,6 +86,48 @@ __device__ __forceinline__ R vlim(R qm, R q0, R qp, R dxm, R dx0, R dxp, R s) {
   delm = R(2) * delm / (dx0 + dxm);
   R gmm = (R(0.5) + fsgn(R(0.5), delp * delm)) * fsgn(R(1), delp) * fmn(dab(delp), dab(delm));
   return g * (R(0.5) - s) + gmm * (R(0.5) + s);
+}
+
+// The same value as vlim(...) evaluating only the branch the switch keeps.
+// vlim returns g*(0.5-s) + gmm*(0.5+s) with s = +-0.5: one term is exactly
+// the selected slope and the other is a zero whose sign is known without
+// computing it (sign(g) = sign(qp-qm) since flmt >= +0 and the width sum is
+// positive; sign(gmm) = sign(delp)), so IEEE addition gives the selected
+// slope unless it is zero, and then -0 only when both zeros are -0.  This
+// saves the two divisions of the branch not taken; inputs beyond 1e150 take
+// the full formula (where the skipped branch could overflow to Inf/NaN).
+__device__ __forceinline__ double vlim_sel(double qm, double q0, double qp, double dxm, double dx0, double dxp,
+                                           double s) {
+  const double eps = 1e-10;
+  double delp = qp - q0;
+  double delm = q0 - qm;
+  if (!(fabs(delp) < 1e150 && fabs(delm) < 1e150)) return vlim<double>(qm, q0, qp, dxm, dx0, dxp, s);
+  double r;
+  bool zneg;   // sign of the discarded zero term
+  if (s > 0.0) {
+    // minmod kept
+    double dp = 2.0 * delp / (dx0 + dxp);
+    double dm = 2.0 * delm / (dx0 + dxm);
+    r = (0.5 + fsgn(0.5, dp * dm)) * fsgn(1.0, dp) * fmn(fabs(dp), fabs(dm));
+    zneg = signbit(qp - qm);
+  } else {
+    // van Albada kept
+    double flmt = fmx(0.0, (2.0 * delp * delm + eps) / (delp * delp + delm * delm + eps));
+    r = flmt * (qp - qm) / (dx0 + 0.5 * dxm + 0.5 * dxp);
+    zneg = signbit(delp);
+  }
+  if (r == 0.0) return (signbit(r) && zneg) ? -0.0 : 0.0;
+  return r;
+}
+__device__ __forceinline__ float vlim_sel(float qm, float q0, float qp, float dxm, float dx0, float dxp, float s) {
+  if (s > 0.0f) {
+    float dp = 2.0f * (qp - q0) / (dx0 + dxp);
+    float dm = 2.0f * (q0 - qm) / (dx0 + dxm);
+    return (dp * dm > 0.0f) ? copysignf(fminf(fabsf(dp), fabsf(dm)), dp) : 0.0f;
+  }
+  float delp = qp - q0, delm = q0 - qm;
+  float flmt = fmaxf(0.0f, __fdividef(2.0f * delp * delm + 1e-10f, delp * delp + delm * delm + 1e-10f));
+  return __fdividef(flmt * (qp - qm), dx0 + 0.5f * dxm + 0.5f * dxp);
 }
 
 template <class R>
@@ -198,11 +241,13 @@ __global__ void ghost_fill_kernel(Grid g, FillArgs a, int d, int nol, int specie
 // Shared buffers (each L*P entries, L = n+4, index (i+1)*P + p):
 enum {
   B_RHO = 0, B_V0, B_V1, B_V2, B_E, B_T1, B_T2, B_XL, B_VA, B_PA,
-  B_G0, B_G1, B_G2, B_G3, B_G4, B_S0, B_S1, B_S2, B_S3, B_S4, B_COUNT
+  B_G0, B_G1, B_G2, B_G3, B_G4, B_S0, B_S1, B_S2, B_S3, B_S4, B_BNA, B_COUNT
 };
 // B_T1/B_T2 hold Bcc transverse then Blg; B_PA holds Pa then dxlag;
 // B_S0..4 hold species (RHS), then Bn, Bay, Vay, Baz, Vaz (MOC), then the
-// remapped species (REMAP); B_G* hold slopes, the T switch and fluxes.
+// remapped species (REMAP); B_G* hold slopes, the T switch and fluxes;
+// B_XL holds the per-cell gamma during the RHS slopes, then xlag; B_BNA
+// holds the face-normal B interpolated to each Lagrangian interface.
 
 struct SweepArgs {
   Grid g;
@@ -294,11 +339,12 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
     int i = t / P, p = t % P;
     R dm = R(dxe[i]), d0 = R(dxe[i + 1]), dp = R(dxe[i + 2]);
     R s = tswitch<R>(B(B_E, i, p), B(B_RHO, i, p), kb);
+    B(B_XL, i, p) = gam_of(B(B_S0, i, p), B(B_S1, i, p), B(B_S3, i, p), B(B_S4, i, p), B(B_S2, i, p));
     const int src[5] = {B_RHO, VB(DIR), B_E, B_T1, B_T2};
 #pragma unroll
     for (int q = 0; q < 5; q++)
-      B(B_G0 + q, i, p) = (double)vlim<R>(R(B(src[q], i - 1, p)), R(B(src[q], i, p)),
-                                          R(B(src[q], i + 1, p)), dm, d0, dp, s);
+      B(B_G0 + q, i, p) = (double)vlim_sel(R(B(src[q], i - 1, p)), R(B(src[q], i, p)),
+                                           R(B(src[q], i + 1, p)), dm, d0, dp, s);
   }
   __syncthreads();
   // Riemann problem at every interface i = 0..N (:1368-1415)
@@ -310,11 +356,11 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
     double HA = B(B_S0, i, p), prA = B(B_S1, i, p), H2A = B(B_S2, i, p), HeA = B(B_S3, i, p), HepA = B(B_S4, i, p);
     double HB = B(B_S0, i + 1, p), prB = B(B_S1, i + 1, p), H2B = B(B_S2, i + 1, p), HeB = B(B_S3, i + 1, p),
            HepB = B(B_S4, i + 1, p);
-    R gamA = R(gam_of(HA, prA, HeA, HepA, H2A));
+    R gamA = R(B(B_XL, i, p));
     R cm = dsq((gamA * R(pA) + R(t1A) * R(t1A) + R(t2A) * R(t2A)) / R(rhoA));
     R depend1 = R(0.5) * (R(dxe[i + 1]) - cm * R(dt)) * R(facdep);
     depend1 = fmx(R(0), depend1);
-    R gamB = R(gam_of(HB, prB, HeB, HepB, H2B));
+    R gamB = R(B(B_XL, i + 1, p));
     cm = dsq((gamB * R(pB) + R(t1B) * R(t1B) + R(t2B) * R(t2B)) / R(rhoB));
     R depend2 = R(0.5) * (R(dxe[i + 2]) - cm * R(dt)) * R(facdep);
     depend2 = fmx(R(0), depend2);
@@ -402,8 +448,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
     const int src[5] = {B_RHO, VB(C1), VB(C2), B_T1, B_T2};
 #pragma unroll
     for (int q = 0; q < 5; q++)
-      B(B_G0 + q, i, p) = (double)vlim<R>(R(B(src[q], i - 1, p)), R(B(src[q], i, p)),
-                                          R(B(src[q], i + 1, p)), dm, d0, dp, s);
+      B(B_G0 + q, i, p) = (double)vlim_sel(R(B(src[q], i - 1, p)), R(B(src[q], i, p)),
+                                           R(B(src[q], i + 1, p)), dm, d0, dp, s);
   }
   __syncthreads();
   // characteristics at every interface (:1996-2057)
@@ -411,6 +457,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
     int i = t / P, p = t % P;
     double Bnap = B(B_S0, i + 1, p) + (B(B_XL, i, p) - xe[i + 1]) * (B(B_S0, i + 2, p) - B(B_S0, i, p)) /
                                           (xe[i + 2] - xe[i]);
+    B(B_BNA, i, p) = Bnap;
     double D0 = B(B_PA, i, p), D1 = B(B_PA, i + 1, p);
     double rA = B(B_RHO, i, p), rB = B(B_RHO, i + 1, p);
     R deni = dsq(R(D0 + D1) / (R(D0) * R(rB) + R(D1) * R(rA)));
@@ -467,10 +514,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
   // Lorentz force and induction, v -> rho v, e -> E (:2059-2093)
   for (int t = tid; t < N * P; t += nth) {
     int i = 1 + t / P, p = t % P;
-    double Bnap = B(B_S0, i + 1, p) + (B(B_XL, i, p) - xe[i + 1]) * (B(B_S0, i + 2, p) - B(B_S0, i, p)) /
-                                          (xe[i + 2] - xe[i]);
-    double Bnam = B(B_S0, i, p) + (B(B_XL, i - 1, p) - xe[i]) * (B(B_S0, i + 1, p) - B(B_S0, i - 1, p)) /
-                                      (xe[i + 1] - xe[i - 1]);
+    // Bnam at cell i is Bnap at interface i-1: the same expression
+    double Bnap = B(B_BNA, i, p), Bnam = B(B_BNA, i - 1, p);
     double Vnap = B(B_VA, i, p), Vnam = B(B_VA, i - 1, p);
     double rho = B(B_RHO, i, p), DL = B(B_PA, i, p);
     double Bay1 = B(B_S1, i, p), Bay0 = B(B_S1, i - 1, p), Vay1 = B(B_S2, i, p), Vay0 = B(B_S2, i - 1, p);
@@ -503,9 +548,9 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
   auto remap_column = [&](int b) {
     for (int t = tid; t < (N + 2) * P; t += nth) {
       int i = t / P, p = t % P;
-      B(B_G1, i, p) = (double)vlim<R>(R(B(b, i - 1, p)), R(B(b, i, p)), R(B(b, i + 1, p)),
-                                      R(B(B_PA, i - 1, p)), R(B(B_PA, i, p)), R(B(B_PA, i + 1, p)),
-                                      R(B(B_G0, i, p)));
+      B(B_G1, i, p) = (double)vlim_sel(R(B(b, i - 1, p)), R(B(b, i, p)), R(B(b, i + 1, p)),
+                                       R(B(B_PA, i - 1, p)), R(B(B_PA, i, p)), R(B(B_PA, i + 1, p)),
+                                       R(B(B_G0, i, p)));
     }
     __syncthreads();
     for (int t = tid; t < (N + 1) * P; t += nth) {
@@ -534,7 +579,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
     int b = (s < 5) ? (B_S0 + s) : B_G3;
     for (int t = tid; t < N * P; t += nth) {
       int i = 1 + t / P, p = t % P;
-      B(b, i, p) = dxe[i + 1] * A.f.sp[s][pc.at(p, i)] / (B(B_XL, i, p) - B(B_XL, i - 1, p));
+      B(b, i, p) = dxe[i + 1] * A.f.sp[s][pc.at(p, i)] / B(B_PA, i, p);   // dxlag = xlag(i)-xlag(i-1)
     }
     __syncthreads();
     const int bl[1] = {b};
@@ -616,7 +661,7 @@ __device__ __forceinline__ R face_slope(const Grid &g, const CTArgs &A, const do
   long long sd = g.st[d];
   const double *dxx = g.dx[d];
   R s = tswitch<R>(A.f.U[4][c], A.f.U[0][c], A.ph.kb);
-  return vlim<R>(R(q[c - sd]), R(q[c]), R(q[c + sd]), R(dxx[pos]), R(dxx[pos + 1]), R(dxx[pos + 2]), s);
+  return vlim_sel(R(q[c - sd]), R(q[c]), R(q[c + sd]), R(dxx[pos]), R(dxx[pos + 1]), R(dxx[pos + 2]), s);
 }
 
 // CC(2) + CCT for the edge direction E (0: Ez on x/y, 1: Ex on y/z,

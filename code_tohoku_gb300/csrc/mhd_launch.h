@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "mhd_kernels.cuh"
+#include "mhd_source32.cuh"
 
 namespace mhd {
 
@@ -18,6 +19,9 @@ cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s);
 // chosen form (FP32 reconstruction / Riemann / characteristics)
 cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s);
 cudaError_t emf_fp32(int e, const CTArgs &a, cudaStream_t s);
+cudaError_t source_fp32(const Source32Args &a, cudaStream_t s);
+// pack FP32 master surrogate parameters into the BF16 device network
+cudaError_t surrogate_pack(const float *master, SurNet *net, cudaStream_t s);
 
 // precision-independent FP64 kernels (built in the FP64 unit)
 cudaError_t ghost_fill(const Grid &g, const FillArgs &f, int dir, int nol, int species, cudaStream_t s);

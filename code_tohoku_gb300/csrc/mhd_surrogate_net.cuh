@@ -1,0 +1,171 @@
+// mhd_surrogate_net.cuh — the KI-cooling surrogate network on tensor cores.
+//
+// The stiff branch of SOURCE solves P + Lambda(P) dt (gamma-1) = P_old by a
+// 30-step log-space bisection (IMC, MCF3DSGincfca3.f90:2898-2921).  Written
+// in temperature, the solution depends only on
+//   x0 = log10 N      (N = rho/1.27, the KI cooling density)
+//   x1 = log10 T      (T in 1e3 K at the start of the solve)
+//   x2 = log10(dt/t_cool),  t_cool = P/((gamma-1)|Lambda|)
+// and the network maps (x0,x1,x2) -> (log10(T_new/T), c), where c is a
+// learned estimate of log10 of its own error.  Layers 3->64->64->2 with SiLU;
+// operands are BF16 (mma.sync m16n8k16, FP32 accumulate), biases FP32.
+//
+// Fragment layouts follow the PTX ISA for mma.m16n8k16 with .bf16: lane
+// l = 4g + t holds A rows g and g+8, columns 2t,2t+1 (and +8); B column g,
+// rows 2t,2t+1 (and +8); the accumulator rows g, g+8, columns 2t, 2t+1.
+// The accumulator of one layer is repacked in registers as the A operand
+// of the next, so a warp evaluates 16 samples per tile without shared
+// memory.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace mhd {
+
+constexpr int SUR_H = 64;           // hidden width
+constexpr int SUR_NPARAM = 64 * 3 + 64 + 64 * 64 + 64 + 2 * 64 + 2;   // FP32 master parameters
+// offsets in the FP32 master vector: W1[64][3], b1, W2[64][64], b2, W3[2][64], b3
+constexpr int SUR_OW1 = 0, SUR_OB1 = 192, SUR_OW2 = 256, SUR_OB2 = 256 + 4096, SUR_OW3 = SUR_OB2 + 64,
+              SUR_OB3 = SUR_OW3 + 128;
+
+// input normalisation: box [-2,5] x [-2, log10 20] x [-3,3] -> [-1,1]^3
+constexpr float SUR_C0 = 1.5f, SUR_S0 = 3.5f;
+constexpr float SUR_C1 = -0.3494850f, SUR_S1 = 1.6505150f;
+constexpr float SUR_C2 = 0.0f, SUR_S2 = 3.0f;
+
+// packed device copy used by the kernels
+struct SurNet {
+  __nv_bfloat16 W1[64 * 16];    // [out][in padded to 16]
+  __nv_bfloat16 W2[64 * 64];    // [out][in]
+  __nv_bfloat16 W2T[64 * 64];   // [in][out]   (backward: dh1 = dz2 W2)
+  __nv_bfloat16 W3[8 * 64];     // [out padded to 8][in]
+  float b1[64], b2[64], b3[8];
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return z * sigm(z); }
+__device__ __forceinline__ float dsilu(float z) {
+  float s = sigm(z);
+  return s * (1.0f + z * (1.0f - s));
+}
+
+// First layer on the CUDA cores in FP32 (3 inputs are too few for a
+// tensor-core tile, and BF16 inputs would quantise log T to 0.3%): the
+// weights are the BF16-rounded values, the products and sums FP32.  Each
+// lane computes the entries it owns in the accumulator layout (rows g, g+8;
+// columns 8nt+2t, 8nt+2t+1), so the result feeds act_frags directly.
+__device__ __forceinline__ void layer1_fp32(const SurNet *net, float n0, float n1, float n2, int rowbase,
+                                            float (&z)[8][4]) {
+  int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  float a0 = __shfl_sync(0xffffffffu, n0, rowbase + g), a1 = __shfl_sync(0xffffffffu, n1, rowbase + g),
+        a2 = __shfl_sync(0xffffffffu, n2, rowbase + g);
+  float c0 = __shfl_sync(0xffffffffu, n0, rowbase + g + 8), c1 = __shfl_sync(0xffffffffu, n1, rowbase + g + 8),
+        c2 = __shfl_sync(0xffffffffu, n2, rowbase + g + 8);
+#pragma unroll
+  for (int nt = 0; nt < 8; nt++) {
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      int n = nt * 8 + 2 * t + q;
+      const __nv_bfloat16 *w = net->W1 + n * 16;
+      float w0 = __bfloat162float(w[0]), w1 = __bfloat162float(w[1]), w2 = __bfloat162float(w[2]);
+      float b = net->b1[n];
+      z[nt][q] = b + w0 * a0 + w1 * a1 + w2 * a2;
+      z[nt][2 + q] = b + w0 * c0 + w1 * c1 + w2 * c2;
+    }
+  }
+}
+
+// z = A W^T + b for a 64-wide layer; W is [64][K] bf16 with K = 16*nk
+template <int NK>
+__device__ __forceinline__ void layer64(const __nv_bfloat16 *W, const float *b, const uint32_t (&a)[NK][4],
+                                        float (&z)[8][4]) {
+  int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int nt = 0; nt < 8; nt++) {
+    float b0 = b[nt * 8 + 2 * t], b1 = b[nt * 8 + 2 * t + 1];
+    z[nt][0] = b0; z[nt][1] = b1; z[nt][2] = b0; z[nt][3] = b1;
+    const __nv_bfloat16 *row = W + (nt * 8 + g) * (16 * NK);
+#pragma unroll
+    for (int kt = 0; kt < NK; kt++) mma_bf16(z[nt], a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
+  }
+}
+
+// accumulator (16 x 64) -> four A fragments of the next layer after SiLU
+__device__ __forceinline__ void act_frags(const float (&z)[8][4], uint32_t (&a)[4][4]) {
+#pragma unroll
+  for (int kt = 0; kt < 4; kt++) {
+    a[kt][0] = pack_bf16(silu(z[2 * kt][0]), silu(z[2 * kt][1]));
+    a[kt][1] = pack_bf16(silu(z[2 * kt][2]), silu(z[2 * kt][3]));
+    a[kt][2] = pack_bf16(silu(z[2 * kt + 1][0]), silu(z[2 * kt + 1][1]));
+    a[kt][3] = pack_bf16(silu(z[2 * kt + 1][2]), silu(z[2 * kt + 1][3]));
+  }
+}
+
+// output layer: y (16 x 8, columns 0,1 used) = A W3^T + b3
+__device__ __forceinline__ void layer_out(const SurNet *net, const uint32_t (&a)[4][4], float (&y)[4]) {
+  int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  float b0 = net->b3[2 * t], b1 = net->b3[2 * t + 1];
+  y[0] = b0; y[1] = b1; y[2] = b0; y[3] = b1;
+  const __nv_bfloat16 *row = net->W3 + g * 64;
+#pragma unroll
+  for (int kt = 0; kt < 4; kt++) mma_bf16(y, a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
+}
+
+// forward pass of the 16 samples whose inputs sit in lanes rowbase..rowbase+15;
+// returns (out0, out1) for the sample of lanes rowbase+r in that lane.
+__device__ __forceinline__ void net_forward16(const SurNet *net, float n0, float n1, float n2, int rowbase,
+                                              float &o0, float &o1) {
+  float z1[8][4];
+  layer1_fp32(net, n0, n1, n2, rowbase, z1);
+  uint32_t a1[4][4];
+  act_frags(z1, a1);
+  float z2[8][4];
+  layer64<4>(net->W2, net->b2, a1, z2);
+  uint32_t a2[4][4];
+  act_frags(z2, a2);
+  float y[4];
+  layer_out(net, a2, y);
+  // row r of the tile: r < 8 at lane 4r (y0,y1), r >= 8 at lane 4(r-8) (y2,y3)
+  int lane = threadIdx.x & 31;
+  int r = lane - rowbase;
+  int src = ((r & 7) << 2);
+  float v0 = __shfl_sync(0xffffffffu, y[0], src), v1 = __shfl_sync(0xffffffffu, y[1], src);
+  float v2 = __shfl_sync(0xffffffffu, y[2], src), v3 = __shfl_sync(0xffffffffu, y[3], src);
+  o0 = (r < 8) ? v0 : v2;
+  o1 = (r < 8) ? v1 : v3;
+}
+
+// Whole-warp inference: every lane brings one sample (all 32 lanes must
+// call).  Returns log10(T_new/T) and writes the confidence estimate.
+__device__ __forceinline__ float surrogate_warp(const SurNet *net, float x0, float x1, float x2, bool active,
+                                                float *conf) {
+  float n0 = active ? (x0 - SUR_C0) / SUR_S0 : 0.0f;
+  float n1 = active ? (x1 - SUR_C1) / SUR_S1 : 0.0f;
+  float n2 = active ? (x2 - SUR_C2) / SUR_S2 : 0.0f;
+  float o0a, o1a, o0b, o1b;
+  unsigned any = __ballot_sync(0xffffffffu, active);
+  o0a = o1a = o0b = o1b = 0.0f;
+  if (any & 0x0000ffffu) net_forward16(net, n0, n1, n2, 0, o0a, o1a);
+  if (any & 0xffff0000u) net_forward16(net, n0, n1, n2, 16, o0b, o1b);
+  int lane = threadIdx.x & 31;
+  *conf = lane < 16 ? o1a : o1b;
+  return lane < 16 ? o0a : o0b;
+}
+
+}  // namespace mhd

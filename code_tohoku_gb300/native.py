@@ -24,7 +24,8 @@ COOL_EXACT, COOL_SURROGATE = 0, 1
 EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_timestep", "mhd_source",
            "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_evolve", "mhd_get_time",
            "mhd_set_time", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
-           "mhd_kernel_launches")
+           "mhd_kernel_launches", "mhd_reset_counters", "mhd_surrogate_nparams", "mhd_surrogate_load",
+           "mhd_surrogate_train", "mhd_surrogate_label", "mhd_surrogate_eval", "mhd_surrogate_grad")
 
 
 class MhdError(RuntimeError):
@@ -95,12 +96,76 @@ def load(build_if_missing=True):
         fn.restype = ctypes.c_int
     L.mhd_kernel_launches.argtypes = [H]
     L.mhd_kernel_launches.restype = ctypes.c_longlong
+    F = ctypes.POINTER(ctypes.c_float)
+    L.mhd_reset_counters.argtypes = [H]
+    L.mhd_reset_counters.restype = ctypes.c_int
+    L.mhd_surrogate_nparams.argtypes = []
+    L.mhd_surrogate_nparams.restype = ctypes.c_int
+    L.mhd_surrogate_load.argtypes = [H, F, ctypes.c_float]
+    L.mhd_surrogate_load.restype = ctypes.c_int
+    L.mhd_surrogate_train.argtypes = [F, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                      ctypes.c_ulonglong, F, ctypes.c_int]
+    L.mhd_surrogate_train.restype = ctypes.c_int
+    L.mhd_surrogate_label.argtypes = [F, F, ctypes.c_longlong, ctypes.c_double, ctypes.c_int]
+    L.mhd_surrogate_label.restype = ctypes.c_int
+    L.mhd_surrogate_eval.argtypes = [F, F, F, ctypes.c_longlong, ctypes.c_int]
+    L.mhd_surrogate_eval.restype = ctypes.c_int
+    L.mhd_surrogate_grad.argtypes = [F, F, F, ctypes.c_longlong, F, F, ctypes.c_int]
+    L.mhd_surrogate_grad.restype = ctypes.c_int
     _lib = L
     return L
 
 
 def _ptr(a):
     return a.ctypes.data_as(_P)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _sck(r, what):
+    if r != MHD_OK:
+        raise MhdError(r, what)
+
+
+def surrogate_nparams():
+    return load().mhd_surrogate_nparams()
+
+
+def surrogate_train(params, n_data=1 << 24, batch=65536, steps=4000, lr=1e-3, seed=1, device=0):
+    """Trains in place on the GPU; returns (params, per-step batch MSE)."""
+    p = np.ascontiguousarray(params, dtype=np.float32).copy()
+    hist = np.zeros(max(steps, 1), dtype=np.float32)
+    _sck(load().mhd_surrogate_train(_fptr(p), n_data, batch, steps, lr, seed, _fptr(hist), device),
+         "mhd_surrogate_train")
+    return p, hist[:steps]
+
+
+def surrogate_label(x, kb=8.63359, device=0):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.zeros(len(x), dtype=np.float32)
+    _sck(load().mhd_surrogate_label(_fptr(x), _fptr(y), len(x), kb, device), "mhd_surrogate_label")
+    return y
+
+
+def surrogate_eval(params, x, device=0):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.zeros((len(x), 2), dtype=np.float32)
+    _sck(load().mhd_surrogate_eval(_fptr(p), _fptr(x), _fptr(out), len(x), device), "mhd_surrogate_eval")
+    return out
+
+
+def surrogate_grad(params, x, y, device=0):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    g = np.zeros(len(p), dtype=np.float32)
+    loss = np.zeros(1, dtype=np.float32)
+    _sck(load().mhd_surrogate_grad(_fptr(p), _fptr(x), _fptr(y), len(x), _fptr(g), _fptr(loss), device),
+         "mhd_surrogate_grad")
+    return g, float(loss[0])
 
 
 def params_struct(p: MhdParams, precision=PREC_FP64, cooling=COOL_EXACT, device=0):
@@ -202,6 +267,13 @@ class Mhd3D:
 
     def set_stream(self, stream_ptr):
         self._ck(self.L.mhd_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def surrogate_load(self, params, tol=1e-3):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._ck(self.L.mhd_surrogate_load(self.h, _fptr(p), tol))
+
+    def reset_counters(self):
+        self._ck(self.L.mhd_reset_counters(self.h))
 
     @property
     def kernel_launches(self):

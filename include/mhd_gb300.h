@@ -121,6 +121,35 @@ int mhd_set_stream(mhd_handle *h, void *stream);
 int mhd_last_error(mhd_handle *h, char *buf, int len);
 /* Number of kernels launched by this handle since creation. */
 long long mhd_kernel_launches(mhd_handle *h);
+/* Zeroes the IMC / surrogate / fallback cell counters of mhd_diagnostics. */
+int mhd_reset_counters(mhd_handle *h);
+
+/* ---- KI-cooling surrogate (chosen form; no counterpart in the reference,
+ * whose stiff cells always take IMC, MCF3DSGincfca3.f90:2898-2921) ----
+ * A 3->64->64->2 SiLU network maps (log10 N, log10 T, log10 dt/t_cool) to
+ * log10(T_new/T) and a confidence; its FP32 master parameters are a vector
+ * of mhd_surrogate_nparams() floats (W1[64][3], b1, W2[64][64], b2,
+ * W3[2][64], b3).  Stiff cells inside the training box take the network's
+ * answer polished by two Newton steps; a cell whose implicit residual
+ * |P + Lambda(P) dt (gamma-1) - P_old| / P_old exceeds tol falls back to
+ * the bisection. */
+int mhd_surrogate_nparams(void);
+/* Attaches a network to a handle created with cooling = MHD_COOL_SURROGATE. */
+int mhd_surrogate_load(mhd_handle *h, const float *params, float tol);
+/* Trains params in place on n_data states drawn log-uniformly in the box
+ * N in [1e-2,1e5] cm^-3, T in [10 K, 2e4 K], dt/t_cool in [1e-3,1e3] and
+ * labelled by the plain integrator (FP64 IMC); Adam, batch, steps, lr.
+ * history[steps] (may be NULL) gets each batch's mean squared error. */
+int mhd_surrogate_train(float *params, long long n_data, int batch, int steps, float lr,
+                        unsigned long long seed, float *history, int device);
+/* Plain-integrator labels log10(T_new/T) for inputs x[n][3]. */
+int mhd_surrogate_label(const float *x, float *y, long long n, double kb, int device);
+/* Network outputs out[n][2] for inputs x[n][3] (the fused kernel's code). */
+int mhd_surrogate_eval(const float *params, const float *x, float *out, long long n, int device);
+/* Gradient of the mean loss over (x, y) at params, computed by the
+ * training kernels; loss gets the mean squared error. */
+int mhd_surrogate_grad(const float *params, const float *x, const float *y, long long n, float *grad,
+                       float *loss, int device);
 
 #ifdef __cplusplus
 }

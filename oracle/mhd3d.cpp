@@ -706,8 +706,8 @@ struct Mhd3D {
   }
 
   // ---------------------------------------------------------- source
-  double Fcool(double T, size_t c) {   // KI form, KIcool/1DMHDwCC3.f90:1166-1173
-    double NN = U[1][c] / 1.27;
+  double Fcool(double T, size_t c) { return FcoolN(T, U[1][c] / 1.27); }
+  static double FcoolN(double T, double NN) {   // KI form, KIcool/1DMHDwCC3.f90:1166-1173
     double AbsL = 3.94656e1, T0 = 1.0e3;
     double Laml = 1.0e7 * detmath::exp(-1.184e5 / (T * T0 + 1.0e3));
     Laml = fmin2(Laml, 5.e3);
@@ -715,12 +715,13 @@ struct Mhd3D {
     return (NN * NN * (Laml + Lamc) - NN) * AbsL;
   }
 
-  void IMC(double &Pv, double n, double dt, double g1c, size_t c) {   // :2898-2921
+  // IMC (:2898-2921) with the KI density NN of the cell
+  static void IMC(double &Pv, double n, double dt, double g1c, double NN, double kb) {
     double Pu = 1.e10, Pd = 1.e-10, Pm = 1.e1, Pmold = -1.0;
-    double nkbi = 1.0 / (P.kb * n);
+    double nkbi = 1.0 / (kb * n);
     for (int kkk = 1; kkk <= 30; kkk++) {
       double T = Pm * nkbi;
-      double CooL = Fcool(T, c);
+      double CooL = FcoolN(T, NN);
       double fev = Pm + CooL * dt * g1c - Pv;
       double iud = fsign(1.0, fev);
       Pd = fmax2(-iud * Pm, Pd);
@@ -774,14 +775,14 @@ struct Mhd3D {
           if (dt <= 0.2 * Pn[a] / (g1c * std::fabs(CooL))) {
             U[5][a] = U[5][a] - g1c * CooL * dt * 0.5;
           } else {
-            IMC(U[5][a], nimc(a), dt * 0.5, g1c, a);
+            IMC(U[5][a], nimc(a), dt * 0.5, g1c, U[1][a] / 1.27, P.kb);
           }
         } else {
           if (dt <= 0.2 * Pn[a] / (g1c * std::fabs(CooL))) {
             U[5][a] = Pn[a] - g1c * CooL * dt;
           } else {
             double pv = Pn[a];
-            IMC(pv, nimc(a), dt, g1c, a);
+            IMC(pv, nimc(a), dt, g1c, U[1][a] / 1.27, P.kb);
             U[5][a] = pv;
           }
         }
@@ -948,5 +949,19 @@ double o3d_step(void *h, double tsave, int *st) {
 }
 
 void o3d_destroy(void *h) { delete static_cast<Mhd3D *>(h); }
+
+// The plain integrator's answer for one surrogate input point: with the KI
+// density N = 10^x0, T = 10^x1 (1e3 K) and dt/t_cool = 10^x2, solve
+// P + Lambda(P) c = P_old with IMC (c = dt (gamma-1), n = N) and return
+// log10(T_new/T).  Same restated IMC and Fcool as the 3D step.
+double o3d_ki_label(double x0, double x1, double x2, double kb) {
+  double N = detmath::exp10(x0), T = detmath::exp10(x1), r = detmath::exp10(x2);
+  double L = Mhd3D::FcoolN(T, N);
+  if (L == 0.0) return 0.0;
+  double Pv = kb * N * T;
+  double cc = r * Pv / std::fabs(L);
+  Mhd3D::IMC(Pv, N, cc, 1.0, N, kb);
+  return detmath::log10((Pv / (kb * N)) / T);
+}
 
 }  // extern "C"

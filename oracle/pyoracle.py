@@ -59,6 +59,8 @@ def lib():
         L.o3d_step.restype = ctypes.c_double
         L.o3d_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
         L.o3d_destroy.argtypes = [ctypes.c_void_p]
+        L.o3d_ki_label.restype = ctypes.c_double
+        L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
     return _lib
 
@@ -158,3 +160,9 @@ class Oracle3D:
         if getattr(self, "h", None):
             lib().o3d_destroy(self.h)
             self.h = None
+
+
+def ki_labels(x, kb=8.63359):
+    """The oracle's IMC answer log10(T_new/T) for surrogate inputs x[n][3]."""
+    L = lib()
+    return np.array([L.o3d_ki_label(float(a), float(b), float(c), kb) for a, b, c in x])

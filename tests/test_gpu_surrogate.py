@@ -1,0 +1,115 @@
+"""The learned part: the KI-cooling surrogate and the FP32 source.
+
+* labels from the GPU's plain integrator equal the oracle's IMC bit for bit
+* the training kernels' gradients agree with the NumPy restatement
+  (oracle/surrogate_ref.py, same BF16 rounding points)
+* training on the GPU lowers the loss
+* inside SOURCE the trained network takes over most stiff cells, and the
+  result stays within the implicit-residual tolerance of the exact solve
+"""
+import numpy as np
+import pytest
+
+from code_tohoku_gb300 import native, problems
+from oracle import pyoracle
+from oracle import surrogate_ref as S
+
+pytestmark = pytest.mark.gpu
+
+BOX_LO = np.array([-2.0, -2.0, -3.0])
+BOX_HI = np.array([5.0, np.log10(20.0), 3.0])
+
+
+def sample(n, seed):
+    return np.random.default_rng(seed).uniform(BOX_LO, BOX_HI, (n, 3)).astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def trained():
+    p0 = S.init_params(0)
+    p, hist = native.surrogate_train(p0, n_data=1 << 20, batch=8192, steps=3000, lr=1e-3, seed=3)
+    return p, hist
+
+
+def test_labels_bit_exact_vs_oracle():
+    x = sample(3000, 1)
+    gpu = native.surrogate_label(x)
+    cpu = pyoracle.ki_labels(x).astype(np.float32)
+    assert np.array_equal(gpu, cpu)
+
+
+def test_training_gradients_match_numpy():
+    p = S.init_params(5)
+    x = sample(1024, 2)
+    y = pyoracle.ki_labels(x).astype(np.float32)
+    g_gpu, loss_gpu = native.surrogate_grad(p, x, y)
+    g_cpu, loss_cpu = S.grad(p, x, y)
+    assert abs(loss_gpu - loss_cpu) <= 1e-4 * abs(loss_cpu) + 1e-7
+    rel = np.linalg.norm(g_gpu - g_cpu) / np.linalg.norm(g_cpu)
+    cos = float(g_gpu @ g_cpu / (np.linalg.norm(g_gpu) * np.linalg.norm(g_cpu)))
+    assert rel < 2e-2 and cos > 0.9998, (rel, cos)
+    # every parameter block, not only the large ones
+    for lo, hi in ((0, 192), (192, 256), (256, 4352), (4352, 4416), (4416, 4544), (4544, 4546)):
+        a, b = g_gpu[lo:hi], g_cpu[lo:hi]
+        assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b) + 1e-9, (lo, hi)
+
+
+def test_training_lowers_loss(trained):
+    p, hist = trained
+    assert np.all(np.isfinite(hist))
+    assert hist[-50:].mean() < 0.05 * hist[:10].mean()
+    x = sample(20000, 9)
+    y = native.surrogate_label(x)
+    out = native.surrogate_eval(p, x)
+    err = np.abs(out[:, 0] - y)
+    assert np.median(err) < 0.05, np.median(err)
+
+
+def stiff_state(n=32):
+    """Colliding-flow state, dense enough that most cells cool faster than
+    the forced step below (stiff)."""
+    st = problems.colliding_flows(n)
+    st.U[0] *= 30.0
+    st.species *= 30.0
+    return st
+
+
+def test_fp32_source_matches_fp64():
+    st = problems.colliding_flows(32)
+    g64 = native.Mhd3D(st.params, precision=native.PREC_FP64)
+    g32 = native.Mhd3D(st.params, precision=native.PREC_FP32)
+    g64.upload(st)
+    g32.upload(st)
+    dt, _ = g64.timestep()
+    g64.source(dt)
+    g32.source(dt)
+    p64 = g64.download()[0][4][2:-2, 2:-2, 2:-2]
+    p32 = g32.download()[0][4][2:-2, 2:-2, 2:-2]
+    assert np.abs(p32 - p64).mean() / np.abs(p64).mean() < 1e-5
+
+
+def test_surrogate_takes_over_stiff_cells(trained):
+    p, _ = trained
+    st = stiff_state()
+    dt = 0.05
+    runs = {}
+    for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
+                             ("exact", native.PREC_FP32, native.COOL_EXACT),
+                             ("surrogate", native.PREC_FP32, native.COOL_SURROGATE)):
+        g = native.Mhd3D(st.params, precision=prec, cooling=cool)
+        if cool == native.COOL_SURROGATE:
+            g.surrogate_load(p, 1e-3)
+        g.upload(st)
+        g.source(dt)
+        d = g.diagnostics()
+        runs[name] = (g.download()[0][4][2:-2, 2:-2, 2:-2], d)
+    p64 = runs["fp64"][0]
+    n_stiff = runs["exact"][1]["imc_cells"]
+    d = runs["surrogate"][1]
+    assert n_stiff > 0.5 * 2 * 32 ** 3            # both passes, most cells stiff
+    assert d["surrogate_cells"] + d["imc_cells"] == n_stiff
+    # the gain: most bisection solves replaced by the network
+    assert d["surrogate_cells"] >= 0.5 * n_stiff, d
+    for name in ("exact", "surrogate"):
+        l1 = np.abs(runs[name][0] - p64).mean() / np.abs(p64).mean()
+        assert l1 < 1e-3, (name, l1)
