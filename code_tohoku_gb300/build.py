@@ -25,6 +25,7 @@ UNITS = {
     "mhd_fp32.cu": ["--fmad=true"],
     "mhd_capi.cu": ["--fmad=false"],
     "mhd_surrogate.cu": ["--fmad=false"],
+    "mhd_noalloc.cu": ["--fmad=false"],
 }
 
 

@@ -16,7 +16,8 @@ from .problems import MhdParams, MhdState
 
 MHD_OK = 0
 ERRORS = {1: "MHD_ERR_ARG", 2: "MHD_ERR_CUDA", 3: "MHD_ERR_NONFINITE", 4: "MHD_ERR_DT",
-          5: "MHD_ERR_STATE", 6: "MHD_ERR_NO_DEVICE"}
+          5: "MHD_ERR_STATE", 6: "MHD_ERR_NO_DEVICE", 7: "MHD_ERR_TOO_LARGE"}
+NOALLOC_MAX_CELLS = 16777216
 PREC_FP64, PREC_FP32 = 0, 1
 COOL_EXACT, COOL_SURROGATE = 0, 1
 
@@ -25,7 +26,8 @@ EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_times
            "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_evolve", "mhd_get_time",
            "mhd_set_time", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
            "mhd_kernel_launches", "mhd_reset_counters", "mhd_surrogate_nparams", "mhd_surrogate_load",
-           "mhd_surrogate_train", "mhd_surrogate_label", "mhd_surrogate_eval", "mhd_surrogate_grad")
+           "mhd_surrogate_train", "mhd_surrogate_label", "mhd_surrogate_eval", "mhd_surrogate_grad",
+           "mhd_timestep_noalloc")
 
 
 class MhdError(RuntimeError):
@@ -49,6 +51,12 @@ class _Diag(ctypes.Structure):
                 ("divb_max", ctypes.c_double), ("time", ctypes.c_double), ("steps", ctypes.c_longlong),
                 ("imc_cells", ctypes.c_longlong), ("surrogate_cells", ctypes.c_longlong),
                 ("fallback_cells", ctypes.c_longlong)]
+
+
+class DeviceState(ctypes.Structure):
+    """Device pointers (as integers) of arrays in the mhd_upload layout."""
+    _fields_ = [("U", ctypes.c_void_p), ("species", ctypes.c_void_p), ("bcc", ctypes.c_void_p),
+                ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p), ("dz", ctypes.c_void_p)]
 
 
 _lib = None
@@ -112,6 +120,9 @@ def load(build_if_missing=True):
     L.mhd_surrogate_eval.restype = ctypes.c_int
     L.mhd_surrogate_grad.argtypes = [F, F, F, ctypes.c_longlong, F, F, ctypes.c_int]
     L.mhd_surrogate_grad.restype = ctypes.c_int
+    L.mhd_timestep_noalloc.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(DeviceState), _P,
+                                       ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
+    L.mhd_timestep_noalloc.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -166,6 +177,18 @@ def surrogate_grad(params, x, y, device=0):
     _sck(load().mhd_surrogate_grad(_fptr(p), _fptr(x), _fptr(y), len(x), _fptr(g), _fptr(loss), device),
          "mhd_surrogate_grad")
     return g, float(loss[0])
+
+
+def timestep_noalloc(params: MhdParams, dev_state: DeviceState, stream=None, device=0):
+    """mhd_timestep_noalloc: (dt, limiter) from device arrays the caller owns;
+    no device memory is allocated by the library."""
+    ps = params_struct(params, device=device)
+    dt = ctypes.c_double()
+    st = ctypes.c_int()
+    r = load().mhd_timestep_noalloc(ctypes.byref(ps), ctypes.byref(dev_state), ctypes.byref(dt),
+                                    ctypes.byref(st), ctypes.c_void_p(stream) if stream else None)
+    _sck(r, "mhd_timestep_noalloc")
+    return dt.value, st.value
 
 
 def params_struct(p: MhdParams, precision=PREC_FP64, cooling=COOL_EXACT, device=0):

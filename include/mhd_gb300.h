@@ -49,6 +49,7 @@ extern "C" {
 #define MHD_ERR_DT 4           /* dt <= 0 or not finite ('err at Couran')   */
 #define MHD_ERR_STATE 5        /* call out of order (e.g. no upload yet)    */
 #define MHD_ERR_NO_DEVICE 6    /* no CUDA device / kernels not loadable     */
+#define MHD_ERR_TOO_LARGE 7    /* grid beyond MHD_NOALLOC_MAX_CELLS          */
 
 #define MHD_PREC_FP64 0        /* plain form: every operation in FP64       */
 #define MHD_PREC_FP32 1        /* FP32 reconstruction/flux, FP64 accumulate */
@@ -150,6 +151,32 @@ int mhd_surrogate_eval(const float *params, const float *x, float *out, long lon
  * training kernels; loss gets the mean squared error. */
 int mhd_surrogate_grad(const float *params, const float *x, const float *y, long long n, float *grad,
                        float *loss, int device);
+
+/* ---- Time-step limits without device allocation ----
+ * No counterpart in the reference (which has no device memory at all).
+ * mhd_timestep needs a handle, and a handle allocates its state with
+ * cudaMalloc.  Callers that cannot allocate device memory -- a code that
+ * owns every device array through its own pool or arena, or one running
+ * where new allocations are not allowed -- call this instead with device
+ * pointers to arrays they already have, in the layout of mhd_upload: U
+ * (8 blocks), species (8 blocks), Bcc (3 blocks, the cell-centred field of
+ * CC(4)) and dx, dy, dz (n+4 each).  The result equals mhd_timestep's.
+ *
+ * The kernels' scratch is a fixed file-scope device array (about 1 MB) that
+ * every GPU loading the library keeps until exit, so grids are limited to
+ * MHD_NOALLOC_MAX_CELLS interior cells (256^3); larger grids return
+ * MHD_ERR_TOO_LARGE before any GPU work.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the one array, so calls
+ * whose kernels overlap on the GPU (different streams, or different host
+ * threads, at the same time) race; the call synchronises its stream before
+ * returning.  stream may be NULL (the legacy default stream). */
+#define MHD_NOALLOC_MAX_CELLS 16777216LL
+typedef struct mhd_device_state {
+  const double *U, *species, *bcc;
+  const double *dx, *dy, *dz;
+} mhd_device_state;
+int mhd_timestep_noalloc(const mhd_params *p, const mhd_device_state *s, double *dt, int *st, void *stream);
 
 #ifdef __cplusplus
 }
