@@ -317,7 +317,7 @@ def main():
     achieved = B_ALG_SWEEP * n3 / (sweep_ms * 1e-3) / 1e9
     tr = ncu_traffic()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": tr * n3 if tr else None, "kernel": "sweep_kernel<float> (fused RHS+MOC+REMAP)",
+            "traffic": tr * n3 if tr else None, "kernel": "sweep32_kernel (fused RHS+MOC+REMAP, FP32 recon/flux + FP64 accumulation)",
             "peak_source": f"{which} (MEASURED_PEAKS.json hbm_gbs)" if which == "measured" else which,
             "algorithmic_bytes_per_zone": B_ALG_SWEEP}
     line = {"metric": "zone-updates/s, 256^3 MHD+KI cool: FP32+surrogate vs plain FP64 at stated L1 err",

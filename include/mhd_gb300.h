@@ -4,7 +4,7 @@
  * inside EVOLVE (:562-657) by calling Fortran subroutines on module arrays.
  * Each entry point below replaces one of those calls, so the Fortran driver,
  * its decks (INPUT3D.DAT) and its output writers stay as they are and a
- * bind(C) interface module routes the calls here (see INTEGRATION.md):
+ * bind(C) interface module routes the calls here:
  *
  *   mhd_timestep      Couran :1912-1930 + Stblty :2784-2822 + the dt
  *                     gather/min/bcast of EVOLVE :569-599
