@@ -3,7 +3,8 @@
 Three translation units are compiled in parallel with nvcc and linked into
 one shared library next to this file:
   csrc/mhd_fp64.cu  plain FP64 kernels, --fmad=false (bit-exact arithmetic)
-  csrc/mhd_fp32.cu  FP32 reconstruction/flux kernels (contraction allowed)
+  csrc/mhd_fp32.cu  FP32 reconstruction/flux kernels (contraction allowed, FP32
+                    denormals flushed, approximate FP32 division and square root)
   csrc/mhd_capi.cu  the extern "C" boundary of include/mhd_gb300.h
   csrc/mhd_surrogate.cu  surrogate data, training and evaluation kernels
                     (--fmad=false: its FP64 labels match the CPU IMC bit for bit)
@@ -22,7 +23,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
 UNITS = {
     "mhd_fp64.cu": ["--fmad=false"],
-    "mhd_fp32.cu": ["--fmad=true"],
+    "mhd_fp32.cu": ["--fmad=true", "-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "mhd_capi.cu": ["--fmad=false"],
     "mhd_surrogate.cu": ["--fmad=false"],
     "mhd_noalloc.cu": ["--fmad=false"],

@@ -31,6 +31,15 @@ struct mhd_handle {
   double *vf[3] = {nullptr, nullptr, nullptr};
   double *emf[3] = {nullptr, nullptr, nullptr};
   double *pnew = nullptr;
+  // chosen form only: FP32 scratch (cell temperatures for SOURCE; face
+  // velocities, face B, rho, T switch and EMFs for CT) and FP32 widths
+  float *fblock = nullptr;
+  float *temp32 = nullptr;
+  float *vf32[3] = {nullptr, nullptr, nullptr};
+  float *bf32[3] = {nullptr, nullptr, nullptr};
+  float *rn32 = nullptr, *sw32 = nullptr;
+  float *emf32[3] = {nullptr, nullptr, nullptr};
+  float *coordsf = nullptr;
   double *divv = nullptr;
   double *diag_part = nullptr;
   unsigned long long *dtred = nullptr;   // [0] tCFL, [1] tLMT bits, [2] IMC, [3] surrogate, [4] fallback
@@ -45,7 +54,8 @@ struct mhd_handle {
   long long launches = 0;
   long long imc_cells = 0;
   bool uploaded = false;
-  std::vector<double> rdx_host;
+  std::vector<double> rdx_host, rdxc_host;   // staging for the async coordinate copies
+  std::vector<float> dxf_host;
   std::string msg;
 };
 
@@ -153,10 +163,11 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   for (int c = 0; c < 3; c++) { h->vf[c] = q; q += g.ncell; }
   for (int c = 0; c < 3; c++) { h->emf[c] = q; q += g.ncell; }
   h->pnew = q;
-  size_t ncoord = 3 * (size_t)(g.s[0] + g.s[1] + g.s[2]);
+  size_t ncoord = 4 * (size_t)(g.s[0] + g.s[1] + g.s[2]);
   size_t ndivv = 2 * 12 * (size_t)(g.n[1] + 2) * (g.n[2] + 2);
   size_t ndiag = 6 * (size_t)((g.n[0] * (long long)g.n[1] * g.n[2] + 255) / 256);
   bool ok = cudaMalloc(&h->coords, ncoord * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&h->coordsf, (size_t)(g.s[0] + g.s[1] + g.s[2]) * sizeof(float)) == cudaSuccess &&
             cudaMalloc(&h->divv, ndivv * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&h->diag_part, ndiag * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&h->dtred, 8 * sizeof(unsigned long long)) == cudaSuccess &&
@@ -169,14 +180,34 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     return MHD_ERR_CUDA;
   }
   h->own_stream = true;
+  if (p->precision == MHD_PREC_FP32) {
+    const size_t nf = 12;
+    size_t fbytes = nf * (size_t)g.ncell * sizeof(float);
+    if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess) {
+      cudaGetLastError();
+      mhd_destroy(h);
+      return MHD_ERR_CUDA;
+    }
+    float *fq = h->fblock;
+    h->temp32 = fq; fq += g.ncell;
+    for (int c = 0; c < 3; c++) { h->vf32[c] = fq; fq += g.ncell; }
+    for (int c = 0; c < 3; c++) { h->bf32[c] = fq; fq += g.ncell; }
+    h->rn32 = fq; fq += g.ncell;
+    h->sw32 = fq; fq += g.ncell;
+    for (int c = 0; c < 3; c++) { h->emf32[c] = fq; fq += g.ncell; }
+    cudaMemsetAsync(h->fblock, 0, fbytes, h->stream);
+  }
   cudaMemsetAsync(h->block, 0, bytes, h->stream);
   cudaMemsetAsync(h->err, 0, sizeof(int), h->stream);
   cudaMemsetAsync(h->dtred, 0, 8 * sizeof(unsigned long long), h->stream);
   double *c = h->coords;
+  float *cf = h->coordsf;
   for (int d = 0; d < 3; d++) {
     g.x[d] = c; c += g.s[d];
     g.dx[d] = c; c += g.s[d];
     g.rdx[d] = c; c += g.s[d];
+    g.rdxc[d] = c; c += g.s[d];
+    g.dxf[d] = cf; cf += g.s[d];
   }
   *out = h;
   return MHD_OK;
@@ -188,6 +219,8 @@ int mhd_destroy(mhd_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaFree(h->block);
   cudaFree(h->coords);
+  cudaFree(h->coordsf);
+  cudaFree(h->fblock);
   cudaFree(h->divv);
   cudaFree(h->diag_part);
   cudaFree(h->dtred);
@@ -225,6 +258,8 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
     CKR(cudaMemcpyAsync(h->f.sp[s], species + (size_t)s * g.ncell, nb, cudaMemcpyHostToDevice, h->stream));
   const double *src[6] = {x, dx, y, dy, z, dz};
   h->rdx_host.resize((size_t)(g.s[0] + g.s[1] + g.s[2]));
+  h->rdxc_host.resize(h->rdx_host.size());
+  h->dxf_host.resize(h->rdx_host.size());
   size_t off = 0;
   for (int d = 0; d < 3; d++) {
     CKR(cudaMemcpyAsync((void *)g.x[d], src[2 * d], g.s[d] * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -235,6 +270,15 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
     r[0] = 1.0 / src[2 * d + 1][0];
     for (int i = 1; i < g.s[d]; i++) r[i] = 1.0 / (xx[i] - xx[i - 1]);
     CKR(cudaMemcpyAsync((void *)g.rdx[d], r, g.s[d] * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    // chosen form: 1/dx(i) and dx(i) in FP32
+    double *rc = h->rdxc_host.data() + off;
+    float *wf = h->dxf_host.data() + off;
+    for (int i = 0; i < g.s[d]; i++) {
+      rc[i] = 1.0 / src[2 * d + 1][i];
+      wf[i] = (float)src[2 * d + 1][i];
+    }
+    CKR(cudaMemcpyAsync((void *)g.rdxc[d], rc, g.s[d] * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CKR(cudaMemcpyAsync((void *)g.dxf[d], wf, g.s[d] * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     off += g.s[d];
   }
   // CC(4) as INITIA:470
@@ -267,7 +311,8 @@ int mhd_timestep(mhd_handle *h, double *dt, int *st) {
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
   CKR(cudaMemsetAsync(h->dtred, 0xff, 2 * sizeof(unsigned long long), h->stream));
-  CK(dt_reduce(h->g, h->ph, h->f, h->dtred, h->err, h->stream));
+  if (h->p.precision == MHD_PREC_FP32) CK(dt_reduce_fp32(h->g, h->ph, h->f, h->dtred, h->err, h->stream));
+  else CK(dt_reduce(h->g, h->ph, h->f, h->dtred, h->err, h->stream));
   CKR(cudaMemcpyAsync(h->h_small, h->dtred, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
   TRY(check_err(h));
   double tcfl, tlmt;
@@ -307,10 +352,13 @@ int mhd_source(mhd_handle *h, double dt) {
     a.imc_count = h->dtred + 2; a.sur_count = h->dtred + 3; a.fb_count = h->dtred + 4;
     a.W = (h->p.cooling == MHD_COOL_SURROGATE) ? h->sur_net : nullptr;
     a.tol = h->sur_tol;
+    a.T = h->temp32;
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
+    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
     CK(source_fp32(a, h->stream));
     TRY(fill(h, {h->pnew}, 7, 1));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
+    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
     CK(source_fp32(a, h->stream));
     return MHD_OK;
   }
@@ -345,23 +393,32 @@ int mhd_ct(mhd_handle *h, double dt) {
   TRY(fill(h, {f.U[1], f.U[6], f.U[7]}, 1, 2));
   TRY(fill(h, {f.U[2], f.U[5], f.U[7]}, 2, 2));
   TRY(fill(h, {f.U[3], f.U[5], f.U[6]}, 4, 2));
-  CK(face_velocity(h->g, f, h->vf[0], h->vf[1], h->vf[2], h->stream));
+  const bool fp32 = h->p.precision == MHD_PREC_FP32;
+  if (fp32) CK(face_velocity_fp32(h->g, f, h->vf[0], h->vf[1], h->vf[2], h->stream));
+  else CK(face_velocity(h->g, f, h->vf[0], h->vf[1], h->vf[2], h->stream));
   TRY(fill(h, {h->vf[1], h->vf[2]}, 1, 2));
   TRY(fill(h, {h->vf[0], h->vf[2]}, 2, 2));
   TRY(fill(h, {h->vf[0], h->vf[1]}, 4, 2));
   TRY(fill(h, {f.U[4]}, 7, 2));
   // CC(2) for Ez :2142
   TRY(fill(h, {f.U[0]}, 7, 2));
-  CTArgs a{};
-  a.g = h->g; a.ph = h->ph; a.f = f; a.dt = dt;
-  for (int c = 0; c < 3; c++) { a.vf[c] = h->vf[c]; a.emf[c] = h->emf[c]; }
-  for (int e = 0; e < 3; e++) {
-    if (h->p.precision == MHD_PREC_FP32) CK(emf_fp32(e, a, h->stream));
-    else CK(emf_fp64(e, a, h->stream));
+  if (fp32) {
+    CT32Args a{};
+    a.g = h->g;
+    for (int c = 0; c < 3; c++) { a.vf[c] = h->vf32[c]; a.bf[c] = h->bf32[c]; a.emf[c] = h->emf32[c]; }
+    a.rn = h->rn32; a.sw = h->sw32;
+    a.dt = (float)dt; a.facm = (float)(h->ph.facdep * 0.5);
+    CK(ct_prep_fp32(h->g, f, h->vf, h->ph.kb, a, h->stream));
+    for (int e = 0; e < 3; e++) CK(emf32(e, a, h->stream));
+    CK(face_b_fp32(h->g, f, h->emf32, dt, h->stream));
+  } else {
+    CTArgs a{};
+    a.g = h->g; a.ph = h->ph; a.f = f; a.dt = dt;
+    for (int c = 0; c < 3; c++) { a.vf[c] = h->vf[c]; a.emf[c] = h->emf[c]; }
+    for (int e = 0; e < 3; e++) CK(emf_fp64(e, a, h->stream));
+    CK(face_b(h->g, f, h->emf[0], h->emf[1], h->emf[2], dt, h->stream));   // CC(3)
   }
-  // CC(3), CC(4)
-  CK(face_b(h->g, f, h->emf[0], h->emf[1], h->emf[2], dt, h->stream));
-  CK(cell_b(h->g, f, h->stream));
+  CK(cell_b(h->g, f, h->stream));   // CC(4)
   TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2));
   return MHD_OK;
 }

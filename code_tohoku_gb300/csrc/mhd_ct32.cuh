@@ -1,0 +1,195 @@
+// mhd_ct32.cuh — chosen-form constrained transport: CC(1)-CC(3) of
+// MCF3DSGincfca3.f90:2115-2445 with the face velocities, the characteristic
+// EMF solve (CCT) and every limiter in FP32, and the face-field update in
+// FP64.
+//
+//   face_velocity32   CC(1) face velocities, FP32 arithmetic, FP64 store
+//                     (the ghost exchanges of the FP64 path follow it)
+//   ct_prep32         one pass over the padded grid after those exchanges:
+//                     FP32 copies of the face velocities, face B, rho and
+//                     VLIMIT's T switch, so the EMF kernels load only FP32
+//   emf32<E>          CC(2) + CCT for the edges along E, thread per edge,
+//                     FP32 loads, FP32 arithmetic, FP32 EMF
+//   face_b32          CC(3): B_face += dt/dy (E(j+1)-E(j)) - ..., the EMF
+//                     differences taken in FP64 from the FP32 values, so the
+//                     discrete div B of the update cancels to FP64 round-off
+//                     exactly as in the FP64 path
+//
+// Conversions use the integer routines of mhd_conv.cuh (GB300 runs the
+// hardware ones on its narrow FP64 pipe).
+#pragma once
+
+#include "mhd_conv.cuh"
+#include "mhd_kernels.cuh"
+
+namespace mhd {
+
+struct CT32Args {
+  Grid g;
+  const float *vf[3];   // face velocities
+  const float *bf[3];   // face B
+  const float *rn;      // rho
+  const float *sw;      // VLIMIT T switch (+-0.5) per cell
+  float *emf[3];        // [0] Ez, [1] Ex, [2] Ey
+  float dt, facm;       // facm = facdep / 2
+};
+
+#ifdef MHD_FP32_KERNELS
+__global__ void __launch_bounds__(256) face_velocity32_kernel(Grid g, Fields f, double *vf0, double *vf1,
+                                                              double *vf2) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
+  if (t >= (long long)nx1 * ny1 * nz1) return;
+  int i = 1 + (int)(t % nx1);
+  int j = 1 + (int)((t / nx1) % ny1);
+  int k = 1 + (int)(t / ((long long)nx1 * ny1));
+  long long a = gidx(g, i, j, k);
+  const float *dx = g.dxf[0], *dy = g.dxf[1], *dz = g.dxf[2];
+  if (j <= g.n[1] && k <= g.n[2])
+    vf0[a] = f2d(__fdividef(dx[i] * d2f(f.U[1][a]) + dx[i + 1] * d2f(f.U[1][a - 1]), dx[i] + dx[i + 1]));
+  if (i <= g.n[0] && k <= g.n[2])
+    vf1[a] = f2d(__fdividef(dy[j] * d2f(f.U[2][a]) + dy[j + 1] * d2f(f.U[2][a - g.st[1]]), dy[j] + dy[j + 1]));
+  if (i <= g.n[0] && j <= g.n[1])
+    vf2[a] = f2d(__fdividef(dz[k] * d2f(f.U[3][a]) + dz[k + 1] * d2f(f.U[3][a - g.st[2]]), dz[k] + dz[k + 1]));
+}
+
+__global__ void __launch_bounds__(256) ct_prep32_kernel(long long ncell, Fields f, const double *vf0,
+                                                        const double *vf1, const double *vf2, float kb,
+                                                        CT32Args A) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncell) return;
+  const_cast<float *>(A.vf[0])[t] = d2f(vf0[t]);
+  const_cast<float *>(A.vf[1])[t] = d2f(vf1[t]);
+  const_cast<float *>(A.vf[2])[t] = d2f(vf2[t]);
+  for (int c = 0; c < 3; c++) const_cast<float *>(A.bf[c])[t] = d2f(f.U[5 + c][t]);
+  float r = d2f(f.U[0][t]);
+  const_cast<float *>(A.rn)[t] = r;
+  // T = 1.27 p/(kb rho); sign(0.5, T-3)
+  const_cast<float *>(A.sw)[t] = (1.27f * d2f(f.U[4][t]) >= 3.0f * kb * r) ? 0.5f : -0.5f;
+}
+
+// CC(2) + CCT for the edge direction E (0: Ez on x/y, 1: Ex on y/z,
+// 2: Ey on z/x): the arithmetic of emf_kernel (:2140-2157, :2186-2445) in
+// FP32 on FP32 inputs.
+template <int E>
+__global__ void __launch_bounds__(128) emf32_kernel(CT32Args A) {
+  const Grid &g = A.g;
+  constexpr int da = E, db = (E + 1) % 3, dc = (E + 2) % 3;
+  int Na = g.n[da], Nb = g.n[db], Nc = g.n[dc];
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long na1 = Na + 1, nb1 = Nb + 1;
+  if (t >= na1 * nb1 * Nc) return;
+  int aa = 1 + (int)(t % na1);
+  int bb = 1 + (int)((t / na1) % nb1);
+  int cc = 1 + (int)(t / (na1 * nb1));
+  int c3[3];
+  c3[da] = aa; c3[db] = bb; c3[dc] = cc;
+  long long p0 = gidx(g, c3[0], c3[1], c3[2]);
+  const long long sa = g.st[da], sb = g.st[db];
+  const float *rn = A.rn, *sw = A.sw;
+  const float dncv = 0.25f * (rn[p0] + rn[p0 - sa] + rn[p0 - sb] + rn[p0 - sa - sb]);
+  const float *Vx = A.vf[da], *Vy = A.vf[db];
+  const float *Bxf = A.bf[da], *Byf = A.bf[db];
+  const float dsqinv = rsqrtf(dncv);
+  const float facm = A.facm, dt = A.dt;
+  const float *dxe = g.dxf[da], *dye = g.dxf[db];
+  const float dxm = dxe[aa], dx0 = dxe[aa + 1], dym = dye[bb], dy0 = dye[bb + 1];
+  // VLIMIT of a face array along direction d at cell c (T switch of cell c)
+  auto slope = [&](const float *q, long long c, long long sd, const float *dxx, int pos) {
+    return vlim_sel(q[c - sd], q[c], q[c + sd], dxx[pos], dxx[pos + 1], dxx[pos + 2], sw[c]);
+  };
+  auto load1 = [&](long long p, int bpos, float &a1p, float &a1m, float &da1p, float &da1m) {
+    float v = Vx[p], b = Bxf[p];
+    float q1 = slope(Vx, p, sb, dye, bpos);
+    float q3 = slope(Bxf, p, sb, dye, bpos);
+    a1p = v + b * dsqinv;
+    da1p = (q1 + q3 * dsqinv) * facm;
+    a1m = v - b * dsqinv;
+    da1m = (q1 - q3 * dsqinv) * facm;
+  };
+  auto load2 = [&](long long p, int apos, float &a2m, float &a2p, float &da2m, float &da2p) {
+    float v = Vy[p], b = Byf[p];
+    float q2 = slope(Vy, p, sa, dxe, apos);
+    float q4 = slope(Byf, p, sa, dxe, apos);
+    a2m = v - b * dsqinv;
+    da2m = (q2 - q4 * dsqinv) * facm;
+    a2p = v + b * dsqinv;
+    da2p = (q2 + q4 * dsqinv) * facm;
+  };
+  float a1pL, a1mL, da1pL, da1mL, a1pR, a1mR, da1pR, da1mR;
+  float a2mL, a2pL, da2mL, da2pL, a2mR, a2pR, da2mR, da2pR;
+  load1(p0 - sb, bb - 1, a1pL, a1mL, da1pL, da1mL);   // (a, b-1)
+  load1(p0, bb, a1pR, a1mR, da1pR, da1mR);            // (a, b)
+  load2(p0 - sa, aa - 1, a2mL, a2pL, da2mL, da2pL);   // (a-1, b)
+  load2(p0, aa, a2mR, a2pR, da2mR, da2pR);            // (a, b)
+
+  auto cand = [&](float a1p, float da1p, float a1m, float da1m, float a2m, float da2m, float a2p, float da2p,
+                  float dyv, float dxv, float S1, float S2, float &C1p, float &C2m, float &C1m, float &C2p) {
+    float r1 = __fdividef(1.0f, 1.0f - da1p * da2m * dt * dt);
+    float r2 = __fdividef(1.0f, 1.0f - da1m * da2p * dt * dt);
+    C1p = (a1p + da1p * dyv * S1 - da1p * (a2m + da2m * dxv * S2) * dt) * r1;
+    C2m = (a2m + da2m * dxv * S2 - da2m * (a1p + da1p * dyv * S1) * dt) * r1;
+    C1m = (a1m + da1m * dyv * S1 - da1m * (a2p + da2p * dxv * S2) * dt) * r2;
+    C2p = (a2p + da2p * dxv * S2 - da2p * (a1m + da1m * dyv * S1) * dt) * r2;
+  };
+  float C1pLL, C2mLL, C1mLL, C2pLL, C1pRL, C2mRL, C1mRL, C2pRL;
+  float C1pLR, C2mLR, C1mLR, C2pLR, C1pRR, C2mRR, C1mRR, C2pRR;
+  cand(a1pL, da1pL, a1mL, da1mL, a2mL, da2mL, a2pL, da2pL, dym, dxm, 1.0f, 1.0f, C1pLL, C2mLL, C1mLL, C2pLL);
+  cand(a1pR, da1pR, a1mR, da1mR, a2mL, da2mL, a2pL, da2pL, dy0, dxm, -1.0f, 1.0f, C1pRL, C2mRL, C1mRL, C2pRL);
+  cand(a1pL, da1pL, a1mL, da1mL, a2mR, da2mR, a2pR, da2pR, dym, dx0, 1.0f, -1.0f, C1pLR, C2mLR, C1mLR, C2pLR);
+  cand(a1pR, da1pR, a1mR, da1mR, a2mR, da2mR, a2pR, da2pR, dy0, dx0, -1.0f, -1.0f, C1pRR, C2mRR, C1mRR, C2pRR);
+
+  const bool w11 = C1pLL > 0.0f && C2mLL > 0.0f, w12 = C1mLL > 0.0f && C2pLL > 0.0f;
+  const bool w21 = C1pRL > 0.0f && C2mRL < 0.0f, w22 = C1mRL > 0.0f && C2pRL < 0.0f;
+  const bool w31 = C1pLR < 0.0f && C2mLR > 0.0f, w32 = C1mLR < 0.0f && C2pLR > 0.0f;
+  const bool w41 = C1pRR < 0.0f && C2mRR < 0.0f, w42 = C1mRR < 0.0f && C2pRR < 0.0f;
+  // weight w + (1e13-1) * int(0.51 w1 + 0.51 w2): the boost is w1 AND w2
+  const float big = 1.e13f - 1.0f;
+  auto W = [&](bool w, bool x1, bool x2) { return (w ? 1.0f : 0.0f) + ((x1 && x2) ? big : 0.0f); };
+  float W11 = W(w11, w11, w12), W12 = W(w12, w11, w12);
+  float W21 = W(w21, w21, w22), W22 = W(w22, w21, w22);
+  float W31 = W(w31, w31, w32), W32 = W(w32, w31, w32);
+  float W41 = W(w41, w41, w42), W42 = W(w42, w41, w42);
+  float C1p = 0.0f, C2m = 0.0f, C1m = 0.0f, C2p = 0.0f;
+  if (w11 || w21 || w31 || w41) {
+    C1p = __fdividef(W11 * fabsf(C2mLL) * C1pLL + W21 * fabsf(C2mRL) * C1pRL + W31 * fabsf(C2mLR) * C1pLR +
+                         W41 * fabsf(C2mRR) * C1pRR,
+                     W11 * fabsf(C2mLL) + W21 * fabsf(C2mRL) + W31 * fabsf(C2mLR) + W41 * fabsf(C2mRR));
+    C2m = __fdividef(W11 * fabsf(C1pLL) * C2mLL + W21 * fabsf(C1pRL) * C2mRL + W31 * fabsf(C1pLR) * C2mLR +
+                         W41 * fabsf(C1pRR) * C2mRR,
+                     W11 * fabsf(C1pLL) + W21 * fabsf(C1pRL) + W31 * fabsf(C1pLR) + W41 * fabsf(C1pRR));
+  }
+  if (w12 || w22 || w32 || w42) {
+    C1m = __fdividef(W12 * fabsf(C2pLL) * C1mLL + W22 * fabsf(C2pRL) * C1mRL + W32 * fabsf(C2pLR) * C1mLR +
+                         W42 * fabsf(C2pRR) * C1mRR,
+                     W12 * fabsf(C2pLL) + W22 * fabsf(C2pRL) + W32 * fabsf(C2pLR) + W42 * fabsf(C2pRR));
+    C2p = __fdividef(W12 * fabsf(C1mLL) * C2pLL + W22 * fabsf(C1mRL) * C2pRL + W32 * fabsf(C1mLR) * C2pLR +
+                         W42 * fabsf(C1mRR) * C2pRR,
+                     W12 * fabsf(C1mLL) + W22 * fabsf(C1mRL) + W32 * fabsf(C1mLR) + W42 * fabsf(C1mRR));
+  }
+  float v1a = C1p + C1m, v2a = C2p + C2m, B1a = C1p - C1m, B2a = C2p - C2m;
+  A.emf[E][p0] = 0.25f * (v1a * B2a - v2a * B1a) * (dncv * dsqinv);
+}
+
+// CC(3): face B from the EMF curl (:2159-2169); emf[0]=Ez, [1]=Ex, [2]=Ey
+__global__ void __launch_bounds__(256) face_b32_kernel(Grid g, Fields f, const float *Ez, const float *Ex,
+                                                       const float *Ey, double dt) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
+  if (t >= (long long)nx1 * ny1 * nz1) return;
+  int i = 1 + (int)(t % nx1);
+  int j = 1 + (int)((t / nx1) % ny1);
+  int k = 1 + (int)(t / ((long long)nx1 * ny1));
+  long long a = gidx(g, i, j, k);
+  long long sx = 1, sy = g.st[1], sz = g.st[2];
+  const double cx = dt * g.rdxc[0][i + 1], cy = dt * g.rdxc[1][j + 1], cz = dt * g.rdxc[2][k + 1];
+  if (j <= g.n[1] && k <= g.n[2])
+    f.U[5][a] = f.U[5][a] + cy * (f2d(Ez[a + sy]) - f2d(Ez[a])) - cz * (f2d(Ey[a + sz]) - f2d(Ey[a]));
+  if (i <= g.n[0] && k <= g.n[2])
+    f.U[6][a] = f.U[6][a] + cz * (f2d(Ex[a + sz]) - f2d(Ex[a])) - cx * (f2d(Ez[a + sx]) - f2d(Ez[a]));
+  if (i <= g.n[0] && j <= g.n[1])
+    f.U[7][a] = f.U[7][a] + cx * (f2d(Ey[a + sx]) - f2d(Ey[a])) - cy * (f2d(Ex[a + sy]) - f2d(Ex[a]));
+}
+#endif  // MHD_FP32_KERNELS
+
+}  // namespace mhd

@@ -3,31 +3,41 @@
 // the default contraction (FMA) enabled.
 #define MHD_FP32_KERNELS
 #include "mhd_sweep32.cuh"
+#include "mhd_ct32.cuh"
 #include "mhd_source32.cuh"
 #include "mhd_sweep_impl.cuh"
 
 namespace mhd {
+// Sweep launch shape: 288 threads (9 warps) and two CTAs per SM.  Every
+// phase of the kernel loops over n, n+1 or n+2 positions of P pencils;
+// with 288 threads all three counts take the same number of trips for the
+// pencil lengths used here, so no phase runs a nearly empty last trip.
+// P pencils per CTA are chosen so that two CTAs fit in the SM's shared memory.
+constexpr int kSweepThreads = 288;
+constexpr int kSweepMinBlocks = 2;
+constexpr size_t kSweepSmemPerCta = 113 * 1024;
+
 template <int DIR, int P>
 static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
   const Grid &g = a.g;
   size_t smem = sweep32_smem_bytes(g.n[DIR], P);
-  auto k = sweep32_kernel<DIR, P, 512>;
+  auto k = sweep32_kernel<DIR, P, kSweepThreads, kSweepMinBlocks>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   dim3 grid;
   if (DIR == 0) grid = dim3(g.n[1] / P, g.n[2]);
   else if (DIR == 1) grid = dim3(g.n[0] / P, g.n[2]);
   else grid = dim3(g.n[0] / P, g.n[1]);
-  k<<<grid, 512, smem, s>>>(a);
+  k<<<grid, kSweepThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int DIR>
 static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
   int nb = (DIR == 0) ? a.g.n[1] : a.g.n[0];
-  size_t lim = 227 * 1024;
-  if (nb % 4 == 0 && sweep32_smem_bytes(a.g.n[DIR], 4) <= lim) return launch32<DIR, 4>(a, s);
-  if (nb % 2 == 0 && sweep32_smem_bytes(a.g.n[DIR], 2) <= lim) return launch32<DIR, 2>(a, s);
+  if (nb % 4 == 0 && sweep32_smem_bytes(a.g.n[DIR], 4) <= kSweepSmemPerCta) return launch32<DIR, 4>(a, s);
+  if (nb % 2 == 0 && sweep32_smem_bytes(a.g.n[DIR], 2) <= kSweepSmemPerCta) return launch32<DIR, 2>(a, s);
+  if (sweep32_smem_bytes(a.g.n[DIR], 1) > 227 * 1024) return cudaErrorInvalidValue;
   return launch32<DIR, 1>(a, s);
 }
 
@@ -36,7 +46,53 @@ cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s) {
   if (dir == 1) return launch32_d<1>(a, s);
   return launch32_d<2>(a, s);
 }
-cudaError_t emf_fp32(int e, const CTArgs &a, cudaStream_t s) { return launch_emf<float>(e, a, s); }
+cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
+                           cudaStream_t s) {
+  long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+  dt32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, out, err);
+  return cudaGetLastError();
+}
+
+static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, cudaStream_t s) {
+  temp32_kernel<<<blocks_for(g.ncell, 256), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T);
+  return cudaGetLastError();
+}
+
+cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s) {
+  long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
+  face_velocity32_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, f, v0, v1, v2);
+  return cudaGetLastError();
+}
+
+cudaError_t ct_prep_fp32(const Grid &g, const Fields &f, double *const vf[3], double kb, const CT32Args &a,
+                         cudaStream_t s) {
+  ct_prep32_kernel<<<blocks_for(g.ncell, 256), 256, 0, s>>>(g.ncell, f, vf[0], vf[1], vf[2], d2f(kb), a);
+  return cudaGetLastError();
+}
+
+template <int E>
+static cudaError_t emf32_e(const CT32Args &a, cudaStream_t s) {
+  const Grid &g = a.g;
+  constexpr int da = E, db = (E + 1) % 3, dc = (E + 2) % 3;
+  long long n = (long long)(g.n[da] + 1) * (g.n[db] + 1) * g.n[dc];
+  emf32_kernel<E><<<blocks_for(n, 128), 128, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t emf32(int e, const CT32Args &a, cudaStream_t s) {
+  if (e == 0) return emf32_e<0>(a, s);
+  if (e == 1) return emf32_e<1>(a, s);
+  return emf32_e<2>(a, s);
+}
+
+cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], double dt, cudaStream_t s) {
+  long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
+  face_b32_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, f, emf[0], emf[1], emf[2], dt);
+  return cudaGetLastError();
+}
+
 cudaError_t source_fp32(const Source32Args &a, cudaStream_t s) {
   long long n = (long long)a.g.n[0] * a.g.n[1] * a.g.n[2];
   source32_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);

@@ -37,6 +37,8 @@ struct Grid {
   const double *x[3];       // coordinates x(-1..n+2) per direction
   const double *dx[3];      // spacings dx(-1..n+2)
   const double *rdx[3];     // 1/(x(i)-x(i-1)), i = -1..n+2 (chosen form)
+  const double *rdxc[3];    // 1/dx(i) (chosen form)
+  const float *dxf[3];      // dx(i) in FP32 (chosen form)
 };
 
 struct Phys {

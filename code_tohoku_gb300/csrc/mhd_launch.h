@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "mhd_kernels.cuh"
+#include "mhd_ct32.cuh"
 #include "mhd_source32.cuh"
 
 namespace mhd {
@@ -16,10 +17,17 @@ size_t sweep_smem_bytes(const Grid &g, int dir, int P);
 // plain form (every operation FP64, no contraction)
 cudaError_t sweep_fp64(int dir, const SweepArgs &a, cudaStream_t s);
 cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s);
-// chosen form (FP32 reconstruction / Riemann / characteristics)
+// chosen form (FP32 reconstruction / Riemann / characteristics / EMF)
 cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s);
-cudaError_t emf_fp32(int e, const CTArgs &a, cudaStream_t s);
 cudaError_t source_fp32(const Source32Args &a, cudaStream_t s);
+cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, cudaStream_t s);
+cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
+                           cudaStream_t s);
+cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
+cudaError_t ct_prep_fp32(const Grid &g, const Fields &f, double *const vf[3], double kb, const CT32Args &a,
+                         cudaStream_t s);
+cudaError_t emf32(int e, const CT32Args &a, cudaStream_t s);
+cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], double dt, cudaStream_t s);
 // pack FP32 master surrogate parameters into the BF16 device network
 cudaError_t surrogate_pack(const float *master, SurNet *net, cudaStream_t s);
 

@@ -10,6 +10,7 @@
 // tolerance.
 #pragma once
 
+#include "mhd_conv.cuh"
 #include "mhd_kernels.cuh"
 #include "mhd_surrogate_net.cuh"
 
@@ -51,6 +52,7 @@ struct Source32Args {
   const double *pin;
   const double *pold;
   double *pout;
+  const float *T;                  // FP32 temperature of every cell (temp32_kernel)
   double dt;
   int pass;
   int *err;
@@ -66,7 +68,19 @@ struct Source32Args {
 namespace mhd {
 
 #ifdef MHD_FP32_KERNELS
-// One pass of the chosen-form SOURCE for one cell (thread per cell).
+// T = p / (kb (H + p + H2 + He + He+)) of every padded cell in FP32: the
+// conduction stencil of SOURCE reads the temperatures of six neighbours,
+// so they are formed once per pass instead of once per neighbour.
+__global__ void __launch_bounds__(256) temp32_kernel(long long ncell, Fields f, const double *pin, float kb,
+                                                     float *T) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncell) return;
+  float n = d2f(f.sp[1][t]) + d2f(f.sp[0][t]) + d2f(f.sp[2][t]) + d2f(f.sp[3][t]) + d2f(f.sp[4][t]);
+  T[t] = __fdividef(d2f(pin[t]), kb * n);
+}
+
+// One pass of the chosen-form SOURCE for one cell (thread per cell).  The
+// only FP64 operation is p_new = base + dp; conversions are integer ones.
 __global__ void __launch_bounds__(128) source32_kernel(Source32Args A) {
   const Grid &g = A.g;
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -77,45 +91,46 @@ __global__ void __launch_bounds__(128) source32_kernel(Source32Args A) {
   int j = 1 + (int)((tt / nx) % ny);
   int k = 1 + (int)(tt / ((long long)nx * ny));
   long long a = gidx(g, i, j, k);
-  const float kb = (float)A.ph.kb, Kc = (float)A.ph.kcond;
-  const float dt = (float)A.dt;
-  const double *pin = A.pin;
+  const float kb = d2f(A.ph.kb), Kc = d2f(A.ph.kcond);
+  const float dt = d2f(A.dt);
   const Fields &f = A.f;
-  auto ntot = [&](long long c) { return (float)(f.sp[1][c] + f.sp[0][c] + f.sp[2][c] + f.sp[3][c] + f.sp[4][c]); };
-  auto Tn = [&](long long c) { return (float)pin[c] / (kb * ntot(c)); };
-  const double *dx = g.dx[0], *dy = g.dx[1], *dz = g.dx[2];
+  const float *T = A.T;
+  const float *dx = g.dxf[0], *dy = g.dxf[1], *dz = g.dxf[2];
   long long sy = g.st[1], sz = g.st[2];
-  float T0 = Tn(a);
+  float T0 = T[a];
   auto flux = [&](float Tl, float Tu, float dl, float du) {
-    float rt = sqrtf((dl * Tu + du * Tl) / (dl + du));
-    return Kc * fminf(rt, 3.873f) * (Tu - Tl) * 2.0f / (dl + du);
+    float rdu = __fdividef(1.0f, dl + du);
+    float rt = sqrtf((dl * Tu + du * Tl) * rdu);
+    return Kc * fminf(rt, 3.873f) * (Tu - Tl) * 2.0f * rdu;
   };
-  float dxm = (float)dx[i], dx0 = (float)dx[i + 1], dxp = (float)dx[i + 2];
-  float dym = (float)dy[j], dy0 = (float)dy[j + 1], dyp = (float)dy[j + 2];
-  float dzm = (float)dz[k], dz0 = (float)dz[k + 1], dzp = (float)dz[k + 2];
-  float div = (flux(T0, Tn(a + 1), dx0, dxp) - flux(Tn(a - 1), T0, dxm, dx0)) / dx0 +
-              (flux(T0, Tn(a + sy), dy0, dyp) - flux(Tn(a - sy), T0, dym, dy0)) / dy0 +
-              (flux(T0, Tn(a + sz), dz0, dzp) - flux(Tn(a - sz), T0, dzm, dz0)) / dz0;
-  float H = (float)f.sp[0][a], pr = (float)f.sp[1][a], H2 = (float)f.sp[2][a], He = (float)f.sp[3][a],
-        Hep = (float)f.sp[4][a];
-  float g1 = (2.0f * (H + pr + He + Hep) + 2.0f * H2) / (3.0f * (H + pr + He + Hep) + 5.0f * H2);
-  float NN = (float)f.U[0][a] / 1.27f;
+  float dxm = dx[i], dx0 = dx[i + 1], dxp = dx[i + 2];
+  float dym = dy[j], dy0 = dy[j + 1], dyp = dy[j + 2];
+  float dzm = dz[k], dz0 = dz[k + 1], dzp = dz[k + 2];
+  float div = __fdividef(flux(T0, T[a + 1], dx0, dxp) - flux(T[a - 1], T0, dxm, dx0), dx0) +
+              __fdividef(flux(T0, T[a + sy], dy0, dyp) - flux(T[a - sy], T0, dym, dy0), dy0) +
+              __fdividef(flux(T0, T[a + sz], dz0, dzp) - flux(T[a - sz], T0, dzm, dz0), dz0);
+  float H = d2f(f.sp[0][a]), pr = d2f(f.sp[1][a]), H2 = d2f(f.sp[2][a]), He = d2f(f.sp[3][a]),
+        Hep = d2f(f.sp[4][a]);
+  float g1 = __fdividef(2.0f * (H + pr + He + Hep) + 2.0f * H2, 3.0f * (H + pr + He + Hep) + 5.0f * H2);
+  float NN = d2f(f.U[0][a]) * (1.0f / 1.27f);
   float CooL = fcool_ki(T0, NN);
   double Pn = A.pold[a];
+  float Pnf = d2f(Pn);
   float h = (A.pass == 0) ? 0.5f : 1.0f;          // predictor: half of dt
   float dts = dt * h;
-  double base = (A.pass == 0) ? pin[a] : Pn;       // p the cooling acts on
-  bool stiff = valid && !((float)dt <= 0.2f * (float)Pn / (g1 * fabsf(CooL)));
-  double dp_cool = 0.0;
+  double base = (A.pass == 0) ? A.pin[a] : Pn;     // p the cooling acts on
+  float basef = (A.pass == 0) ? d2f(base) : Pnf;
+  bool stiff = valid && !(dt <= 0.2f * Pnf / (g1 * fabsf(CooL)));
+  float dp_cool = 0.0f;
   bool need_imc = stiff;
   float nimc = H + pr + He + Hep + H2;
-  float nkbi = 1.0f / (kb * nimc);
-  float Tb = (float)base * nkbi;                  // temperature the implicit solve starts from
+  float nkbi = __fdividef(1.0f, kb * nimc);
+  float Tb = basef * nkbi;                         // temperature the implicit solve starts from
   if (A.W) {
     // surrogate: inputs log10 N, log10 T, log10(dts / t_cool) with
     // t_cool = P/((gamma-1)|Lambda|) at the starting state
     float Lb = fcool_ki(Tb, NN);
-    float r = dts * g1 * fabsf(Lb) / (float)base;
+    float r = dts * g1 * fabsf(Lb) / basef;
     float x0 = log10f(NN), x1 = log10f(Tb), x2 = log10f(fmaxf(r, 1e-30f));
     bool inbox = stiff && x0 >= -2.0f && x0 <= 5.0f && x1 >= -2.0f && x1 <= 1.30103f && x2 >= -3.0f && x2 <= 3.0f;
     float conf;
@@ -128,14 +143,14 @@ __global__ void __launch_bounds__(128) source32_kernel(Source32Args A) {
       for (int it = 0; it < 2; it++) {
         float L, dL;
         fcool_ki_d(P * nkbi, NN, L, dL);
-        float fv = P + c * L - (float)base;
+        float fv = P + c * L - basef;
         float fp = 1.0f + c * dL * nkbi;
         if (fp > 0.0f) P = fmaxf(P - fv / fp, 0.1f * P);
       }
       // implicit residual |P + Lambda(P) dt (gamma-1) - P_old| / P_old
-      float res = fabsf(P + fcool_ki(P * nkbi, NN) * c - (float)base) / (float)base;
+      float res = fabsf(P + fcool_ki(P * nkbi, NN) * c - basef) / basef;
       if (res <= A.tol) {
-        dp_cool = (double)P - base;
+        dp_cool = P - basef;
         need_imc = false;
         atomicAdd(A.sur_count, 1ull);
       } else {
@@ -145,20 +160,80 @@ __global__ void __launch_bounds__(128) source32_kernel(Source32Args A) {
   }
   if (!valid) return;
   if (!stiff) {
-    dp_cool = -(double)(g1 * CooL * dts);
+    dp_cool = -(g1 * CooL * dts);
   } else if (need_imc) {
-    float Pm = imc32((float)base, nkbi, dts * g1, NN);
-    dp_cool = (double)Pm - base;
+    float Pm = imc32(basef, nkbi, dts * g1, NN);
+    dp_cool = Pm - basef;
     atomicAdd(A.imc_count, 1ull);
   }
   float tcd = g1 * Kc * sqrtf(T0);
-  tcd = 0.49f * nimc * kb / tcd * (dx0 * dx0);
+  tcd = __fdividef(0.49f * nimc * kb, tcd) * (dx0 * dx0);
   float w = (tcd - dt >= 0.0f) ? 1.0f : 0.0f;      // (sign(0.5, tcd-dt) + 0.5)
-  double pnew = base + dp_cool + (double)(w * g1 * dts * div);
-  pnew = fmx(pnew, A.ph.pmin);
-  pnew = fmn(pnew, A.ph.pmax);
+  float dp = dp_cool + w * g1 * dts * div;
+  double pnew = base + f2d(dp);
+  float pf = basef + dp;
+  // floors max(pnew, pmin), min(pnew, pmax); a NaN passes and is reported
+  if (pf < d2f(A.ph.pmin)) pnew = A.ph.pmin;
+  if (pf > d2f(A.ph.pmax)) pnew = A.ph.pmax;
   A.pout[a] = pnew;
-  if (!(pnew == pnew)) flag(A.err, ERRB_NONFINITE);
+  if (!(pf == pf)) flag(A.err, ERRB_NONFINITE);
+}
+
+// dt for the chosen form: the Courant limit (:1912-1930) and the thermal
+// limit of Stblty (:2784-2822) in FP32; the per-cell minima are widened to
+// FP64 bit patterns for the same order-independent atomicMin reduction.
+__global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, unsigned long long *out, int *err) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  float c_min = d2f(ph.tfinal), s_min = c_min;
+  if (t < (long long)nx * ny * nz) {
+    int i = 1 + (int)(t % nx);
+    int j = 1 + (int)((t / nx) % ny);
+    int k = 1 + (int)(t / ((long long)nx * ny));
+    long long a = gidx(g, i, j, k);
+    float H = d2f(f.sp[0][a]), pr = d2f(f.sp[1][a]), H2 = d2f(f.sp[2][a]), He = d2f(f.sp[3][a]),
+          Hep = d2f(f.sp[4][a]);
+    float S = H + pr + He + Hep;
+    float rg = __fdividef(1.0f, 3.0f * S + 5.0f * H2);
+    float gam = (5.0f * S + 7.0f * H2) * rg;
+    float bx = d2f(f.bcc[0][a]), by = d2f(f.bcc[1][a]), bz = d2f(f.bcc[2][a]);
+    float rho = d2f(f.U[0][a]), p5 = d2f(f.U[4][a]);
+    float cs = sqrtf(__fdividef(gam * p5 + bx * bx + by * by + bz * bz, rho));
+    float dxi = g.dxf[0][i + 1], dyj = g.dxf[1][j + 1], dzk = g.dxf[2][k + 1];
+    c_min = fminf(c_min, __fdividef(dxi, cs + fabsf(d2f(f.U[1][a]))));
+    c_min = fminf(c_min, __fdividef(dyj, cs + fabsf(d2f(f.U[2][a]))));
+    c_min = fminf(c_min, __fdividef(dzk, cs + fabsf(d2f(f.U[3][a]))));
+    if (ph.ifthrm == 2) {
+      float Nn = S + H2;
+      const float kb = d2f(ph.kb);
+      float Tn = __fdividef(p5, kb * Nn);
+      float dl = fminf(fminf(dxi, dyj), dzk);
+      float g1c = (2.0f * S + 2.0f * H2) * rg;
+      float alpha = __fdividef(0.4f * Nn * kb, g1c * d2f(ph.kcond) * sqrtf(fminf(Tn, 15.0f))) * (dl * dl);
+      float tauC = fmaxf(__fdividef(0.2f * p5, g1c * fabsf(fcool_ki(Tn, rho * (1.0f / 1.27f)))), 2.5e-4f);
+      s_min = fminf(s_min, fminf(tauC, alpha));
+    }
+    if (!(c_min > 0.0f) || !(s_min > 0.0f)) flag(err, ERRB_DT);
+  }
+  unsigned long long cb = (unsigned long long)__double_as_longlong(f2d(c_min > 0.0f ? c_min : 0.0f));
+  unsigned long long sb = (unsigned long long)__double_as_longlong(f2d(s_min > 0.0f ? s_min : 0.0f));
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long c2 = __shfl_xor_sync(0xffffffffu, cb, o), s2 = __shfl_xor_sync(0xffffffffu, sb, o);
+    cb = c2 < cb ? c2 : cb;
+    sb = s2 < sb ? s2 : sb;
+  }
+  __shared__ unsigned long long wc[8], ws[8];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { wc[w] = cb; ws[w] = sb; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+      cb = wc[q] < cb ? wc[q] : cb;
+      sb = ws[q] < sb ? ws[q] : sb;
+    }
+    atomicMin(&out[0], cb);
+    atomicMin(&out[1], sb);
+  }
 }
 
 #endif  // MHD_FP32_KERNELS

@@ -1,146 +1,184 @@
 // mhd_sweep32.cuh — the chosen-form sweep: the same Lagrange + MOC + remap
-// scheme as sweep_kernel (MCF3DSGincfca3.f90:1264-2098), rewritten so that
-// every quantity that is reconstructed, limited, solved for or divided runs
-// in FP32, and FP64 is used only where the conserved state accumulates:
+// scheme as sweep_kernel (MCF3DSGincfca3.f90:1264-2098) with every
+// reconstruction, limiter, Riemann and characteristic solve and division in
+// FP32, and FP64 used only where the resident FP64 state is updated:
 //
-//   mass       dm = rho dx                      (Lagrangian mass, exact)
-//   momentum   M  = v dm - dt dPa + dt dMag     (RHS + MOC in flux form)
-//   energy     E  = e dm - dt d(PaVa) + dt dW   (RHS + MOC in flux form)
-//   transverse Phi = Bt dx + dt d(Bn Va_t)       (Blg * dxlag)
-//   species    S  = n dx
-//   remap      Q_new = (Q + F_i - F_{i-1}) / dx (F upwind MUSCL, FP32)
+//   rho_new = rho + rdx * ((double)F_i - (double)F_{i-1})     FP64 flux difference
+//   v_new   = v   + (double)dv,  dv = (dM - drho v) / rho_new  (dM, drho in FP32)
+//   n_new   = n   + (double)dn                                 species
+//   p_new   = (double)p(E, rho_new, v_new, B)                  FP32 energy
 //
-// These are the reference's updates multiplied through by the Lagrangian
-// width: v_lag = v - dt/dm dPa becomes M = v dm - dt dPa, the MOC update
-// (rho v + dt/dxlag X) dxlag becomes M + dt X, and the remap numerator
-// U dxlag + F_i - F_{i-1} uses the accumulated Q directly, so mass, momentum
-// and energy stay conserved to FP64 round-off while the FP32 part carries
-// only reconstruction error.  The T switch of VLIMIT is kept with the same
-// meaning at every stage (U(:,5) is p, then e inside / p in the ghosts for
-// MOC, then E for the remap).
+// dM is the reference's Lagrangian pressure and MOC Lorentz increments plus
+// the remap flux difference, i.e. M_new dx = (rho v dx + dM dx): the update
+// of the momentum content multiplied through by the cell width, written as
+// an increment so its FP32 rounding scales with the change, not the state.
+// The mass update differences the FP32 fluxes in FP64, so the total mass of
+// a periodic grid is conserved to FP64 round-off.  The energy follows the
+// reference's own structure — E is rebuilt from the pressure every sweep
+// and turned back into a pressure at the end — and runs in FP32.
+//
+// On GB300 the FP64 pipe runs at ~1/64 of the FP32 rate and also executes
+// the hardware double<->float conversions, so this kernel converts with
+// integer instructions (mhd_conv.cuh) and keeps 13 FP64 operations per cell
+// (the additions above).  All pencil buffers are FP32: 22 of them, L*P floats
+// each (L = n+4), plus FP32 copies of the coordinate widths.  Ghost entries
+// of a buffer are written by the thread that computes their source cell
+// (periodic wrap or free copy), so the in-pencil halo exchanges cost no
+// extra barrier: the sweep has 11 barriers.
+//
+// VLIMIT's T switch keeps the reference's meaning at every stage: p for
+// RHS, e inside and p in the ghosts for MOC, E for the remap.
 #pragma once
 
+#include "mhd_conv.cuh"
 #include "mhd_kernels.cuh"
 
 namespace mhd {
 
-// float buffers (L*P floats each)
+// Pencil buffers and their successive contents.
 enum {
-  F_R = 0, F_VN, F_VT1, F_VT2, F_E, F_B1, F_B2, F_BN, F_DL, F_DXL, F_PA, F_VA,
-  F_G0, F_G1, F_G2, F_G3, F_G4, F_S, F_H2, F_GAM, F_T, F_FX, F_Q, F_COUNT
+  F_R = 0,   // rho -> rho_lag (= q_rho) -> rho_new
+  F_VN,      // v_n -> q_mn -> v_n,new
+  F_VT1,     // v_t1 -> q_m1 -> v_t1,new
+  F_VT2,     // v_t2 -> q_m2 -> v_t2,new
+  F_P,       // p -> Bnap (MOC) -> flux m2 -> species flux 3 / 7
+  F_B1,      // Bcc_t1 -> Blg1 -> q_B1 -> B1,new
+  F_B2,      // Bcc_t2 -> Blg2 -> q_B2 -> B2,new
+  F_BN,      // face-normal B
+  F_DXL,     // Lagrangian width
+  F_VA,      // Va at interface i+1/2
+  F_PA,      // Pa -> Bay -> flux E -> species q 7
+  F_GAM,     // gamma -> Vay -> flux B1
+  F_S,       // sum H+p+He+He+ -> Baz -> flux B2 -> remapped sum
+  F_H2,      // H2 -> Vaz -> species q 3 -> remapped H2
+  F_G0,      // slope; then IM1 -> species q 0 / 4
+  F_G1,      // slope; then IM2 -> species q 1 / 5
+  F_G2,      // slope; then flux rho -> species flux 0 / 4
+  F_G3,      // slope; then flux mn -> species flux 1 / 5
+  F_G4,      // slope; then flux m1 -> species flux 2 / 6
+  F_T,       // T-switch variable (p ghosts, e inside) -> q_E -> E_new
+  F_IMN,     // momentum increment along the sweep -> species q 2 / 6
+  F_SW,      // remap T switch (+-0.5) of cells 0..n+1
+  F_COUNT
 };
-// double buffers (L*P doubles each)
-enum { D_DM = 0, D_MN, D_MT1, D_MT2, D_EN, D_PH1, D_PH2, D_SP, D_COUNT };
+enum { C_DX = 0, C_RDX, C_X2, C_COUNT };   // FP32 dx(i), 1/(x(i)-x(i-1)), x(i+1)-x(i-1)
 
 __host__ __device__ inline size_t sweep32_smem_bytes(int n, int P) {
   size_t L = (size_t)n + 4;
-  return L * P * (D_COUNT * sizeof(double) + F_COUNT * sizeof(float));
+  return (L * P * F_COUNT + L * C_COUNT) * sizeof(float);
 }
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
-template <int DIR, int P, int NT>
-__global__ void __launch_bounds__(NT) sweep32_kernel(SweepArgs A) {
-  extern __shared__ double smd[];
+// The P pencils of a CTA, addressed without a per-pencil table: pencil p
+// starts p transverse strides after pencil 0 (adjacent y rows for the x
+// sweep, adjacent x columns for the y and z sweeps).
+template <int DIR, int P>
+struct PencilRun {
+  long long b0, sp, sd;
+  __device__ PencilRun(const Grid &g) {
+    sd = g.st[DIR];
+    if (DIR == 0) { b0 = gidx(g, -1, blockIdx.x * P + 1, blockIdx.y + 1); sp = g.st[1]; }
+    else if (DIR == 1) { b0 = gidx(g, blockIdx.x * P + 1, -1, blockIdx.y + 1); sp = 1; }
+    else { b0 = gidx(g, blockIdx.x * P + 1, blockIdx.y + 1, -1); sp = 1; }
+  }
+  // global offset of sweep position i (-1..n+2) on pencil p
+  __device__ __forceinline__ long long at(int p, int i) const { return b0 + p * sp + (long long)(i + 1) * sd; }
+};
+
+template <int DIR, int P, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
+  extern __shared__ float smf[];
   const Grid &g = A.g;
   const int N = g.n[DIR];
   const int L = N + 4;
   const int LP = L * P;
-  float *smf = reinterpret_cast<float *>(smd + (size_t)D_COUNT * LP);
-  const double dtd = A.dt;
+  float *cf = smf + (size_t)F_COUNT * LP;
   const float dt = (float)A.dt;
   const float facdep = (float)A.ph.facdep;
   const float kb = (float)A.ph.kb;
   const int tid = threadIdx.x;
-  const double *xe = g.x[DIR];
-  const double *dxe = g.dx[DIR];
-  const double *rdx = g.rdx[DIR];   // 1/(x(i)-x(i-1))
-  Pencil<DIR, P> pc(g);
+  const double *rdx = g.rdx[DIR];
+  PencilRun<DIR, P> pc(g);
   constexpr int C1 = (DIR + 1) % 3, C2 = (DIR + 2) % 3;
   auto Fb = [&](int b, int i, int p) -> float & { return smf[b * LP + (i + 1) * P + p]; };
-  auto Db = [&](int b, int i, int p) -> double & { return smd[b * LP + (i + 1) * P + p]; };
+  auto cx = [&](int c, int i) -> float { return cf[c * L + i + 1]; };
   const bool perL = g.bcl[DIR] != 1, perR = g.bcr[DIR] != 1;
-  auto src_of = [&](int i) {
-    if (i <= 0) return perL ? i + N : 1;
-    return perR ? i - N : N;
+  // ghost positions whose value is a copy of interior cell i
+  auto for_ghosts = [&](int i, auto &&fn) {
+    if (perL ? i == N - 1 : i == 1) fn(-1);
+    if (perL ? i == N : i == 1) fn(0);
+    if (perR ? i == 1 : i == N) fn(N + 1);
+    if (perR ? i == 2 : i == N) fn(N + 2);
   };
-  auto fillf = [&](const int *bl, int nb) {
-    for (int t = tid; t < 4 * P * nb; t += NT) {
-      int b = bl[t / (4 * P)];
-      int r = t % (4 * P);
-      int q = r / P, p = r % P;
-      int i = (q < 2) ? (q - 1) : (N + q - 1);
-      Fb(b, i, p) = Fb(b, src_of(i), p);
-    }
+  auto put = [&](int b, int i, int p, float v) {
+    Fb(b, i, p) = v;
+    for_ghosts(i, [&](int gi) { Fb(b, gi, p) = v; });
   };
-  // VLIMIT in FP32 with the T switch s = sign(0.5, T-3) given
   auto vl = [&](int b, int i, int p, float dm, float d0, float dp, float s) {
     return vlim_sel(Fb(b, i - 1, p), Fb(b, i, p), Fb(b, i + 1, p), dm, d0, dp, s);
   };
-  auto tsw = [&](float e5, float rho) { return fsgn(0.5f, fdiv(1.27f * e5, kb * rho) - 3.0f); };
+  auto tsw = [&](float e5, float rho) { return (1.27f * e5 >= 3.0f * kb * rho) ? 0.5f : -0.5f; };
+  // upwind MUSCL flux of reconstruction buffer qb through interface i
+  auto flux = [&](int qb, int i, int p, float vadt) {
+    const int c = (vadt <= 0.0f) ? i + 1 : i;
+    float gs = vl(qb, c, p, Fb(F_DXL, c - 1, p), Fb(F_DXL, c, p), Fb(F_DXL, c + 1, p), Fb(F_SW, c, p));
+    if (vadt <= 0.0f) return -vadt * (Fb(qb, c, p) - (0.5f * (Fb(F_DXL, c, p) + vadt) * facdep) * gs);
+    return -vadt * (Fb(qb, c, p) + (0.5f * (Fb(F_DXL, c, p) - vadt) * facdep) * gs);
+  };
 
-  // ---------------------------------------------------------------- load
-  for (int t = tid; t < N * P; t += NT) {
-    int i = 1 + t / P, p = t % P;
-    long long a = pc.at(p, i);
-    double rho = A.f.U[0][a];
-    double v[3] = {A.f.U[1][a], A.f.U[2][a], A.f.U[3][a]};
-    Fb(F_R, i, p) = (float)rho;
-    Fb(F_VN, i, p) = (float)v[DIR];
-    Fb(F_VT1, i, p) = (float)v[C1];
-    Fb(F_VT2, i, p) = (float)v[C2];
-    Fb(F_E, i, p) = (float)A.f.U[4][a];
-    double H = A.f.sp[0][a], pr = A.f.sp[1][a], H2 = A.f.sp[2][a], He = A.f.sp[3][a], Hep = A.f.sp[4][a];
-    Fb(F_S, i, p) = (float)(H + pr + He + Hep);
-    Fb(F_H2, i, p) = (float)H2;
-    double dm = dxe[i + 1] * rho;
-    Db(D_DM, i, p) = dm;
-    Db(D_MT1, i, p) = v[C1] * dm;
-    Db(D_MT2, i, p) = v[C2] * dm;
-    Db(D_MN, i, p) = v[DIR] * dm;
-    Fb(F_BN, i, p) = (float)A.f.U[5 + DIR][a];
+  // ------------------------------------------------ A: load (+ ghosts)
+  for (int t = tid; t < L; t += NT) {
+    const double *xe = g.x[DIR];
+    cf[C_DX * L + t] = d2f(g.dx[DIR][t]);
+    cf[C_RDX * L + t] = d2f(rdx[t]);
+    cf[C_X2 * L + t] = (t >= 1 && t + 1 < L) ? d2f(xe[t + 1] - xe[t - 1]) : 1.0f;
   }
   for (int t = tid; t < L * P; t += NT) {
     int i = t / P - 1, p = t % P;
     long long a = pc.at(p, i);
-    Fb(F_B1, i, p) = (float)A.f.bcc[C1][a];
-    Fb(F_B2, i, p) = (float)A.f.bcc[C2][a];
+    Fb(F_B1, i, p) = d2f(A.f.bcc[C1][a]);
+    Fb(F_B2, i, p) = d2f(A.f.bcc[C2][a]);
+    if (i < 1 || i > N) continue;
+    put(F_R, i, p, d2f(A.f.U[0][a]));
+    put(F_VN, i, p, d2f(A.f.U[1 + DIR][a]));
+    put(F_VT1, i, p, d2f(A.f.U[1 + C1][a]));
+    put(F_VT2, i, p, d2f(A.f.U[1 + C2][a]));
+    float pr = d2f(A.f.U[4][a]);
+    put(F_P, i, p, pr);
+    for_ghosts(i, [&](int gi) { Fb(F_T, gi, p) = pr; });
+    float S = d2f(A.f.sp[0][a]) + d2f(A.f.sp[1][a]) + d2f(A.f.sp[3][a]) + d2f(A.f.sp[4][a]);
+    put(F_S, i, p, S);
+    put(F_H2, i, p, d2f(A.f.sp[2][a]));
+    // the face-field exchange rewrites the ghost faces (incl. face n+1)
+    double bn = A.f.U[5 + DIR][a];
+    put(F_BN, i, p, d2f(bn));
+    for_ghosts(i, [&](int gi) { A.f.U[5 + DIR][pc.at(p, gi)] = bn; });
   }
   __syncthreads();
-  {
-    const int bl[8] = {F_R, F_VN, F_VT1, F_VT2, F_E, F_S, F_H2, F_BN};
-    fillf(bl, 8);
-  }
-  __syncthreads();
-  // the face-field exchange rewrites the ghost faces (incl. face n+1)
-  for (int t = tid; t < 4 * P; t += NT) {
-    int q = t / P, p = t % P;
-    int i = (q < 2) ? (q - 1) : (N + q - 1);
-    A.f.U[5 + DIR][pc.at(p, i)] = (double)A.f.U[5 + DIR][pc.at(p, src_of(i))];
-  }
-  // per-cell gamma and the RHS slopes (T from p)
+  // ------------------------------------------------ B: gamma, RHS slopes
   for (int t = tid; t < (N + 2) * P; t += NT) {
     int i = t / P, p = t % P;
     float S = Fb(F_S, i, p), H2 = Fb(F_H2, i, p);
     Fb(F_GAM, i, p) = fdiv(5.0f * S + 7.0f * H2, 3.0f * S + 5.0f * H2);
-    float dm = (float)dxe[i], d0 = (float)dxe[i + 1], dp = (float)dxe[i + 2];
-    float s = tsw(Fb(F_E, i, p), Fb(F_R, i, p));
+    float dm = cx(C_DX, i - 1), d0 = cx(C_DX, i), dp = cx(C_DX, i + 1);
+    float s = tsw(Fb(F_P, i, p), Fb(F_R, i, p));
     Fb(F_G0, i, p) = vl(F_R, i, p, dm, d0, dp, s);
     Fb(F_G1, i, p) = vl(F_VN, i, p, dm, d0, dp, s);
-    Fb(F_G2, i, p) = vl(F_E, i, p, dm, d0, dp, s);
+    Fb(F_G2, i, p) = vl(F_P, i, p, dm, d0, dp, s);
     Fb(F_G3, i, p) = vl(F_B1, i, p, dm, d0, dp, s);
     Fb(F_G4, i, p) = vl(F_B2, i, p, dm, d0, dp, s);
   }
   __syncthreads();
-  // ------------------------------------------------------------ RHS
+  // ------------------------------------------------ C: Riemann (RHS)
   for (int t = tid; t < (N + 1) * P; t += NT) {
     int i = t / P, p = t % P;
-    float rA = Fb(F_R, i, p), rB = Fb(F_R, i + 1, p), pA = Fb(F_E, i, p), pB = Fb(F_E, i + 1, p);
+    float rA = Fb(F_R, i, p), rB = Fb(F_R, i + 1, p), pA = Fb(F_P, i, p), pB = Fb(F_P, i + 1, p);
     float t1A = Fb(F_B1, i, p), t2A = Fb(F_B2, i, p), t1B = Fb(F_B1, i + 1, p), t2B = Fb(F_B2, i + 1, p);
     float cm = sqrtf(fdiv(Fb(F_GAM, i, p) * pA + t1A * t1A + t2A * t2A, rA));
-    float depend1 = fmx(0.0f, 0.5f * ((float)dxe[i + 1] - cm * dt) * facdep);
+    float depend1 = fmx(0.0f, 0.5f * (cx(C_DX, i) - cm * dt) * facdep);
     cm = sqrtf(fdiv(Fb(F_GAM, i + 1, p) * pB + t1B * t1B + t2B * t2B, rB));
-    float depend2 = fmx(0.0f, 0.5f * ((float)dxe[i + 2] - cm * dt) * facdep);
+    float depend2 = fmx(0.0f, 0.5f * (cx(C_DX, i + 1) - cm * dt) * facdep);
     float QL1 = posmask(rA + depend1 * Fb(F_G0, i, p), rA);
     float QR1 = posmask(rB - depend2 * Fb(F_G0, i + 1, p), rB);
     float QL2 = Fb(F_VN, i, p) + depend1 * Fb(F_G1, i, p);
@@ -158,52 +196,32 @@ __global__ void __launch_bounds__(NT) sweep32_kernel(SweepArgs A) {
     Fb(F_VA, i, p) = Va;
   }
   __syncthreads();
-  // interface displacement Va dt and the Lagrangian widths
-  for (int t = tid; t < L * P; t += NT) {
-    int i = t / P - 1, p = t % P;
-    Fb(F_DL, i, p) = (i >= 0 && i <= N) ? Fb(F_VA, i, p) * dt : 0.0f;
-  }
-  __syncthreads();
+  // ------------------------------------------------ D: Lagrangian step
   for (int t = tid; t < N * P; t += NT) {
     int i = 1 + t / P, p = t % P;
     long long a = pc.at(p, i);
-    float dxl = ((float)dxe[i + 1] + Fb(F_DL, i, p)) - Fb(F_DL, i - 1, p);
-    Fb(F_DXL, i, p) = dxl;
-    double dm = Db(D_DM, i, p);
+    float dx0 = cx(C_DX, i);
+    float Va1 = Fb(F_VA, i, p), Va0 = Fb(F_VA, i - 1, p), Pa1 = Fb(F_PA, i, p), Pa0 = Fb(F_PA, i - 1, p);
+    float dxl = (dx0 + Va1 * dt) - Va0 * dt;
     float rho = Fb(F_R, i, p);
+    float dm = dx0 * rho;
     float S = Fb(F_S, i, p), H2 = Fb(F_H2, i, p);
     float g1 = fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
     float vn = Fb(F_VN, i, p), v1 = Fb(F_VT1, i, p), v2 = Fb(F_VT2, i, p);
-    float bx = (float)A.f.bcc[0][a], by = (float)A.f.bcc[1][a], bz = (float)A.f.bcc[2][a];
-    float e = fdiv(Fb(F_E, i, p), rho * g1) + 0.5f * (vn * vn + v1 * v1 + v2 * v2) +
-              fdiv(0.5f * (bx * bx + by * by + bz * bz), rho);
-    double dPa = (double)(Fb(F_PA, i, p) - Fb(F_PA, i - 1, p));
-    double dPV = (double)(Fb(F_PA, i, p) * Fb(F_VA, i, p) - Fb(F_PA, i - 1, p) * Fb(F_VA, i - 1, p));
-    Db(D_MN, i, p) = Db(D_MN, i, p) - dtd * dPa;
-    double En = (double)e * dm - dtd * dPV;
-    Db(D_EN, i, p) = En;
-    double ph1 = (double)Fb(F_B1, i, p) * dxe[i + 1], ph2 = (double)Fb(F_B2, i, p) * dxe[i + 1];
-    Db(D_PH1, i, p) = ph1;
-    Db(D_PH2, i, p) = ph2;
+    float bn = d2f(A.f.bcc[DIR][a]), b1 = Fb(F_B1, i, p), b2 = Fb(F_B2, i, p);
+    float e = fdiv(Fb(F_P, i, p), rho * g1) + 0.5f * (vn * vn + v1 * v1 + v2 * v2) +
+              fdiv(0.5f * (bn * bn + b1 * b1 + b2 * b2), rho);
+    float EL = e * dm - dt * (Pa1 * Va1 - Pa0 * Va0);
+    Fb(F_IMN, i, p) = -dt * (Pa1 - Pa0);
     float inv = fdiv(1.0f, dxl);
-    Fb(F_R, i, p) = (float)dm * inv;                       // rho after the Lagrangian step
-    Fb(F_B1, i, p) = (float)ph1 * inv;                     // Blg
-    Fb(F_B2, i, p) = (float)ph2 * inv;
-    Fb(F_T, i, p) = (float)(En / dm);                      // e, for MOC's T switch inside
+    Fb(F_T, i, p) = fdiv(EL, dm);   // e after RHS: MOC's T switch inside
+    put(F_DXL, i, p, dxl);
+    put(F_R, i, p, dm * inv);
+    put(F_B1, i, p, b1 * dx0 * inv);
+    put(F_B2, i, p, b2 * dx0 * inv);
   }
   __syncthreads();
-  // ------------------------------------------------------------ MOC
-  {
-    // rho (E2), dxlagM and Blg (E3); the p ghosts keep p for the switch
-    const int bl[4] = {F_R, F_DXL, F_B1, F_B2};
-    fillf(bl, 4);
-    for (int t = tid; t < 4 * P; t += NT) {
-      int q = t / P, p = t % P;
-      int i = (q < 2) ? (q - 1) : (N + q - 1);
-      Fb(F_T, i, p) = Fb(F_E, i, p);
-    }
-  }
-  __syncthreads();
+  // ------------------------------------------------ E: MOC slopes
   for (int t = tid; t < (N + 2) * P; t += NT) {
     int i = t / P, p = t % P;
     float dm = Fb(F_DXL, i - 1, p), d0 = Fb(F_DXL, i, p), dp = Fb(F_DXL, i + 1, p);
@@ -215,10 +233,10 @@ __global__ void __launch_bounds__(NT) sweep32_kernel(SweepArgs A) {
     Fb(F_G4, i, p) = vl(F_B2, i, p, dm, d0, dp, s);
   }
   __syncthreads();
+  // ------------------------------------------------ F: characteristics
   for (int t = tid; t < (N + 1) * P; t += NT) {
     int i = t / P, p = t % P;
-    float Bnap = Fb(F_BN, i + 1, p) +
-                 Fb(F_DL, i, p) * fdiv(Fb(F_BN, i + 2, p) - Fb(F_BN, i, p), (float)(xe[i + 2] - xe[i]));
+    float Bnap = Fb(F_BN, i + 1, p) + Fb(F_VA, i, p) * dt * fdiv(Fb(F_BN, i + 2, p) - Fb(F_BN, i, p), cx(C_X2, i));
     float D0 = Fb(F_DXL, i, p), D1 = Fb(F_DXL, i + 1, p);
     float rA = Fb(F_R, i, p), rB = Fb(F_R, i + 1, p);
     float deni = sqrtf(fdiv(D0 + D1, D0 * rB + D1 * rA));
@@ -242,129 +260,160 @@ __global__ void __launch_bounds__(NT) sweep32_kernel(SweepArgs A) {
     float Bay, Vay, Baz, Vaz;
     chareq<float>(QL11, QL12, QL13, QR11, QR12, QR13, Bay, Vay);
     chareq<float>(QL21, QL22, QL13, QR21, QR22, QR13, Baz, Vaz);
-    // reuse slope-free buffers: Bnap, Bay, Vay, Baz, Vaz
-    Fb(F_S, i, p) = Bnap;     // species sums are no longer needed until REMAP
-    Fb(F_H2, i, p) = Bay;
+    Fb(F_P, i, p) = Bnap;
+    Fb(F_PA, i, p) = Bay;
     Fb(F_GAM, i, p) = Vay;
-    Fb(F_PA, i, p) = Baz;
-    Fb(F_FX, i, p) = Vaz;
+    Fb(F_S, i, p) = Baz;
+    Fb(F_H2, i, p) = Vaz;
   }
   __syncthreads();
+  // ------------------------------ G: MOC update and remap reconstruction
   for (int t = tid; t < N * P; t += NT) {
     int i = 1 + t / P, p = t % P;
-    float Bnap = Fb(F_S, i, p), Bnam = Fb(F_S, i - 1, p);
+    float Bnap = Fb(F_P, i, p), Bnam = Fb(F_P, i - 1, p);
     float Vnap = Fb(F_VA, i, p), Vnam = Fb(F_VA, i - 1, p);
-    float Bay1 = Fb(F_H2, i, p), Bay0 = Fb(F_H2, i - 1, p), Vay1 = Fb(F_GAM, i, p), Vay0 = Fb(F_GAM, i - 1, p);
-    float Baz1 = Fb(F_PA, i, p), Baz0 = Fb(F_PA, i - 1, p), Vaz1 = Fb(F_FX, i, p), Vaz0 = Fb(F_FX, i - 1, p);
-    Db(D_MN, i, p) += dtd * (double)(0.5f * (Bnap * Bnap - Bnam * Bnam));
-    Db(D_MT1, i, p) += dtd * (double)(Bnap * Bay1 - Bnam * Bay0);
-    Db(D_MT2, i, p) += dtd * (double)(Bnap * Baz1 - Bnam * Baz0);
-    Db(D_EN, i, p) += dtd * (double)((0.5f * Bnap * Vnap + Bay1 * Vay1 + Baz1 * Vaz1) * Bnap -
-                                     (0.5f * Bnam * Vnam + Bay0 * Vay0 + Baz0 * Vaz0) * Bnam);
-    Db(D_PH1, i, p) += dtd * (double)(Bnap * Vay1 - Bnam * Vay0);
-    Db(D_PH2, i, p) += dtd * (double)(Bnap * Vaz1 - Bnam * Vaz0);
+    float Bay1 = Fb(F_PA, i, p), Bay0 = Fb(F_PA, i - 1, p), Vay1 = Fb(F_GAM, i, p), Vay0 = Fb(F_GAM, i - 1, p);
+    float Baz1 = Fb(F_S, i, p), Baz0 = Fb(F_S, i - 1, p), Vaz1 = Fb(F_H2, i, p), Vaz0 = Fb(F_H2, i - 1, p);
+    float dxl = Fb(F_DXL, i, p), inv = fdiv(1.0f, dxl);
+    float rl = Fb(F_R, i, p), dm = rl * dxl;
+    float imn = Fb(F_IMN, i, p) + dt * (0.5f * (Bnap * Bnap - Bnam * Bnam));
+    float im1 = dt * (Bnap * Bay1 - Bnam * Bay0);
+    float im2 = dt * (Bnap * Baz1 - Bnam * Baz0);
+    Fb(F_IMN, i, p) = imn;
+    Fb(F_G0, i, p) = im1;
+    Fb(F_G1, i, p) = im2;
+    float EL = Fb(F_T, i, p) * dm + dt * ((0.5f * Bnap * Vnap + Bay1 * Vay1 + Baz1 * Vaz1) * Bnap -
+                                          (0.5f * Bnam * Vnam + Bay0 * Vay0 + Baz0 * Vaz0) * Bnam);
+    const float qE = EL * inv;
+    put(F_T, i, p, qE);
+    put(F_SW, i, p, tsw(qE, rl));   // the remap's T switch, from E and rho
+    put(F_B1, i, p, Fb(F_B1, i, p) + dt * (Bnap * Vay1 - Bnam * Vay0) * inv);
+    put(F_B2, i, p, Fb(F_B2, i, p) + dt * (Bnap * Vaz1 - Bnam * Vaz0) * inv);
+    put(F_VN, i, p, Fb(F_VN, i, p) * rl + imn * inv);
+    put(F_VT1, i, p, Fb(F_VT1, i, p) * rl + im1 * inv);
+    put(F_VT2, i, p, Fb(F_VT2, i, p) * rl + im2 * inv);
   }
   __syncthreads();
-  // ------------------------------------------------------------ REMAP
-  // reconstruction densities q = Q / dxlag (FP32), ghosts by E4
-  for (int t = tid; t < N * P; t += NT) {
-    int i = 1 + t / P, p = t % P;
-    float inv = fdiv(1.0f, Fb(F_DXL, i, p));
-    Fb(F_R, i, p) = (float)Db(D_DM, i, p) * inv;
-    Fb(F_VN, i, p) = (float)Db(D_MN, i, p) * inv;
-    Fb(F_VT1, i, p) = (float)Db(D_MT1, i, p) * inv;
-    Fb(F_VT2, i, p) = (float)Db(D_MT2, i, p) * inv;
-    Fb(F_E, i, p) = (float)Db(D_EN, i, p) * inv;
-    Fb(F_B1, i, p) = (float)Db(D_PH1, i, p) * inv;
-    Fb(F_B2, i, p) = (float)Db(D_PH2, i, p) * inv;
-  }
-  __syncthreads();
-  {
-    const int bl[7] = {F_R, F_VN, F_VT1, F_VT2, F_E, F_B1, F_B2};
-    fillf(bl, 7);
-  }
-  __syncthreads();
-  for (int t = tid; t < (N + 2) * P; t += NT) {
+  // ------------------------------------------------ H: field fluxes
+  for (int t = tid; t < (N + 1) * P; t += NT) {
     int i = t / P, p = t % P;
-    Fb(F_T, i, p) = tsw(Fb(F_E, i, p), Fb(F_R, i, p));
+    float vadt = Fb(F_VA, i, p) * dt;
+    Fb(F_G2, i, p) = flux(F_R, i, p, vadt);
+    Fb(F_G3, i, p) = flux(F_VN, i, p, vadt);
+    Fb(F_G4, i, p) = flux(F_VT1, i, p, vadt);
+    Fb(F_P, i, p) = flux(F_VT2, i, p, vadt);
+    Fb(F_PA, i, p) = flux(F_T, i, p, vadt);
+    Fb(F_GAM, i, p) = flux(F_B1, i, p, vadt);
+    Fb(F_S, i, p) = flux(F_B2, i, p, vadt);
   }
   __syncthreads();
-  // one remapped column: slope -> upwind flux -> FP64 accumulation
-  auto remap = [&](int qb, int db, auto &&store) {
-    for (int t = tid; t < (N + 2) * P; t += NT) {
-      int i = t / P, p = t % P;
-      Fb(F_G0, i, p) = vl(qb, i, p, Fb(F_DXL, i - 1, p), Fb(F_DXL, i, p), Fb(F_DXL, i + 1, p), Fb(F_T, i, p));
-    }
-    __syncthreads();
-    for (int t = tid; t < (N + 1) * P; t += NT) {
-      int i = t / P, p = t % P;
-      float vadt = Fb(F_DL, i, p);
-      float F;
-      if (vadt <= 0.0f) F = -vadt * (Fb(qb, i + 1, p) - (0.5f * (Fb(F_DXL, i + 1, p) + vadt) * facdep) * Fb(F_G0, i + 1, p));
-      else F = -vadt * (Fb(qb, i, p) + (0.5f * (Fb(F_DXL, i, p) - vadt) * facdep) * Fb(F_G0, i, p));
-      Fb(F_FX, i, p) = F;
-    }
-    __syncthreads();
-    for (int t = tid; t < N * P; t += NT) {
-      int i = 1 + t / P, p = t % P;
-      double q = Db(db, i, p) + (double)Fb(F_FX, i, p) - (double)Fb(F_FX, i - 1, p);
-      store(i, p, q * rdx[i + 1]);
-    }
-    __syncthreads();
-  };
-  // species first: S = n dx, q = S / dxlag
-  for (int s = 0; s < 8; s++) {
-    for (int t = tid; t < N * P; t += NT) {
-      int i = 1 + t / P, p = t % P;
-      double S = A.f.sp[s][pc.at(p, i)] * dxe[i + 1];
-      Db(D_SP, i, p) = S;
-      Fb(F_Q, i, p) = (float)S * fdiv(1.0f, Fb(F_DXL, i, p));
-      if (s == 0) { Fb(F_S, i, p) = 0.0f; Fb(F_H2, i, p) = 0.0f; }
-    }
-    __syncthreads();
-    const int bl[1] = {F_Q};
-    fillf(bl, 1);
-    __syncthreads();
-    const double mn = A.ph.ndmin[s];
-    remap(F_Q, D_SP, [&](int i, int p, double v) {
-      A.f.sp[s][pc.at(p, i)] = fmx(mn, v);
-      if (s == 2) Fb(F_H2, i, p) = (float)v;
-      else if (s < 5) Fb(F_S, i, p) += (float)v;
-    });
-  }
-  remap(F_R, D_DM, [&](int i, int p, double v) { Db(D_DM, i, p) = v; });
-  remap(F_VN, D_MN, [&](int i, int p, double v) { Db(D_MN, i, p) = v; });
-  remap(F_VT1, D_MT1, [&](int i, int p, double v) { Db(D_MT1, i, p) = v; });
-  remap(F_VT2, D_MT2, [&](int i, int p, double v) { Db(D_MT2, i, p) = v; });
-  remap(F_E, D_EN, [&](int i, int p, double v) { Db(D_EN, i, p) = v; });
-  remap(F_B1, D_PH1, [&](int i, int p, double v) { Db(D_PH1, i, p) = v; });
-  remap(F_B2, D_PH2, [&](int i, int p, double v) { Db(D_PH2, i, p) = v; });
-  // -------------------------------------------- primitives and floors
+  // ------------------------- I: field finish, species 0-3 reconstruction
   const double rfloor = 1.27 * A.ph.rmin;
+  const float rfloor_f = d2f(rfloor);
   for (int t = tid; t < N * P; t += NT) {
     int i = 1 + t / P, p = t % P;
     long long a = pc.at(p, i);
-    double rho = fmx(rfloor, Db(D_DM, i, p));
-    double invd = 1.0 / rho;
-    double v[3];
-    v[DIR] = Db(D_MN, i, p) * invd;
-    v[C1] = Db(D_MT1, i, p) * invd;
-    v[C2] = Db(D_MT2, i, p) * invd;
-    float S = Fb(F_S, i, p), H2 = Fb(F_H2, i, p);
-    double g1 = (double)fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
-    double ekin = 0.5 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) * rho;
-    double bn = A.f.bcc[DIR][a], l1 = Db(D_PH1, i, p), l2 = Db(D_PH2, i, p);
-    double emag = 0.5 * (bn * bn + l1 * l1 + l2 * l2);
-    double pr = (Db(D_EN, i, p) - ekin - emag) * g1;
-    pr = fmx(A.ph.pmin, pr);
-    pr = fmn(A.ph.pmax, pr);
-    A.f.U[0][a] = rho;
-    A.f.U[1][a] = v[0];
-    A.f.U[2][a] = v[1];
-    A.f.U[3][a] = v[2];
-    A.f.U[4][a] = pr;
-    if (!(pr == pr) || !(v[0] == v[0]) || !(v[1] == v[1]) || !(v[2] == v[2]) || !(rho < 1e300))
-      flag(A.err, ERRB_NONFINITE);
+    const float rw = cx(C_RDX, i), dxl = Fb(F_DXL, i, p);
+    double r0 = A.f.U[0][a];
+    double r1 = r0 + rdx[i + 1] * (f2d(Fb(F_G2, i, p)) - f2d(Fb(F_G2, i - 1, p)));
+    float rf = d2f(r1);
+    float drho = (Fb(F_G2, i, p) - Fb(F_G2, i - 1, p)) * rw;
+    if (!(rf > rfloor_f)) {   // density floor (:1293-1296)
+      r1 = rfloor;
+      rf = rfloor_f;
+      drho = rfloor_f - d2f(r0);
+    }
+    A.f.U[0][a] = r1;
+    Fb(F_R, i, p) = rf;
+    const float irf = fdiv(1.0f, rf);
+    auto mom = [&](int comp, int fb, float inc) {
+      double v0 = A.f.U[1 + comp][a];
+      float v0f = d2f(v0);
+      float dM = (inc + Fb(fb, i, p) - Fb(fb, i - 1, p)) * rw;
+      float dv = (dM - drho * v0f) * irf;
+      A.f.U[1 + comp][a] = v0 + f2d(dv);
+      return v0f + dv;
+    };
+    float vn = mom(DIR, F_G3, Fb(F_IMN, i, p));
+    float v1 = mom(C1, F_G4, Fb(F_G0, i, p));
+    float v2 = mom(C2, F_P, Fb(F_G1, i, p));
+    Fb(F_VN, i, p) = vn;
+    Fb(F_VT1, i, p) = v1;
+    Fb(F_VT2, i, p) = v2;
+    Fb(F_T, i, p) = (Fb(F_T, i, p) * dxl + Fb(F_PA, i, p) - Fb(F_PA, i - 1, p)) * rw;
+    Fb(F_B1, i, p) = (Fb(F_B1, i, p) * dxl + Fb(F_GAM, i, p) - Fb(F_GAM, i - 1, p)) * rw;
+    Fb(F_B2, i, p) = (Fb(F_B2, i, p) * dxl + Fb(F_S, i, p) - Fb(F_S, i - 1, p)) * rw;
+    if (!(vn == vn) || !(v1 == v1) || !(v2 == v2) || !(rf < 3e38f)) flag(A.err, ERRB_NONFINITE);
+    // species 0..3: content n dx is unchanged by the Lagrangian step
+    const float w = cx(C_DX, i) * fdiv(1.0f, dxl);
+    put(F_G0, i, p, d2f(A.f.sp[0][a]) * w);
+    put(F_G1, i, p, d2f(A.f.sp[1][a]) * w);
+    put(F_IMN, i, p, d2f(A.f.sp[2][a]) * w);
+    put(F_H2, i, p, d2f(A.f.sp[3][a]) * w);
+  }
+  __syncthreads();
+  // ------------------------------------------------ J: species 0-3 fluxes
+  for (int t = tid; t < (N + 1) * P; t += NT) {
+    int i = t / P, p = t % P;
+    float vadt = Fb(F_VA, i, p) * dt;
+    Fb(F_G2, i, p) = flux(F_G0, i, p, vadt);
+    Fb(F_G3, i, p) = flux(F_G1, i, p, vadt);
+    Fb(F_G4, i, p) = flux(F_IMN, i, p, vadt);
+    Fb(F_P, i, p) = flux(F_H2, i, p, vadt);
+  }
+  __syncthreads();
+  // ------------------------- K: species 0-3 finish, 4-7 reconstruction
+  auto species_new = [&](int s, long long a, int i, int p, int fb) {
+    const float rw = cx(C_RDX, i);
+    double n0 = A.f.sp[s][a];
+    float dn = (Fb(fb, i, p) - Fb(fb, i - 1, p)) * rw;
+    float nf = d2f(n0) + dn;   // remapped value, before the floor
+    const double mn = A.ph.ndmin[s];
+    A.f.sp[s][a] = (nf > d2f(mn)) ? n0 + f2d(dn) : mn;
+    return nf;
+  };
+  for (int t = tid; t < N * P; t += NT) {
+    int i = 1 + t / P, p = t % P;
+    long long a = pc.at(p, i);
+    float S = species_new(0, a, i, p, F_G2) + species_new(1, a, i, p, F_G3) + species_new(3, a, i, p, F_P);
+    float H2 = species_new(2, a, i, p, F_G4);
+    Fb(F_S, i, p) = S;
+    const float w = cx(C_DX, i) * fdiv(1.0f, Fb(F_DXL, i, p));
+    put(F_G0, i, p, d2f(A.f.sp[4][a]) * w);
+    put(F_G1, i, p, d2f(A.f.sp[5][a]) * w);
+    put(F_IMN, i, p, d2f(A.f.sp[6][a]) * w);
+    put(F_PA, i, p, d2f(A.f.sp[7][a]) * w);
+    Fb(F_H2, i, p) = H2;
+  }
+  __syncthreads();
+  // ------------------------------------------------ L: species 4-7 fluxes
+  for (int t = tid; t < (N + 1) * P; t += NT) {
+    int i = t / P, p = t % P;
+    float vadt = Fb(F_VA, i, p) * dt;
+    Fb(F_G2, i, p) = flux(F_G0, i, p, vadt);
+    Fb(F_G3, i, p) = flux(F_G1, i, p, vadt);
+    Fb(F_G4, i, p) = flux(F_IMN, i, p, vadt);
+    Fb(F_P, i, p) = flux(F_PA, i, p, vadt);
+  }
+  __syncthreads();
+  // ---------------------------- M: species 4-7 finish, pressure + floors
+  const float pmin = d2f(A.ph.pmin), pmax = d2f(A.ph.pmax);
+  for (int t = tid; t < N * P; t += NT) {
+    int i = 1 + t / P, p = t % P;
+    long long a = pc.at(p, i);
+    float S = Fb(F_S, i, p) + species_new(4, a, i, p, F_G2);
+    species_new(5, a, i, p, F_G3);
+    species_new(6, a, i, p, F_G4);
+    species_new(7, a, i, p, F_P);
+    float H2 = Fb(F_H2, i, p);
+    float g1 = fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
+    float rf = Fb(F_R, i, p), vn = Fb(F_VN, i, p), v1 = Fb(F_VT1, i, p), v2 = Fb(F_VT2, i, p);
+    float ekin = 0.5f * (vn * vn + v1 * v1 + v2 * v2) * rf;
+    float bn = d2f(A.f.bcc[DIR][a]), l1 = Fb(F_B1, i, p), l2 = Fb(F_B2, i, p);
+    float emag = 0.5f * (bn * bn + l1 * l1 + l2 * l2);
+    float pr = (Fb(F_T, i, p) - ekin - emag) * g1;
+    pr = fminf(pmax, fmaxf(pmin, pr));
+    A.f.U[4][a] = f2d(pr);
   }
 }
 
