@@ -75,15 +75,18 @@ template <int E>
 __global__ void __launch_bounds__(128) emf32_kernel(CT32Args A) {
   const Grid &g = A.g;
   constexpr int da = E, db = (E + 1) % 3, dc = (E + 2) % 3;
-  int Na = g.n[da], Nb = g.n[db], Nc = g.n[dc];
+  // edges: n+1 positions along da and db, n along dc; the thread index
+  // runs fastest along x whatever E is, so neighbouring threads load
+  // neighbouring words
+  int ext[3];
+  ext[da] = g.n[da] + 1; ext[db] = g.n[db] + 1; ext[dc] = g.n[dc];
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long na1 = Na + 1, nb1 = Nb + 1;
-  if (t >= na1 * nb1 * Nc) return;
-  int aa = 1 + (int)(t % na1);
-  int bb = 1 + (int)((t / na1) % nb1);
-  int cc = 1 + (int)(t / (na1 * nb1));
+  if (t >= (long long)ext[0] * ext[1] * ext[2]) return;
   int c3[3];
-  c3[da] = aa; c3[db] = bb; c3[dc] = cc;
+  c3[0] = 1 + (int)(t % ext[0]);
+  c3[1] = 1 + (int)((t / ext[0]) % ext[1]);
+  c3[2] = 1 + (int)(t / ((long long)ext[0] * ext[1]));
+  const int aa = c3[da], bb = c3[db];
   long long p0 = gidx(g, c3[0], c3[1], c3[2]);
   const long long sa = g.st[da], sb = g.st[db];
   const float *rn = A.rn, *sw = A.sw;

@@ -24,17 +24,21 @@ static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
   auto k = sweep32_kernel<DIR, P, kSweepThreads, kSweepMinBlocks>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  // x sweep: P adjacent y rows per CTA; y and z sweeps: P adjacent x columns
+  // starting at padded x = P*blockIdx.x, which covers x = -1 .. n+2
+  const unsigned xgroups = (unsigned)((g.n[0] + 2 + P - 1) / P);
   dim3 grid;
   if (DIR == 0) grid = dim3(g.n[1] / P, g.n[2]);
-  else if (DIR == 1) grid = dim3(g.n[0] / P, g.n[2]);
-  else grid = dim3(g.n[0] / P, g.n[1]);
+  else if (DIR == 1) grid = dim3(xgroups, g.n[2]);
+  else grid = dim3(xgroups, g.n[1]);
   k<<<grid, kSweepThreads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int DIR>
 static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
-  int nb = (DIR == 0) ? a.g.n[1] : a.g.n[0];
+  // the x sweep needs P to divide ny; the y and z sweeps pad their groups
+  const int nb = (DIR == 0) ? a.g.n[1] : 4;
   if (nb % 4 == 0 && sweep32_smem_bytes(a.g.n[DIR], 4) <= kSweepSmemPerCta) return launch32<DIR, 4>(a, s);
   if (nb % 2 == 0 && sweep32_smem_bytes(a.g.n[DIR], 2) <= kSweepSmemPerCta) return launch32<DIR, 2>(a, s);
   if (sweep32_smem_bytes(a.g.n[DIR], 1) > 227 * 1024) return cudaErrorInvalidValue;

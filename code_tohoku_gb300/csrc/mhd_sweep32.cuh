@@ -70,20 +70,59 @@ __host__ __device__ inline size_t sweep32_smem_bytes(int n, int P) {
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
+// Work loop of a phase: items t = threadIdx.x + k*NT < cnt.  Groups of UNR
+// items that are all in range run as one unrolled block, so the loads of
+// the group can be in flight together; the rest run one by one.
+template <int NT, int UNR, class F>
+__device__ __forceinline__ void unrolled(int cnt, F &&f) {
+  int t0 = threadIdx.x;
+  for (; t0 + (UNR - 1) * NT < cnt; t0 += UNR * NT) {
+#pragma unroll
+    for (int k = 0; k < UNR; k++) f(t0 + k * NT);
+  }
+  for (int t = t0; t < cnt; t += NT) f(t);
+}
+
+// Unroll depth of the phases that only touch shared memory.  Their loads
+// have short latency and deeper unrolling raises register pressure: with
+// depth 2 or 4 the 256^3 sweeps run 15-40 % slower on GB300 than with 1.
+constexpr int kSmemUnroll = 1;
+
 // The P pencils of a CTA, addressed without a per-pencil table: pencil p
 // starts p transverse strides after pencil 0 (adjacent y rows for the x
-// sweep, adjacent x columns for the y and z sweeps).
+// sweep, adjacent x columns for the y and z sweeps).  For the y and z
+// sweeps a group starts at padded x index P*blockIdx.x, so the P words a
+// row of the group reads sit in one 32-byte sector (the padded row length
+// n+4 is a multiple of 4 for n divisible by 4); the group may then contain
+// ghost columns (x < 1 or x > n), which are computed along but never
+// stored.  Columns beyond the padded grid read the last column.
 template <int DIR, int P>
 struct PencilRun {
   long long b0, sp, sd;
+  unsigned act;   // bit p: pencil p is an interior pencil
+  int plast;      // last pencil inside the padded grid
   __device__ PencilRun(const Grid &g) {
     sd = g.st[DIR];
-    if (DIR == 0) { b0 = gidx(g, -1, blockIdx.x * P + 1, blockIdx.y + 1); sp = g.st[1]; }
-    else if (DIR == 1) { b0 = gidx(g, blockIdx.x * P + 1, -1, blockIdx.y + 1); sp = 1; }
-    else { b0 = gidx(g, blockIdx.x * P + 1, blockIdx.y + 1, -1); sp = 1; }
+    act = (1u << P) - 1;
+    plast = P - 1;
+    if (DIR == 0) {
+      b0 = gidx(g, -1, blockIdx.x * P + 1, blockIdx.y + 1);
+      sp = g.st[1];
+    } else {
+      const int x0 = (int)blockIdx.x * P - 1;
+      b0 = (DIR == 1) ? gidx(g, x0, -1, blockIdx.y + 1) : gidx(g, x0, blockIdx.y + 1, -1);
+      sp = 1;
+      act = 0;
+      for (int p = 0; p < P; p++)
+        if (x0 + p >= 1 && x0 + p <= g.n[0]) act |= 1u << p;
+      plast = min(P - 1, g.n[0] + 2 - x0);
+    }
   }
+  __device__ __forceinline__ bool active(int p) const { return (act >> p) & 1u; }
   // global offset of sweep position i (-1..n+2) on pencil p
-  __device__ __forceinline__ long long at(int p, int i) const { return b0 + p * sp + (long long)(i + 1) * sd; }
+  __device__ __forceinline__ long long at(int p, int i) const {
+    return b0 + min(p, plast) * sp + (long long)(i + 1) * sd;
+  }
 };
 
 template <int DIR, int P, int NT, int MINB>
@@ -134,30 +173,39 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     cf[C_RDX * L + t] = d2f(rdx[t]);
     cf[C_X2 * L + t] = (t >= 1 && t + 1 < L) ? d2f(xe[t + 1] - xe[t - 1]) : 1.0f;
   }
-  for (int t = tid; t < L * P; t += NT) {
+  unrolled<NT, 4>(L * P, [&](int t) {
     int i = t / P - 1, p = t % P;
     long long a = pc.at(p, i);
-    Fb(F_B1, i, p) = d2f(A.f.bcc[C1][a]);
-    Fb(F_B2, i, p) = d2f(A.f.bcc[C2][a]);
-    if (i < 1 || i > N) continue;
-    put(F_R, i, p, d2f(A.f.U[0][a]));
-    put(F_VN, i, p, d2f(A.f.U[1 + DIR][a]));
-    put(F_VT1, i, p, d2f(A.f.U[1 + C1][a]));
-    put(F_VT2, i, p, d2f(A.f.U[1 + C2][a]));
-    float pr = d2f(A.f.U[4][a]);
+    Fb(F_B1, i, p) = d2f(__ldg(A.f.bcc[C1] + a));
+    Fb(F_B2, i, p) = d2f(__ldg(A.f.bcc[C2] + a));
+  });
+  unrolled<NT, 4>(N * P, [&](int t) {
+    int i = 1 + t / P, p = t % P;
+    long long a = pc.at(p, i);
+    double u0 = __ldg(A.f.U[0] + a), un = __ldg(A.f.U[1 + DIR] + a), u1 = __ldg(A.f.U[1 + C1] + a),
+           u2 = __ldg(A.f.U[1 + C2] + a), u4 = __ldg(A.f.U[4] + a);
+    put(F_R, i, p, d2f(u0));
+    put(F_VN, i, p, d2f(un));
+    put(F_VT1, i, p, d2f(u1));
+    put(F_VT2, i, p, d2f(u2));
+    float pr = d2f(u4);
     put(F_P, i, p, pr);
     for_ghosts(i, [&](int gi) { Fb(F_T, gi, p) = pr; });
-    float S = d2f(A.f.sp[0][a]) + d2f(A.f.sp[1][a]) + d2f(A.f.sp[3][a]) + d2f(A.f.sp[4][a]);
-    put(F_S, i, p, S);
-    put(F_H2, i, p, d2f(A.f.sp[2][a]));
+  });
+  unrolled<NT, 4>(N * P, [&](int t) {
+    int i = 1 + t / P, p = t % P;
+    long long a = pc.at(p, i);
+    double s0 = __ldg(A.f.sp[0] + a), s1 = __ldg(A.f.sp[1] + a), s2 = __ldg(A.f.sp[2] + a),
+           s3 = __ldg(A.f.sp[3] + a), s4 = __ldg(A.f.sp[4] + a), bn = __ldg(A.f.U[5 + DIR] + a);
+    put(F_S, i, p, d2f(s0) + d2f(s1) + d2f(s3) + d2f(s4));
+    put(F_H2, i, p, d2f(s2));
     // the face-field exchange rewrites the ghost faces (incl. face n+1)
-    double bn = A.f.U[5 + DIR][a];
     put(F_BN, i, p, d2f(bn));
-    for_ghosts(i, [&](int gi) { A.f.U[5 + DIR][pc.at(p, gi)] = bn; });
-  }
+    if (pc.active(p)) for_ghosts(i, [&](int gi) { A.f.U[5 + DIR][pc.at(p, gi)] = bn; });
+  });
   __syncthreads();
   // ------------------------------------------------ B: gamma, RHS slopes
-  for (int t = tid; t < (N + 2) * P; t += NT) {
+  unrolled<NT, kSmemUnroll>((N + 2) * P, [&](int t) {
     int i = t / P, p = t % P;
     float S = Fb(F_S, i, p), H2 = Fb(F_H2, i, p);
     Fb(F_GAM, i, p) = fdiv(5.0f * S + 7.0f * H2, 3.0f * S + 5.0f * H2);
@@ -168,10 +216,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     Fb(F_G2, i, p) = vl(F_P, i, p, dm, d0, dp, s);
     Fb(F_G3, i, p) = vl(F_B1, i, p, dm, d0, dp, s);
     Fb(F_G4, i, p) = vl(F_B2, i, p, dm, d0, dp, s);
-  }
+  });
   __syncthreads();
   // ------------------------------------------------ C: Riemann (RHS)
-  for (int t = tid; t < (N + 1) * P; t += NT) {
+  unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
     float rA = Fb(F_R, i, p), rB = Fb(F_R, i + 1, p), pA = Fb(F_P, i, p), pB = Fb(F_P, i + 1, p);
     float t1A = Fb(F_B1, i, p), t2A = Fb(F_B2, i, p), t1B = Fb(F_B1, i + 1, p), t2B = Fb(F_B2, i + 1, p);
@@ -194,10 +242,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
                    l1 * l1 + l2 * l2, QR1, QR2, QR3, r1 * r1 + r2 * r2, Pa, Va);
     Fb(F_PA, i, p) = Pa;
     Fb(F_VA, i, p) = Va;
-  }
+  });
   __syncthreads();
   // ------------------------------------------------ D: Lagrangian step
-  for (int t = tid; t < N * P; t += NT) {
+  unrolled<NT, 4>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
     long long a = pc.at(p, i);
     float dx0 = cx(C_DX, i);
@@ -208,7 +256,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     float S = Fb(F_S, i, p), H2 = Fb(F_H2, i, p);
     float g1 = fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
     float vn = Fb(F_VN, i, p), v1 = Fb(F_VT1, i, p), v2 = Fb(F_VT2, i, p);
-    float bn = d2f(A.f.bcc[DIR][a]), b1 = Fb(F_B1, i, p), b2 = Fb(F_B2, i, p);
+    float bn = d2f(__ldg(A.f.bcc[DIR] + a)), b1 = Fb(F_B1, i, p), b2 = Fb(F_B2, i, p);
     float e = fdiv(Fb(F_P, i, p), rho * g1) + 0.5f * (vn * vn + v1 * v1 + v2 * v2) +
               fdiv(0.5f * (bn * bn + b1 * b1 + b2 * b2), rho);
     float EL = e * dm - dt * (Pa1 * Va1 - Pa0 * Va0);
@@ -219,10 +267,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     put(F_R, i, p, dm * inv);
     put(F_B1, i, p, b1 * dx0 * inv);
     put(F_B2, i, p, b2 * dx0 * inv);
-  }
+  });
   __syncthreads();
   // ------------------------------------------------ E: MOC slopes
-  for (int t = tid; t < (N + 2) * P; t += NT) {
+  unrolled<NT, kSmemUnroll>((N + 2) * P, [&](int t) {
     int i = t / P, p = t % P;
     float dm = Fb(F_DXL, i - 1, p), d0 = Fb(F_DXL, i, p), dp = Fb(F_DXL, i + 1, p);
     float s = tsw(Fb(F_T, i, p), Fb(F_R, i, p));
@@ -231,10 +279,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     Fb(F_G2, i, p) = vl(F_VT2, i, p, dm, d0, dp, s);
     Fb(F_G3, i, p) = vl(F_B1, i, p, dm, d0, dp, s);
     Fb(F_G4, i, p) = vl(F_B2, i, p, dm, d0, dp, s);
-  }
+  });
   __syncthreads();
   // ------------------------------------------------ F: characteristics
-  for (int t = tid; t < (N + 1) * P; t += NT) {
+  unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
     float Bnap = Fb(F_BN, i + 1, p) + Fb(F_VA, i, p) * dt * fdiv(Fb(F_BN, i + 2, p) - Fb(F_BN, i, p), cx(C_X2, i));
     float D0 = Fb(F_DXL, i, p), D1 = Fb(F_DXL, i + 1, p);
@@ -265,10 +313,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     Fb(F_GAM, i, p) = Vay;
     Fb(F_S, i, p) = Baz;
     Fb(F_H2, i, p) = Vaz;
-  }
+  });
   __syncthreads();
   // ------------------------------ G: MOC update and remap reconstruction
-  for (int t = tid; t < N * P; t += NT) {
+  unrolled<NT, 4>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
     float Bnap = Fb(F_P, i, p), Bnam = Fb(F_P, i - 1, p);
     float Vnap = Fb(F_VA, i, p), Vnam = Fb(F_VA, i - 1, p);
@@ -292,10 +340,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     put(F_VN, i, p, Fb(F_VN, i, p) * rl + imn * inv);
     put(F_VT1, i, p, Fb(F_VT1, i, p) * rl + im1 * inv);
     put(F_VT2, i, p, Fb(F_VT2, i, p) * rl + im2 * inv);
-  }
+  });
   __syncthreads();
   // ------------------------------------------------ H: field fluxes
-  for (int t = tid; t < (N + 1) * P; t += NT) {
+  unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
     float vadt = Fb(F_VA, i, p) * dt;
     Fb(F_G2, i, p) = flux(F_R, i, p, vadt);
@@ -305,16 +353,17 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     Fb(F_PA, i, p) = flux(F_T, i, p, vadt);
     Fb(F_GAM, i, p) = flux(F_B1, i, p, vadt);
     Fb(F_S, i, p) = flux(F_B2, i, p, vadt);
-  }
+  });
   __syncthreads();
   // ------------------------- I: field finish, species 0-3 reconstruction
   const double rfloor = 1.27 * A.ph.rmin;
   const float rfloor_f = d2f(rfloor);
-  for (int t = tid; t < N * P; t += NT) {
+  unrolled<NT, 4>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
+    const bool act = pc.active(p);
     long long a = pc.at(p, i);
     const float rw = cx(C_RDX, i), dxl = Fb(F_DXL, i, p);
-    double r0 = A.f.U[0][a];
+    double r0 = __ldg(A.f.U[0] + a);
     double r1 = r0 + rdx[i + 1] * (f2d(Fb(F_G2, i, p)) - f2d(Fb(F_G2, i - 1, p)));
     float rf = d2f(r1);
     float drho = (Fb(F_G2, i, p) - Fb(F_G2, i - 1, p)) * rw;
@@ -323,15 +372,15 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
       rf = rfloor_f;
       drho = rfloor_f - d2f(r0);
     }
-    A.f.U[0][a] = r1;
+    if (act) A.f.U[0][a] = r1;
     Fb(F_R, i, p) = rf;
     const float irf = fdiv(1.0f, rf);
     auto mom = [&](int comp, int fb, float inc) {
-      double v0 = A.f.U[1 + comp][a];
+      double v0 = __ldg(A.f.U[1 + comp] + a);
       float v0f = d2f(v0);
       float dM = (inc + Fb(fb, i, p) - Fb(fb, i - 1, p)) * rw;
       float dv = (dM - drho * v0f) * irf;
-      A.f.U[1 + comp][a] = v0 + f2d(dv);
+      if (act) A.f.U[1 + comp][a] = v0 + f2d(dv);
       return v0f + dv;
     };
     float vn = mom(DIR, F_G3, Fb(F_IMN, i, p));
@@ -343,78 +392,81 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     Fb(F_T, i, p) = (Fb(F_T, i, p) * dxl + Fb(F_PA, i, p) - Fb(F_PA, i - 1, p)) * rw;
     Fb(F_B1, i, p) = (Fb(F_B1, i, p) * dxl + Fb(F_GAM, i, p) - Fb(F_GAM, i - 1, p)) * rw;
     Fb(F_B2, i, p) = (Fb(F_B2, i, p) * dxl + Fb(F_S, i, p) - Fb(F_S, i - 1, p)) * rw;
-    if (!(vn == vn) || !(v1 == v1) || !(v2 == v2) || !(rf < 3e38f)) flag(A.err, ERRB_NONFINITE);
+    if (act && (!(vn == vn) || !(v1 == v1) || !(v2 == v2) || !(rf < 3e38f))) flag(A.err, ERRB_NONFINITE);
     // species 0..3: content n dx is unchanged by the Lagrangian step
     const float w = cx(C_DX, i) * fdiv(1.0f, dxl);
-    put(F_G0, i, p, d2f(A.f.sp[0][a]) * w);
-    put(F_G1, i, p, d2f(A.f.sp[1][a]) * w);
-    put(F_IMN, i, p, d2f(A.f.sp[2][a]) * w);
-    put(F_H2, i, p, d2f(A.f.sp[3][a]) * w);
-  }
+    put(F_G0, i, p, d2f(__ldg(A.f.sp[0] + a)) * w);
+    put(F_G1, i, p, d2f(__ldg(A.f.sp[1] + a)) * w);
+    put(F_IMN, i, p, d2f(__ldg(A.f.sp[2] + a)) * w);
+    put(F_H2, i, p, d2f(__ldg(A.f.sp[3] + a)) * w);
+  });
   __syncthreads();
   // ------------------------------------------------ J: species 0-3 fluxes
-  for (int t = tid; t < (N + 1) * P; t += NT) {
+  unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
     float vadt = Fb(F_VA, i, p) * dt;
     Fb(F_G2, i, p) = flux(F_G0, i, p, vadt);
     Fb(F_G3, i, p) = flux(F_G1, i, p, vadt);
     Fb(F_G4, i, p) = flux(F_IMN, i, p, vadt);
     Fb(F_P, i, p) = flux(F_H2, i, p, vadt);
-  }
+  });
   __syncthreads();
   // ------------------------- K: species 0-3 finish, 4-7 reconstruction
-  auto species_new = [&](int s, long long a, int i, int p, int fb) {
+  auto species_new = [&](int s, long long a, int i, int p, int fb, bool act) {
     const float rw = cx(C_RDX, i);
-    double n0 = A.f.sp[s][a];
+    double n0 = __ldg(A.f.sp[s] + a);
     float dn = (Fb(fb, i, p) - Fb(fb, i - 1, p)) * rw;
     float nf = d2f(n0) + dn;   // remapped value, before the floor
     const double mn = A.ph.ndmin[s];
-    A.f.sp[s][a] = (nf > d2f(mn)) ? n0 + f2d(dn) : mn;
+    if (act) A.f.sp[s][a] = (nf > d2f(mn)) ? n0 + f2d(dn) : mn;
     return nf;
   };
-  for (int t = tid; t < N * P; t += NT) {
+  unrolled<NT, 4>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
+    const bool act = pc.active(p);
     long long a = pc.at(p, i);
-    float S = species_new(0, a, i, p, F_G2) + species_new(1, a, i, p, F_G3) + species_new(3, a, i, p, F_P);
-    float H2 = species_new(2, a, i, p, F_G4);
+    float S = species_new(0, a, i, p, F_G2, act) + species_new(1, a, i, p, F_G3, act) +
+              species_new(3, a, i, p, F_P, act);
+    float H2 = species_new(2, a, i, p, F_G4, act);
     Fb(F_S, i, p) = S;
     const float w = cx(C_DX, i) * fdiv(1.0f, Fb(F_DXL, i, p));
-    put(F_G0, i, p, d2f(A.f.sp[4][a]) * w);
-    put(F_G1, i, p, d2f(A.f.sp[5][a]) * w);
-    put(F_IMN, i, p, d2f(A.f.sp[6][a]) * w);
-    put(F_PA, i, p, d2f(A.f.sp[7][a]) * w);
+    put(F_G0, i, p, d2f(__ldg(A.f.sp[4] + a)) * w);
+    put(F_G1, i, p, d2f(__ldg(A.f.sp[5] + a)) * w);
+    put(F_IMN, i, p, d2f(__ldg(A.f.sp[6] + a)) * w);
+    put(F_PA, i, p, d2f(__ldg(A.f.sp[7] + a)) * w);
     Fb(F_H2, i, p) = H2;
-  }
+  });
   __syncthreads();
   // ------------------------------------------------ L: species 4-7 fluxes
-  for (int t = tid; t < (N + 1) * P; t += NT) {
+  unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
     float vadt = Fb(F_VA, i, p) * dt;
     Fb(F_G2, i, p) = flux(F_G0, i, p, vadt);
     Fb(F_G3, i, p) = flux(F_G1, i, p, vadt);
     Fb(F_G4, i, p) = flux(F_IMN, i, p, vadt);
     Fb(F_P, i, p) = flux(F_PA, i, p, vadt);
-  }
+  });
   __syncthreads();
   // ---------------------------- M: species 4-7 finish, pressure + floors
   const float pmin = d2f(A.ph.pmin), pmax = d2f(A.ph.pmax);
-  for (int t = tid; t < N * P; t += NT) {
+  unrolled<NT, 4>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
+    const bool act = pc.active(p);
     long long a = pc.at(p, i);
-    float S = Fb(F_S, i, p) + species_new(4, a, i, p, F_G2);
-    species_new(5, a, i, p, F_G3);
-    species_new(6, a, i, p, F_G4);
-    species_new(7, a, i, p, F_P);
+    float S = Fb(F_S, i, p) + species_new(4, a, i, p, F_G2, act);
+    species_new(5, a, i, p, F_G3, act);
+    species_new(6, a, i, p, F_G4, act);
+    species_new(7, a, i, p, F_P, act);
     float H2 = Fb(F_H2, i, p);
     float g1 = fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
     float rf = Fb(F_R, i, p), vn = Fb(F_VN, i, p), v1 = Fb(F_VT1, i, p), v2 = Fb(F_VT2, i, p);
     float ekin = 0.5f * (vn * vn + v1 * v1 + v2 * v2) * rf;
-    float bn = d2f(A.f.bcc[DIR][a]), l1 = Fb(F_B1, i, p), l2 = Fb(F_B2, i, p);
+    float bn = d2f(__ldg(A.f.bcc[DIR] + a)), l1 = Fb(F_B1, i, p), l2 = Fb(F_B2, i, p);
     float emag = 0.5f * (bn * bn + l1 * l1 + l2 * l2);
     float pr = (Fb(F_T, i, p) - ekin - emag) * g1;
     pr = fminf(pmax, fmaxf(pmin, pr));
-    A.f.U[4][a] = f2d(pr);
-  }
+    if (act) A.f.U[4][a] = f2d(pr);
+  });
 }
 
 }  // namespace mhd

@@ -229,11 +229,21 @@ class Mhd3D:
         co = [np.ascontiguousarray(a, dtype=np.float64) for a in (st.x, st.dx, st.y, st.dy, st.z, st.dz)]
         self._ck(self.L.mhd_upload(self.h, _ptr(U), _ptr(sp), *[_ptr(c) for c in co]))
 
-    def download(self, with_bcc=True):
-        U = np.empty((8,) + self.shape)
-        sp = np.empty((8,) + self.shape)
-        bcc = np.empty((3,) + self.shape) if with_bcc else None
-        self._ck(self.L.mhd_download(self.h, _ptr(U), _ptr(sp), _ptr(bcc) if with_bcc else None))
+    def download(self, with_bcc=True, out=None):
+        """Copy the state to host arrays: new ones, or `out` = (U, species, bcc)
+        of shapes (8,)+shape, (8,)+shape and (3,)+shape (bcc may be None),
+        C-contiguous float64 (pinned host memory makes the copy faster)."""
+        if out is None:
+            U = np.empty((8,) + self.shape)
+            sp = np.empty((8,) + self.shape)
+            bcc = np.empty((3,) + self.shape) if with_bcc else None
+        else:
+            U, sp, bcc = out
+            for a, lead in ((U, 8), (sp, 8), (bcc, 3)):
+                if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous
+                                      or a.shape != (lead,) + self.shape):
+                    raise ValueError("download: output arrays must be C-contiguous float64 of the state shape")
+        self._ck(self.L.mhd_download(self.h, _ptr(U), _ptr(sp), _ptr(bcc) if bcc is not None else None))
         return U, sp, bcc
 
     def timestep(self):
