@@ -18,7 +18,10 @@ through the C ABI with the state uploaded from pinned host memory and
 downloaded again every step.  `roofline` is for the dominant kernel (the
 fused sweep), with algorithmic bytes from the per-zone budget of the step.
 `cpu_baseline` is the CPU restatement (oracle, C++ with OpenMP) timed on a
-bounded sample on the host cores.
+bounded sample on the host cores.  `stiff_cooling_source` times SOURCE alone
+in the stiff regime of the KI cooling (30x density, dt = 0.05), where the
+surrogate replaces the implicit bisection: FP64, FP32 exact and FP32 +
+surrogate from the same state, with the pressure error against FP64.
 
 `--impl reference` times that CPU restatement alone (the reference itself is
 Fortran + MPI and no Fortran compiler exists on this machine; the restatement
@@ -41,12 +44,13 @@ B_ALG_SWEEP = 104.0     # per sweep: read rho, v3, p, face-B3 (64) + write rho, 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-stiff", action="store_true", help="skip the stiff-cooling SOURCE comparison")
     ap.add_argument("--l1-steps", type=int, default=100,
                     help="FP64 steps of the accuracy comparison (the chosen form runs to the same time)")
     ap.add_argument("--sur-steps", type=int, default=2000)
@@ -83,34 +87,54 @@ def ncu_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks during the timed region (one sample / 200 ms)."""
+    """nvidia-smi clocks during the timed region (one sample every 50 ms).
+
+    The sampler is started first and the region begins once nvidia-smi has
+    produced its first line; only lines read between __enter__'s return and
+    __exit__ are kept."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
         self.lines = []
+        self._all = []
+        self._t0 = self._t1 = None
+
+    def _reader(self):
+        for line in self.proc.stdout:
+            if line.strip():
+                self._all.append((time.perf_counter(), line))
 
     def __enter__(self):
+        import threading
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+        if self.proc:
+            threading.Thread(target=self._reader, daemon=True).start()
+            deadline = time.perf_counter() + 5.0
+            while not self._all and time.perf_counter() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
+        self._t0 = time.perf_counter()
         return self
 
     def __exit__(self, *a):
+        self._t1 = time.perf_counter()
         if self.proc:
+            time.sleep(0.06)   # the sample that covers the end of the region
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [l for l in out.splitlines() if l.strip()]
+                self.proc.wait()
+            self.lines = [l for t, l in self._all if self._t0 <= t <= self._t1 + 0.06]
 
     def summary(self):
         import statistics
@@ -332,6 +356,52 @@ def main():
     e2e = {"value": world * n3 / e2e_s, "unit": "zone-updates/s", "h2d_bytes_per_step": 2 * nb,
            "d2h_bytes_per_step": 2 * nb}
 
+    # The stiff regime of KI cooling, where the learned part works: the same
+    # colliding flow at 30x the density (n = 30 cm^-3) and SOURCE(dt) with
+    # dt = 0.05 Myr, longer than the cooling time of most cells.  SOURCE only,
+    # from the same uploaded state each time; the FP64 form gives the
+    # reference pressure.
+    stiff = None
+    if not args.no_stiff:
+        sst = problems.colliding_flows(args.n)
+        sst.U[0] *= 30.0
+        sst.species *= 30.0
+        sdt = 0.05
+        stiff = {"state": "colliding flow at 30x density", "dt": sdt}
+        p_ref = None
+        for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
+                                 ("fp32_exact", native.PREC_FP32, native.COOL_EXACT),
+                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE)):
+            gs = native.Mhd3D(sst.params, precision=prec, cooling=cool, device=dev)
+            gs.set_stream(stream.cuda_stream)
+            if cool == native.COOL_SURROGATE:
+                gs.surrogate_load(sur_params, 1e-3)
+            times = []
+            for _ in range(3):
+                gs.upload(sst)
+                gs.reset_counters()
+                barrier()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                gs.source(sdt)
+                b.record(stream)
+                barrier()
+                times.append(a.elapsed_time(b))
+            d = gs.diagnostics()
+            pp = gs.download(with_bcc=False)[0][4][2:-2, 2:-2, 2:-2]
+            if p_ref is None:
+                p_ref = pp
+            stiff[name] = {"ms_per_source": min(times), "bisection_cells": d["imc_cells"],
+                           "surrogate_cells": d["surrogate_cells"], "fallback_cells": d["fallback_cells"],
+                           "l1_p_vs_fp64": float(np.abs(pp - p_ref).mean() / np.abs(p_ref).mean())}
+            del gs
+        stiff["surrogate_speedup_vs_fp32_exact"] = (stiff["fp32_exact"]["ms_per_source"] /
+                                                    stiff["fp32_surrogate"]["ms_per_source"])
+        stiff["fp32_surrogate"]["fallback_fraction"] = (
+            stiff["fp32_surrogate"]["fallback_cells"] /
+            max(1, stiff["fp32_surrogate"]["fallback_cells"] + stiff["fp32_surrogate"]["surrogate_cells"]))
+
     if rank != 0:
         return
     hbm, which = peaks()
@@ -352,7 +422,7 @@ def main():
                        "cooling": "KI surrogate MLP (BF16 tensor cores) + Newton polish, IMC fallback",
                        "l2": "inputs larger than L2 (3.7 GB)",
                        "parallelism": f"replicas x{world}"},
-            "plain_fp64": fp64, "l1_error": l1, "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
+            "plain_fp64": fp64, "l1_error": l1, "stiff_cooling_source": stiff, "speedup_vs_fp64": (value / fp64["value"]) if fp64 else None,
             "fp32_exact_cooling": {"value": n3 * args.steps / (msx * 1e-3), "unit": "zone-updates/s",
                                    "imc_cells": dx_["imc_cells"]},
             "surrogate": {"train_s": sur_train_s, "steps": args.sur_steps, "n_data": args.sur_data,
