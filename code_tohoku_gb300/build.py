@@ -8,6 +8,8 @@ one shared library next to this file:
   csrc/mhd_capi.cu  the extern "C" boundary of include/mhd_gb300.h
   csrc/mhd_surrogate.cu  surrogate data, training and evaluation kernels
                     (--fmad=false: its FP64 labels match the CPU IMC bit for bit)
+  csrc/mhd_noalloc.cu  the allocation-free time step
+  csrc/mhd_io.cpp   host code: the reference's output and restart files
 """
 import os
 import shutil
@@ -27,6 +29,7 @@ UNITS = {
     "mhd_capi.cu": ["--fmad=false"],
     "mhd_surrogate.cu": ["--fmad=false"],
     "mhd_noalloc.cu": ["--fmad=false"],
+    "mhd_io.cpp": [],
 }
 
 
@@ -38,8 +41,9 @@ def nvcc():
 
 
 def _sources():
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
-    deps.append(os.path.join(HERE, "..", "include", "mhd_gb300.h"))
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h", ".cpp"))]
+    inc = os.path.join(HERE, "..", "include")
+    deps += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     return deps
 
 
@@ -62,7 +66,7 @@ def build(force=False, verbose=False, extra=()):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = [exe, *ARCH, *COMMON, *flags, *extra, "-c", path, "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
