@@ -40,6 +40,8 @@ struct mhd_handle {
   float *rn32 = nullptr, *sw32 = nullptr;
   float *emf32[3] = {nullptr, nullptr, nullptr};
   float *coordsf = nullptr;
+  float *dtf = nullptr;                  // BC=4 reservoir (device)
+  bool inflow_set = false;
   double *divv = nullptr;
   double *diag_part = nullptr;
   unsigned long long *dtred = nullptr;   // [0] tCFL, [1] tLMT bits, [2] IMC, [3] surrogate, [4] fallback
@@ -94,11 +96,16 @@ int fail(mhd_handle *h, int code, const char *fmt, ...) {
 
 const double kNdMinH = 0.91, kNdMinHe = 0.09;
 
-// ghost exchange of a list of arrays in the directions of mask (x,y,z order)
-int fill(mhd_handle *h, std::initializer_list<double *> arrays, int dirs, int nol, int species = 0) {
+// ghost exchange of a list of arrays in the directions of mask (x,y,z order);
+// rules: the BC=4 rule of each array on an inflow side of x
+int fill(mhd_handle *h, std::initializer_list<double *> arrays, int dirs, int nol, int species = 0,
+         std::initializer_list<int> rules = {}) {
   FillArgs a{};
   a.nf = 0;
   for (double *p : arrays) a.f[a.nf++] = p;
+  int q = 0;
+  for (int r : rules) a.rule[q++] = r;
+  a.in = h->ph.in;
   for (int d = 0; d < 3; d++)
     if (dirs & (1 << d)) CK(ghost_fill(h->g, a, d, nol, species, h->stream));
   return MHD_OK;
@@ -115,6 +122,14 @@ int check_err(mhd_handle *h) {
 
 bool valid_bc(int b) { return b == 1 || b == 3; }
 
+// a handle with BC=4 needs its inflow data before any exchange
+int need_inflow(mhd_handle *h) {
+  if ((h->p.bc[0] == 4 || h->p.bc[1] == 4) && !h->inflow_set)
+    return fail(h, MHD_ERR_STATE, "BC code 4 needs mhd_set_inflow before the state is used");
+  h->ph.in.time = h->time;   // the reference's module time during this step
+  return MHD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -123,8 +138,8 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   if (!p || !out) return MHD_ERR_ARG;
   *out = nullptr;
   if (p->nx < 4 || p->ny < 4 || p->nz < 4) return MHD_ERR_ARG;
-  for (int q = 0; q < 6; q++)
-    if (!valid_bc(p->bc[q])) return MHD_ERR_ARG;   // codes 1 (free) and 3 (periodic)
+  for (int q = 0; q < 6; q++)   // codes 1 (free), 3 (periodic), 4 (inflow, x sides only)
+    if (!(valid_bc(p->bc[q]) || (q < 2 && p->bc[q] == 4))) return MHD_ERR_ARG;
   if (p->precision != MHD_PREC_FP64 && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
   if (p->cooling != MHD_COOL_EXACT && p->cooling != MHD_COOL_SURROGATE) return MHD_ERR_ARG;
   if (p->cooling == MHD_COOL_SURROGATE && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
@@ -147,6 +162,8 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   // species floors, MCF3DSGincfca3.f90:178-179 (slots H,p,H2,He,Hep,C,Cp,CO)
   double mins[8] = {p->rmin * kNdMinH, 1e-20, 1e-20, p->rmin * kNdMinHe, 1e-20, 1e-20, 1e-20, 1e-20};
   for (int s = 0; s < 8; s++) ph.ndmin[s] = mins[s];
+  ph.in.on[0] = p->bc[0] == 4;
+  ph.in.on[1] = p->bc[1] == 4;
 
   // full-grid arrays: 8 U + 8 species + 3 Bcc + 3 face velocities + 3 EMF + pnew
   const int narr = 8 + 8 + 3 + 3 + 3 + 1;
@@ -220,6 +237,7 @@ int mhd_destroy(mhd_handle *h) {
   cudaFree(h->block);
   cudaFree(h->coords);
   cudaFree(h->coordsf);
+  cudaFree(h->dtf);
   cudaFree(h->fblock);
   cudaFree(h->divv);
   cudaFree(h->diag_part);
@@ -250,6 +268,7 @@ int mhd_set_stream(mhd_handle *h, void *stream) {
 int mhd_upload(mhd_handle *h, const double *U, const double *species, const double *x, const double *dx,
                const double *y, const double *dy, const double *z, const double *dz) {
   if (!h || !U || !species || !x || !dx || !y || !dy || !z || !dz) return MHD_ERR_ARG;
+  TRY(need_inflow(h));
   CKR(cudaSetDevice(h->p.device));
   const Grid &g = h->g;
   size_t nb = (size_t)g.ncell * sizeof(double);
@@ -283,7 +302,7 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
   }
   // CC(4) as INITIA:470
   CK(cell_b(h->g, h->f, h->stream));
-  TRY(fill(h, {h->f.bcc[0], h->f.bcc[1], h->f.bcc[2]}, 7, 2));
+  TRY(fill(h, {h->f.bcc[0], h->f.bcc[1], h->f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
   CKR(cudaStreamSynchronize(h->stream));
   h->uploaded = true;
   return MHD_OK;
@@ -341,8 +360,10 @@ int mhd_source(mhd_handle *h, double dt) {
   if (h->p.ifthrm != 2) return MHD_OK;
   CKR(cudaSetDevice(h->p.device));
   // SOURCE :2481-2486 — rho, p and the species, one ghost layer, x y z
-  TRY(fill(h, {h->f.U[0], h->f.U[4]}, 7, 1));
-  TRY(fill(h, {h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]}, 7, 1, 1));
+  TRY(need_inflow(h));
+  TRY(fill(h, {h->f.U[0], h->f.U[4]}, 7, 1, 0, {IN_RHO, IN_P}));
+  TRY(fill(h, {h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]}, 7, 1, 1,
+           {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4}));
   if (h->p.precision == MHD_PREC_FP32) {
     if (h->p.cooling == MHD_COOL_SURROGATE && !h->sur_net)
       return fail(h, MHD_ERR_STATE, "surrogate cooling selected but no network loaded (mhd_surrogate_load)");
@@ -356,7 +377,7 @@ int mhd_source(mhd_handle *h, double dt) {
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
     CK(source_fp32(a, h->stream));
-    TRY(fill(h, {h->pnew}, 7, 1));
+    TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
     CK(source_fp32(a, h->stream));
@@ -367,7 +388,7 @@ int mhd_source(mhd_handle *h, double dt) {
   a.dt = dt; a.err = h->err; a.imc_count = h->dtred + 2; a.skip = nullptr;
   a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
   CK(source_pass(a, h->stream));
-  TRY(fill(h, {h->pnew}, 7, 1));   // :2526-2528
+  TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));   // :2526-2528
   a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
   CK(source_pass(a, h->stream));
   return MHD_OK;
@@ -376,6 +397,7 @@ int mhd_source(mhd_handle *h, double dt) {
 int mhd_sweep(mhd_handle *h, int dir, double dt) {
   if (!h || dir < 0 || dir > 2) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
+  TRY(need_inflow(h));
   CKR(cudaSetDevice(h->p.device));
   SweepArgs a{};
   a.g = h->g; a.ph = h->ph; a.f = h->f; a.dt = dt; a.err = h->err;
@@ -390,18 +412,19 @@ int mhd_ct(mhd_handle *h, double dt) {
   CKR(cudaSetDevice(h->p.device));
   Fields &f = h->f;
   // CC(1) :2122-2137
-  TRY(fill(h, {f.U[1], f.U[6], f.U[7]}, 1, 2));
+  TRY(need_inflow(h));
+  TRY(fill(h, {f.U[1], f.U[6], f.U[7]}, 1, 2, 0, {IN_V1, IN_B2, IN_B3}));
   TRY(fill(h, {f.U[2], f.U[5], f.U[7]}, 2, 2));
   TRY(fill(h, {f.U[3], f.U[5], f.U[6]}, 4, 2));
   const bool fp32 = h->p.precision == MHD_PREC_FP32;
   if (fp32) CK(face_velocity_fp32(h->g, f, h->vf[0], h->vf[1], h->vf[2], h->stream));
   else CK(face_velocity(h->g, f, h->vf[0], h->vf[1], h->vf[2], h->stream));
-  TRY(fill(h, {h->vf[1], h->vf[2]}, 1, 2));
+  TRY(fill(h, {h->vf[1], h->vf[2]}, 1, 2, 0, {IN_VFC, IN_VFC}));
   TRY(fill(h, {h->vf[0], h->vf[2]}, 2, 2));
   TRY(fill(h, {h->vf[0], h->vf[1]}, 4, 2));
-  TRY(fill(h, {f.U[4]}, 7, 2));
+  TRY(fill(h, {f.U[4]}, 7, 2, 0, {IN_P}));
   // CC(2) for Ez :2142
-  TRY(fill(h, {f.U[0]}, 7, 2));
+  TRY(fill(h, {f.U[0]}, 7, 2, 0, {IN_RHO}));
   if (fp32) {
     CT32Args a{};
     a.g = h->g;
@@ -419,7 +442,7 @@ int mhd_ct(mhd_handle *h, double dt) {
     CK(face_b(h->g, f, h->emf[0], h->emf[1], h->emf[2], dt, h->stream));   // CC(3)
   }
   CK(cell_b(h->g, f, h->stream));   // CC(4)
-  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2));
+  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
   return MHD_OK;
 }
 
@@ -427,7 +450,8 @@ int mhd_dissip(mhd_handle *h) {
   if (!h) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
-  TRY(fill(h, {h->f.U[1], h->f.U[2], h->f.U[3]}, 7, 2));
+  TRY(need_inflow(h));
+  TRY(fill(h, {h->f.U[1], h->f.U[2], h->f.U[3]}, 7, 2, 0, {IN_V1, IN_V2, IN_V3}));
   CK(divv(h->g, h->f, h->divv, h->stream));
   CK(dissip(h->g, h->f, h->divv, 0, h->stream));
   CK(dissip(h->g, h->f, h->divv, 1, h->stream));
@@ -477,6 +501,33 @@ int mhd_evolve(mhd_handle *h, int nsteps, double tsave, int *steps_done) {
     }
   }
   if (steps_done) *steps_done = n;
+  return MHD_OK;
+}
+
+int mhd_set_inflow(mhd_handle *h, const mhd_inflow *in, const float *reservoir, double uniform_density) {
+  if (!h || !in) return MHD_ERR_ARG;
+  if (h->p.bc[0] != 4 && h->p.bc[1] != 4) return fail(h, MHD_ERR_ARG, "no x side has BC code 4");
+  if (!reservoir && !(uniform_density > 0.0)) return fail(h, MHD_ERR_ARG, "reservoir density must be positive");
+  CKR(cudaSetDevice(h->p.device));
+  const Grid &g = h->g;
+  if (!h->dtf) CKR(cudaMalloc(&h->dtf, (size_t)g.ncell * sizeof(float)));
+  if (reservoir) {
+    CKR(cudaMemcpyAsync(h->dtf, reservoir, (size_t)g.ncell * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  } else {
+    std::vector<float> u((size_t)g.ncell, (float)uniform_density);
+    CKR(cudaMemcpyAsync(h->dtf, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CKR(cudaStreamSynchronize(h->stream));
+  }
+  CKR(cudaStreamSynchronize(h->stream));
+  InflowDev &d = h->ph.in;
+  d.rho_ref = in->rho_ref;
+  for (int sd = 0; sd < 2; sd++) {
+    d.p[sd] = in->p[sd];
+    for (int c = 0; c < 3; c++) { d.v[sd][c] = in->v[sd][c]; d.b[sd][c] = in->b[sd][c]; }
+  }
+  for (int q = 0; q < 8; q++) d.cm[q] = in->species[q];
+  d.dtf = h->dtf;
+  h->inflow_set = true;
   return MHD_OK;
 }
 

@@ -41,10 +41,43 @@ struct Grid {
   const float *dxf[3];      // dx(i) in FP32 (chosen form)
 };
 
+// BC=4 inflow in x (BC_MPI :814-890, BC_MPI_OT :948-1080, INITIA
+// :182-200): the values a ghost cell on an inflow side receives.  Side 0 is
+// x = 0, side 1 the far end; an inflow side has no periodic neighbour.
+struct InflowDev {
+  int on[2];               // BC=4 on the left / right side of x
+  double rho_ref;          // BBRV(1,*,*)
+  double v[2][3];          // BBRV(2..4,1,side)
+  double p[2];             // BBRV(5,1,side)
+  double b[2][3];          // BBRV(6..8,1,side)
+  double cm[8];            // BBRV_cm, species order H,p,H2,He,He+,C,C+,CO
+  const float *dtf;        // DTF reservoir, REAL*4, padded layout of U
+  double time;             // time of the step (the reference's module time)
+};
+
 struct Phys {
   double facdep, pmin, pmax, rmin, kb, kcond, cfl, tfinal;
   int ifthrm;
   double ndmin[8];
+  InflowDev in;
+};
+
+// what a ghost cell on an inflow side receives at one exchange (the
+// reference's rule for that field and exchange mode); IN_KEEP leaves it
+enum : int {
+  IN_KEEP = 0,
+  IN_RHO,               // the DTF reservoir advected at the inflow speed (:818-826, :855-862)
+  IN_V1, IN_V2, IN_V3,  // inflow velocity components (primitive exchanges)
+  IN_M1,                // rho(ghost) vx_in (conserved exchange, :839-843)
+  IN_M2, IN_M3,         // rho_ref vy_in, rho_ref vz_in
+  IN_P,                 // inflow pressure
+  IN_E,                 // 1.5 p_in + 0.5 (rho vx_in^2 + Bcc1^2 + Blg1^2 + Blg2^2) (:833-837)
+  IN_BXF,               // face Bx: ghost faces copy face 1, or face n+1 into n+2 (:827-831)
+  IN_B2, IN_B3,         // inflow By, Bz (U7, U8, Bcc 2-3, Blg)
+  IN_DXLAG,             // dxlagM = dx(0) or dx(n+1) (:951-962)
+  IN_BCC1,              // Bcc x copies cell 1 or cell n (:971-988)
+  IN_VFC,               // Vfc copies cell 1 or cell n (:1018-1036)
+  IN_SPEC,              // + s: BBRV_cm(s) rho(ghost), interior y,z rows only (:1052-1080)
 };
 
 struct Fields {
@@ -55,6 +88,59 @@ struct Fields {
 
 __host__ __device__ inline long long gidx(const Grid &g, int i, int j, int k) {
   return (long long)(i + 1) + g.st[1] * (long long)(j + 1) + g.st[2] * (long long)(k + 1);
+}
+
+// density of inflow ghost cell gi of row (j,k): DTF at the upstream position
+// x - time vx_in, wrapped into the box (BC_MPI :821-825, :857-861).  The
+// operation order is the reference's; the index is clamped into the padded
+// reservoir (DTF(-1..n+2)).
+__device__ __forceinline__ double inflow_rho(const Grid &g, const InflowDev &in, int side, int gi, int j, int k) {
+  const double *xe = g.x[0], *dxe = g.dx[0];   // x(i) at xe[i+1], dx(i) at dxe[i+1]
+  const double dx0 = dxe[1];
+  const double L = dx0 * g.n[0] * 1;            // dx(0)*Ncellx*NSPLTx
+  double xp;
+  if (side == 0) {
+    xp = xe[1] - 0.5 * dx0 + gi * dx0 - in.time * in.v[0][0];
+    int nn = (int)(fabs(xp) / L) + 1;
+    xp = xp + L * nn;
+  } else {
+    xp = 0.5 * (xe[gi] + xe[gi + 1]) - in.time * in.v[1][0];
+    int nn = (int)(fabs(xp) / L);
+    xp = xp - L * nn;
+  }
+  int II = (int)(xp / dx0) + 1;
+  II = II < -1 ? -1 : (II > g.n[0] + 2 ? g.n[0] + 2 : II);
+  return (double)in.dtf[gidx(g, II, j, k)];
+}
+
+// the value of rule r for inflow ghost cell gi of row (j,k); bccx is Bcc_x
+// at that cell (IN_E), self1 / selfn the array's own cell-1 / cell-n (or
+// face n+1) value for the copy rules
+__device__ __forceinline__ double inflow_value(const Grid &g, const InflowDev &in, int r, int side, int gi, int j,
+                                               int k, double bccx, double self1, double selfn) {
+  const double *v = in.v[side];
+  switch (r) {
+    case IN_RHO: return inflow_rho(g, in, side, gi, j, k);
+    case IN_V1: return v[0];
+    case IN_V2: return v[1];
+    case IN_V3: return v[2];
+    case IN_M1: return inflow_rho(g, in, side, gi, j, k) * v[0];
+    case IN_M2: return in.rho_ref * v[1];
+    case IN_M3: return in.rho_ref * v[2];
+    case IN_P: return in.p[side];
+    case IN_E: {
+      const double rho = inflow_rho(g, in, side, gi, j, k);
+      const double b1 = in.b[side][1], b2 = in.b[side][2];
+      return in.p[side] * 1.5 + 0.5 * (rho * (v[0] * v[0]) + bccx * bccx + b1 * b1 + b2 * b2);
+    }
+    case IN_B2: return in.b[side][1];
+    case IN_B3: return in.b[side][2];
+    case IN_DXLAG: return side == 0 ? g.dx[0][1] : g.dx[0][g.n[0] + 2];
+    case IN_BXF:
+    case IN_BCC1:
+    case IN_VFC: return side == 0 ? self1 : selfn;
+    default: return in.cm[r - IN_SPEC] * inflow_rho(g, in, side, gi, j, k);
+  }
 }
 
 // ---------------------------------------------------------------- scalars
@@ -198,6 +284,8 @@ __device__ __forceinline__ void flag(int *err, int bit) { atomicOr(err, bit); }
 struct FillArgs {
   double *f[8];
   int nf;
+  int rule[8];          // BC=4 rule per array (IN_KEEP where x has no inflow rule)
+  InflowDev in;
 };
 
 #ifdef MHD_COMMON_KERNELS
@@ -221,10 +309,23 @@ __global__ void ghost_fill_kernel(Grid g, FillArgs a, int d, int nol, int specie
   bool fl = g.bcl[d] == 1 && (!species || tr_in);
   bool fr = g.bcr[d] == 1 && (!species || tr_in);
   // position i lives at base + (i+1)*sd
-  for (int q = 1 - nol; q <= 0; q++) F[base + (q + 1) * sd] = F[base + (q + N + 1) * sd];
-  if (fl) for (int q = 1 - nol; q <= 0; q++) F[base + (q + 1) * sd] = F[base + 2 * sd];
-  for (int q = N + 1; q <= N + nol; q++) F[base + (q + 1) * sd] = F[base + (q - N + 1) * sd];
-  if (fr) for (int q = N + 1; q <= N + nol; q++) F[base + (q + 1) * sd] = F[base + (N + 1) * sd];
+  const bool inL = d == 0 && a.in.on[0], inR = d == 0 && a.in.on[1];
+  const int rule = a.rule[fi];
+  if (!inL) {
+    for (int q = 1 - nol; q <= 0; q++) F[base + (q + 1) * sd] = F[base + (q + N + 1) * sd];
+    if (fl) for (int q = 1 - nol; q <= 0; q++) F[base + (q + 1) * sd] = F[base + 2 * sd];
+  } else if (rule != IN_KEEP && (!species || tr_in)) {
+    // BC=4: no neighbour on this side; the inflow value of the field
+    for (int q = 1 - nol; q <= 0; q++)
+      F[base + (q + 1) * sd] = inflow_value(g, a.in, rule, 0, q, q1, q2, 0.0, F[base + 2 * sd], F[base + (N + 1) * sd]);
+  }
+  if (!inR) {
+    for (int q = N + 1; q <= N + nol; q++) F[base + (q + 1) * sd] = F[base + (q - N + 1) * sd];
+    if (fr) for (int q = N + 1; q <= N + nol; q++) F[base + (q + 1) * sd] = F[base + (N + 1) * sd];
+  } else if (rule != IN_KEEP && (!species || tr_in)) {
+    for (int q = N + 1; q <= N + nol; q++)
+      F[base + (q + 1) * sd] = inflow_value(g, a.in, rule, 1, q, q1, q2, 0.0, F[base + 2 * sd], F[base + (N + 1) * sd]);
+  }
 }
 
 #endif  // MHD_COMMON_KERNELS
@@ -295,13 +396,28 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
   auto B = [&](int b, int i, int p) -> double & { return sm[b * LP + (i + 1) * P + p]; };
   auto VB = [](int c) { return B_V0 + c; };   // velocity buffer of component c
   const bool perL = g.bcl[DIR] != 1, perR = g.bcr[DIR] != 1;
-  // in-pencil ghost fill of buffers [b0, b1) (periodic wrap or free copy)
-  auto fill = [&](const int *bl, int nb) {
+  // BC=4 inflow sides of the x sweep (the other sweeps never exchange in x)
+  const bool inL = DIR == 0 && A.ph.in.on[0], inR = DIR == 0 && A.ph.in.on[1];
+  // in-pencil ghost fill of the listed buffers: periodic wrap or free copy,
+  // or on an inflow side the reference's BC=4 value of that buffer's field
+  auto fill = [&](const int *bl, const int *rules, int nb) {
     for (int t = tid; t < 4 * P * nb; t += nth) {
-      int b = bl[t / (4 * P)];
+      int bq = t / (4 * P);
+      int b = bl[bq];
       int r = t % (4 * P);
       int q = r / P, p = r % P;
       int i = (q < 2) ? (q - 1) : (N + q - 1);   // -1, 0, N+1, N+2
+      const int side = i <= 0 ? 0 : 1;
+      if (side == 0 ? inL : inR) {
+        const int rule = rules[bq];
+        if (rule == IN_KEEP || (rule == IN_BXF && i == N + 1)) continue;
+        // DIR == 0 here: pencil p is row (j, k) = (blockIdx.x*P+p+1, blockIdx.y+1)
+        const double bccx = (rule == IN_E) ? A.f.bcc[0][pc.at(p, i)] : 0.0;
+        // the face copy reads face 1 or face n+1, which this fill never writes
+        const double f1 = (rule == IN_BXF) ? B(b, 1, p) : 0.0, fn = (rule == IN_BXF) ? B(b, N + 1, p) : 0.0;
+        B(b, i, p) = inflow_value(g, A.ph.in, rule, side, i, blockIdx.x * P + p + 1, blockIdx.y + 1, bccx, f1, fn);
+        continue;
+      }
       int src;
       if (i <= 0) src = perL ? i + N : 1;
       else src = perR ? i - N : N;
@@ -331,7 +447,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
   {
     // E1 (RHS :1355,:1357): rho, vn, p, species; E2 (:1960): vt1, vt2
     const int bl[10] = {B_RHO, B_V0, B_V1, B_V2, B_E, B_S0, B_S1, B_S2, B_S3, B_S4};
-    fill(bl, 10);
+    const int rl[10] = {IN_RHO, IN_V1, IN_V2, IN_V3, IN_P, IN_SPEC, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4};
+    fill(bl, rl, 10);
   }
   __syncthreads();
 
@@ -426,12 +543,15 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
     int i = 1 + t / P, p = t % P;
     B(B_PA, i, p) = B(B_XL, i, p) - B(B_XL, i - 1, p);
     B(B_S0, i, p) = A.f.U[5 + DIR][pc.at(p, i)];
+    // an inflow side's exchange leaves face n+1 as it is (:862-866)
+    if (inR && i == N) B(B_S0, N + 1, p) = A.f.U[5 + DIR][pc.at(p, N + 1)];
   }
   __syncthreads();
   {
     // E2 rho (:1960), E3 dxlagM + Blg (:1974), and the face-normal B
     const int bl[5] = {B_RHO, B_PA, B_T1, B_T2, B_S0};
-    fill(bl, 5);
+    const int rl[5] = {IN_RHO, IN_DXLAG, IN_B2, IN_B3, IN_BXF};
+    fill(bl, rl, 5);
   }
   __syncthreads();
   // the reference's exchange of the face field also rewrites its ghost
@@ -537,7 +657,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
   {
     // E4 (:1572, :1581): Blg and U(1..5) in conserved form
     const int bl[7] = {B_RHO, B_V0, B_V1, B_V2, B_E, B_T1, B_T2};
-    fill(bl, 7);
+    const int rl[7] = {IN_RHO, IN_M1, IN_M2, IN_M3, IN_E, IN_B2, IN_B3};
+    fill(bl, rl, 7);
   }
   __syncthreads();
   // T switch of every limiter in REMAP, from the state before remapping
@@ -585,7 +706,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs A) {
     }
     __syncthreads();
     const int bl[1] = {b};
-    fill(bl, 1);
+    const int rl[1] = {IN_SPEC + s};
+    fill(bl, rl, 1);
     __syncthreads();
     remap_column(b);
     const double mn = A.ph.ndmin[s];

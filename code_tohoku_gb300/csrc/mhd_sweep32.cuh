@@ -61,7 +61,10 @@ enum {
   F_SW,      // remap T switch (+-0.5) of cells 0..n+1
   F_COUNT
 };
-enum { C_DX = 0, C_RDX, C_X2, C_COUNT };   // FP32 dx(i), 1/(x(i)-x(i-1)), x(i+1)-x(i-1)
+enum { C_DX = 0, C_RDX, C_X2, C_COUNT };
+// inflow rules of this kernel's derived buffers (beside the IN_* of the
+// shared header): the species sum H+p+He+He+ and the remap's T switch
+enum : int { IN_SSUM = 100, IN_SW = 101 };   // FP32 dx(i), 1/(x(i)-x(i-1)), x(i+1)-x(i-1)
 
 __host__ __device__ inline size_t sweep32_smem_bytes(int n, int P) {
   size_t L = (size_t)n + 4;
@@ -143,16 +146,55 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   auto Fb = [&](int b, int i, int p) -> float & { return smf[b * LP + (i + 1) * P + p]; };
   auto cx = [&](int c, int i) -> float { return cf[c * L + i + 1]; };
   const bool perL = g.bcl[DIR] != 1, perR = g.bcr[DIR] != 1;
+  // BC=4 inflow sides of the x sweep (the other sweeps never exchange in x)
+  const bool inL = DIR == 0 && A.ph.in.on[0], inR = DIR == 0 && A.ph.in.on[1];
   // ghost positions whose value is a copy of interior cell i
   auto for_ghosts = [&](int i, auto &&fn) {
-    if (perL ? i == N - 1 : i == 1) fn(-1);
-    if (perL ? i == N : i == 1) fn(0);
-    if (perR ? i == 1 : i == N) fn(N + 1);
-    if (perR ? i == 2 : i == N) fn(N + 2);
+    if (!inL && (perL ? i == N - 1 : i == 1)) fn(-1);
+    if (!inL && (perL ? i == N : i == 1)) fn(0);
+    if (!inR && (perR ? i == 1 : i == N)) fn(N + 1);
+    if (!inR && (perR ? i == 2 : i == N)) fn(N + 2);
   };
-  auto put = [&](int b, int i, int p, float v) {
-    Fb(b, i, p) = v;
+  // value of an inflow ghost cell gi of pencil p under rule r (DIR == 0:
+  // pencil p is row (blockIdx.x*P+p+1, blockIdx.y+1)); two rules of this
+  // kernel's derived buffers: the species sum of gamma and the remap switch
+  auto inflow32 = [&](int r, int side, int gi, int p) -> float {
+    const int j = blockIdx.x * P + p + 1, k = blockIdx.y + 1;
+    if (r == IN_SSUM) {
+      const double rho = inflow_rho(g, A.ph.in, side, gi, j, k);
+      const double *cm = A.ph.in.cm;
+      return d2f(cm[0] * rho) + d2f(cm[1] * rho) + d2f(cm[3] * rho) + d2f(cm[4] * rho);
+    }
+    const double bccx = (r == IN_E || r == IN_SW) ? __ldg(A.f.bcc[0] + pc.at(p, gi)) : 0.0;
+    if (r == IN_SW) {
+      const float e = d2f(inflow_value(g, A.ph.in, IN_E, side, gi, j, k, bccx, 0.0, 0.0));
+      const float rho = d2f(inflow_rho(g, A.ph.in, side, gi, j, k));
+      return (1.27f * e >= 3.0f * kb * rho) ? 0.5f : -0.5f;
+    }
+    return d2f(inflow_value(g, A.ph.in, r, side, gi, j, k, bccx, 0.0, 0.0));
+  };
+  // the ghosts cell i feeds (copies); on an inflow side only the face copy
+  // of face 1 is fed here, the other rules by inflow_fill
+  auto put_ghosts = [&](int b, int i, int p, float v, int rule) {
     for_ghosts(i, [&](int gi) { Fb(b, gi, p) = v; });
+    if (rule == IN_BXF && inL && i == 1) {
+      Fb(b, -1, p) = v;
+      Fb(b, 0, p) = v;
+    }
+  };
+  auto put = [&](int b, int i, int p, float v, int rule) {
+    Fb(b, i, p) = v;
+    put_ghosts(b, i, p, v, rule);
+  };
+  // the inflow ghosts of listed buffers (values that depend on no interior
+  // cell); run by the phase that writes those buffers, before its barrier
+  auto inflow_fill = [&](const int *bl, const int *rl, int nb) {
+    for (int t = tid; t < 4 * P * nb; t += NT) {
+      const int bq = t / (4 * P), r = t % (4 * P), q = r / P, p = r % P;
+      const int gi = (q < 2) ? (q - 1) : (N + q - 1);
+      const int side = gi <= 0 ? 0 : 1;
+      if (side == 0 ? inL : inR) Fb(bl[bq], gi, p) = inflow32(rl[bq], side, gi, p);
+    }
   };
   auto vl = [&](int b, int i, int p, float dm, float d0, float dp, float s) {
     return vlim_sel(Fb(b, i - 1, p), Fb(b, i, p), Fb(b, i + 1, p), dm, d0, dp, s);
@@ -184,25 +226,39 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     long long a = pc.at(p, i);
     double u0 = __ldg(A.f.U[0] + a), un = __ldg(A.f.U[1 + DIR] + a), u1 = __ldg(A.f.U[1 + C1] + a),
            u2 = __ldg(A.f.U[1 + C2] + a), u4 = __ldg(A.f.U[4] + a);
-    put(F_R, i, p, d2f(u0));
-    put(F_VN, i, p, d2f(un));
-    put(F_VT1, i, p, d2f(u1));
-    put(F_VT2, i, p, d2f(u2));
+    put(F_R, i, p, d2f(u0), IN_RHO);
+    put(F_VN, i, p, d2f(un), IN_V1);
+    put(F_VT1, i, p, d2f(u1), IN_V2);
+    put(F_VT2, i, p, d2f(u2), IN_V3);
     float pr = d2f(u4);
-    put(F_P, i, p, pr);
-    for_ghosts(i, [&](int gi) { Fb(F_T, gi, p) = pr; });
+    put(F_P, i, p, pr, IN_P);
+    put_ghosts(F_T, i, p, pr, IN_P);
   });
   unrolled<NT, 4>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
     long long a = pc.at(p, i);
     double s0 = __ldg(A.f.sp[0] + a), s1 = __ldg(A.f.sp[1] + a), s2 = __ldg(A.f.sp[2] + a),
            s3 = __ldg(A.f.sp[3] + a), s4 = __ldg(A.f.sp[4] + a), bn = __ldg(A.f.U[5 + DIR] + a);
-    put(F_S, i, p, d2f(s0) + d2f(s1) + d2f(s3) + d2f(s4));
-    put(F_H2, i, p, d2f(s2));
-    // the face-field exchange rewrites the ghost faces (incl. face n+1)
-    put(F_BN, i, p, d2f(bn));
+    put(F_S, i, p, d2f(s0) + d2f(s1) + d2f(s3) + d2f(s4), IN_SSUM);
+    put(F_H2, i, p, d2f(s2), IN_SPEC + 2);
+    // the face-field exchange rewrites the ghost faces (incl. face n+1; an
+    // inflow side copies face 1 into faces -1, 0 and face n+1 into n+2)
+    put(F_BN, i, p, d2f(bn), IN_BXF);
     if (pc.active(p)) for_ghosts(i, [&](int gi) { A.f.U[5 + DIR][pc.at(p, gi)] = bn; });
+    if (inL && i == 1)
+      for (int gi = -1; gi <= 0; gi++) A.f.U[5 + DIR][pc.at(p, gi)] = bn;
+    if (inR && i == N) {
+      const double bn1 = __ldg(A.f.U[5 + DIR] + pc.at(p, N + 1));
+      Fb(F_BN, N + 1, p) = d2f(bn1);
+      Fb(F_BN, N + 2, p) = d2f(bn1);
+      A.f.U[5 + DIR][pc.at(p, N + 2)] = bn1;
+    }
   });
+  if (inL || inR) {
+    const int bl[8] = {F_R, F_VN, F_VT1, F_VT2, F_P, F_T, F_S, F_H2};
+    const int rl[8] = {IN_RHO, IN_V1, IN_V2, IN_V3, IN_P, IN_P, IN_SSUM, IN_SPEC + 2};
+    inflow_fill(bl, rl, 8);
+  }
   __syncthreads();
   // ------------------------------------------------ B: gamma, RHS slopes
   unrolled<NT, kSmemUnroll>((N + 2) * P, [&](int t) {
@@ -263,11 +319,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     Fb(F_IMN, i, p) = -dt * (Pa1 - Pa0);
     float inv = fdiv(1.0f, dxl);
     Fb(F_T, i, p) = fdiv(EL, dm);   // e after RHS: MOC's T switch inside
-    put(F_DXL, i, p, dxl);
-    put(F_R, i, p, dm * inv);
-    put(F_B1, i, p, b1 * dx0 * inv);
-    put(F_B2, i, p, b2 * dx0 * inv);
+    put(F_DXL, i, p, dxl, IN_DXLAG);
+    put(F_R, i, p, dm * inv, IN_RHO);
+    put(F_B1, i, p, b1 * dx0 * inv, IN_B2);
+    put(F_B2, i, p, b2 * dx0 * inv, IN_B3);
   });
+  if (inL || inR) {
+    const int bl[4] = {F_DXL, F_R, F_B1, F_B2};
+    const int rl[4] = {IN_DXLAG, IN_RHO, IN_B2, IN_B3};
+    inflow_fill(bl, rl, 4);
+  }
   __syncthreads();
   // ------------------------------------------------ E: MOC slopes
   unrolled<NT, kSmemUnroll>((N + 2) * P, [&](int t) {
@@ -333,14 +394,19 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     float EL = Fb(F_T, i, p) * dm + dt * ((0.5f * Bnap * Vnap + Bay1 * Vay1 + Baz1 * Vaz1) * Bnap -
                                           (0.5f * Bnam * Vnam + Bay0 * Vay0 + Baz0 * Vaz0) * Bnam);
     const float qE = EL * inv;
-    put(F_T, i, p, qE);
-    put(F_SW, i, p, tsw(qE, rl));   // the remap's T switch, from E and rho
-    put(F_B1, i, p, Fb(F_B1, i, p) + dt * (Bnap * Vay1 - Bnam * Vay0) * inv);
-    put(F_B2, i, p, Fb(F_B2, i, p) + dt * (Bnap * Vaz1 - Bnam * Vaz0) * inv);
-    put(F_VN, i, p, Fb(F_VN, i, p) * rl + imn * inv);
-    put(F_VT1, i, p, Fb(F_VT1, i, p) * rl + im1 * inv);
-    put(F_VT2, i, p, Fb(F_VT2, i, p) * rl + im2 * inv);
+    put(F_T, i, p, qE, IN_E);
+    put(F_SW, i, p, tsw(qE, rl), IN_SW);   // the remap's T switch, from E and rho
+    put(F_B1, i, p, Fb(F_B1, i, p) + dt * (Bnap * Vay1 - Bnam * Vay0) * inv, IN_B2);
+    put(F_B2, i, p, Fb(F_B2, i, p) + dt * (Bnap * Vaz1 - Bnam * Vaz0) * inv, IN_B3);
+    put(F_VN, i, p, Fb(F_VN, i, p) * rl + imn * inv, IN_M1);
+    put(F_VT1, i, p, Fb(F_VT1, i, p) * rl + im1 * inv, IN_M2);
+    put(F_VT2, i, p, Fb(F_VT2, i, p) * rl + im2 * inv, IN_M3);
   });
+  if (inL || inR) {
+    const int bl[7] = {F_T, F_SW, F_B1, F_B2, F_VN, F_VT1, F_VT2};
+    const int rl[7] = {IN_E, IN_SW, IN_B2, IN_B3, IN_M1, IN_M2, IN_M3};
+    inflow_fill(bl, rl, 7);
+  }
   __syncthreads();
   // ------------------------------------------------ H: field fluxes
   unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
@@ -395,11 +461,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     if (act && (!(vn == vn) || !(v1 == v1) || !(v2 == v2) || !(rf < 3e38f))) flag(A.err, ERRB_NONFINITE);
     // species 0..3: content n dx is unchanged by the Lagrangian step
     const float w = cx(C_DX, i) * fdiv(1.0f, dxl);
-    put(F_G0, i, p, d2f(__ldg(A.f.sp[0] + a)) * w);
-    put(F_G1, i, p, d2f(__ldg(A.f.sp[1] + a)) * w);
-    put(F_IMN, i, p, d2f(__ldg(A.f.sp[2] + a)) * w);
-    put(F_H2, i, p, d2f(__ldg(A.f.sp[3] + a)) * w);
+    put(F_G0, i, p, d2f(__ldg(A.f.sp[0] + a)) * w, IN_SPEC + 0);
+    put(F_G1, i, p, d2f(__ldg(A.f.sp[1] + a)) * w, IN_SPEC + 1);
+    put(F_IMN, i, p, d2f(__ldg(A.f.sp[2] + a)) * w, IN_SPEC + 2);
+    put(F_H2, i, p, d2f(__ldg(A.f.sp[3] + a)) * w, IN_SPEC + 3);
   });
+  if (inL || inR) {
+    const int bl[4] = {F_G0, F_G1, F_IMN, F_H2};
+    const int rl[4] = {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3};
+    inflow_fill(bl, rl, 4);
+  }
   __syncthreads();
   // ------------------------------------------------ J: species 0-3 fluxes
   unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
@@ -430,12 +501,17 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     float H2 = species_new(2, a, i, p, F_G4, act);
     Fb(F_S, i, p) = S;
     const float w = cx(C_DX, i) * fdiv(1.0f, Fb(F_DXL, i, p));
-    put(F_G0, i, p, d2f(__ldg(A.f.sp[4] + a)) * w);
-    put(F_G1, i, p, d2f(__ldg(A.f.sp[5] + a)) * w);
-    put(F_IMN, i, p, d2f(__ldg(A.f.sp[6] + a)) * w);
-    put(F_PA, i, p, d2f(__ldg(A.f.sp[7] + a)) * w);
+    put(F_G0, i, p, d2f(__ldg(A.f.sp[4] + a)) * w, IN_SPEC + 4);
+    put(F_G1, i, p, d2f(__ldg(A.f.sp[5] + a)) * w, IN_SPEC + 5);
+    put(F_IMN, i, p, d2f(__ldg(A.f.sp[6] + a)) * w, IN_SPEC + 6);
+    put(F_PA, i, p, d2f(__ldg(A.f.sp[7] + a)) * w, IN_SPEC + 7);
     Fb(F_H2, i, p) = H2;
   });
+  if (inL || inR) {
+    const int bl[4] = {F_G0, F_G1, F_IMN, F_PA};
+    const int rl[4] = {IN_SPEC + 4, IN_SPEC + 5, IN_SPEC + 6, IN_SPEC + 7};
+    inflow_fill(bl, rl, 4);
+  }
   __syncthreads();
   // ------------------------------------------------ L: species 4-7 fluxes
   unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {

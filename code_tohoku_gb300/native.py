@@ -24,7 +24,7 @@ COOL_EXACT, COOL_SURROGATE = 0, 1
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_timestep", "mhd_source",
            "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_evolve", "mhd_get_time",
-           "mhd_set_time", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
+           "mhd_set_time", "mhd_set_inflow", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
            "mhd_kernel_launches", "mhd_reset_counters", "mhd_surrogate_nparams", "mhd_surrogate_load",
            "mhd_surrogate_train", "mhd_surrogate_label", "mhd_surrogate_eval", "mhd_surrogate_grad",
            "mhd_timestep_noalloc")
@@ -67,6 +67,11 @@ def library_path():
     return _build.LIB
 
 
+class _Inflow(ctypes.Structure):
+    _fields_ = [("rho_ref", ctypes.c_double), ("v", (ctypes.c_double * 3) * 2), ("p", ctypes.c_double * 2),
+                ("b", (ctypes.c_double * 3) * 2), ("species", ctypes.c_double * 8)]
+
+
 def load(build_if_missing=True):
     """Load libmhd_gb300.so, compiling it first when it is missing or stale."""
     global _lib
@@ -97,6 +102,7 @@ def load(build_if_missing=True):
         "mhd_synchronize": [H],
         "mhd_set_stream": [H, ctypes.c_void_p],
         "mhd_last_error": [H, ctypes.c_char_p, ctypes.c_int],
+        "mhd_set_inflow": [H, ctypes.POINTER(_Inflow), ctypes.c_void_p, ctypes.c_double],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -277,6 +283,27 @@ class Mhd3D:
         n = ctypes.c_int()
         self._ck(self.L.mhd_evolve(self.h, nsteps, tsave, ctypes.byref(n)))
         return n.value
+
+    def set_inflow(self, inflow, reservoir=None, uniform_density=0.0):
+        """BC=4 data (problems.Inflow); reservoir: DTF as float32 of the padded
+        state shape, or None for a uniform reservoir.  Call before upload."""
+        c = _Inflow()
+        c.rho_ref = inflow.rho_ref
+        for s_ in range(2):
+            c.p[s_] = inflow.p[s_]
+            for q in range(3):
+                c.v[s_][q] = inflow.v[s_][q]
+                c.b[s_][q] = inflow.b[s_][q]
+        for q in range(8):
+            c.species[q] = inflow.species[q]
+        if reservoir is None:
+            self._ck(self.L.mhd_set_inflow(self.h, ctypes.byref(c), None, float(uniform_density)))
+        else:
+            r = np.ascontiguousarray(reservoir, dtype=np.float32)
+            if r.shape != self.shape:
+                raise ValueError(f"reservoir shape {r.shape}, expected {self.shape}")
+            self._ck(self.L.mhd_set_inflow(self.h, ctypes.byref(c), r.ctypes.data_as(ctypes.c_void_p),
+                                           float(uniform_density)))
 
     def set_time(self, time, ifevo=1):
         self._ck(self.L.mhd_set_time(self.h, time, ifevo))

@@ -61,7 +61,8 @@ typedef struct mhd_params {
   int nx, ny, nz;              /* interior cells (Ncellx, Ncelly, Ncellz)   */
   double cfl, facdep, tfinal;  /* INPUT3D.DAT rows 13-14                    */
   int bc[6];                   /* BCx1,BCx2,BCy1,BCy2,BCz1,BCz2: 1 = free
-                                  (zero-gradient), 3 = periodic              */
+                                  (zero-gradient), 3 = periodic, 4 = inflow
+                                  (x sides only; see mhd_set_inflow)         */
   double pmin, pmax, rmin;     /* floors, MCF3DSGincfca3.f90:173-176        */
   double kb, kcond;            /* 8.63359, 1.6384e-2                        */
   int ifthrm;                  /* 2: KI source and thermal dt limit; 0: off */
@@ -70,6 +71,19 @@ typedef struct mhd_params {
   int cooling;                 /* MHD_COOL_EXACT or MHD_COOL_SURROGATE      */
   int device;                  /* CUDA device ordinal                       */
 } mhd_params;
+
+/* Inflow boundary data (BC code 4 on an x side): the values a ghost cell on
+ * that side receives at each exchange, as INITIA sets them up
+ * (MCF3DSGincfca3.f90:182-200) and BC_MPI / BC_MPI_OT apply them
+ * (:814-890, :948-1080).  Side 0 is x = 0, side 1 the far end. */
+typedef struct mhd_inflow {
+  double rho_ref;        /* BBRV(1,*,*): the reference density dBC        */
+  double v[2][3];        /* inflow velocity per side, BBRV(2..4,1,side)   */
+  double p[2];           /* inflow pressure, BBRV(5,1,side)               */
+  double b[2][3];        /* inflow field, BBRV(6..8,1,side)               */
+  double species[8];     /* BBRV_cm: number density per unit mass density,
+                            order H, p, H2, He, He+, C, C+, CO            */
+} mhd_inflow;
 
 typedef struct mhd_diag {
   double mass, momentum[3], energy;   /* sums over interior cells × volume  */
@@ -110,6 +124,15 @@ int mhd_advance(mhd_handle *h, double dt);
 int mhd_step(mhd_handle *h, double tsave, double *dt, int *st);
 /* nsteps iterations of mhd_step; stops early at tfinal or tsave. */
 int mhd_evolve(mhd_handle *h, int nsteps, double tsave, int *steps_done);
+
+/* Inflow data for a handle with BC code 4 on an x side; required before
+ * mhd_upload on such a handle.  reservoir: the DTF density field (REAL*4,
+ * the padded layout of U, DTF(-1..nx+2,-1..ny+2,-1..nz+2), read by the
+ * reference from D###.dat at :402-417), advected across the inflow ghosts
+ * at the inflow speed; NULL gives a uniform reservoir of density
+ * uniform_density (the shipped code's DTF = dinit1).  Replaces the BBRV /
+ * BBRV_cm / DTF set-up of INITIA :182-200, :402-432. */
+int mhd_set_inflow(mhd_handle *h, const mhd_inflow *in, const float *reservoir, double uniform_density);
 
 int mhd_get_time(mhd_handle *h, double *time, int *ifevo);
 int mhd_set_time(mhd_handle *h, double time, int ifevo);

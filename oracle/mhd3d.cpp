@@ -34,10 +34,38 @@ using detmath::fsign;
 // species slots, in the order of the reference's VLIMIT_OT / REMAP G(:,1..8)
 enum { SH = 0, SP = 1, SH2 = 2, SHE = 3, SHEP = 4, SC = 5, SCP = 6, SCO = 7 };
 
+// BC=4 inflow in x (BC_MPI :814-890, BC_MPI_OT :948-1080): what a ghost
+// cell on an inflow side receives at one exchange.  The inflow side has no
+// periodic neighbour (INITIA :467-468 sets LEFT/RIGT to MPI_PROC_NULL), so a
+// field without a rule keeps its ghost value.
+enum Inflow : int {
+  IN_KEEP = 0,
+  IN_RHO,               // the DTF reservoir advected at the inflow speed (:818-826, :855-862)
+  IN_V1, IN_V2, IN_V3,  // BBRV(2..4,1,side): inflow velocity (primitive exchanges)
+  IN_M1,                // U1(ghost) * vx_in (conserved exchange, :839-843)
+  IN_M2, IN_M3,         // BBRV(3..4,2,side) = rho_ref * vy_in, rho_ref * vz_in
+  IN_P,                 // BBRV(5,1,side)
+  IN_E,                 // 1.5 p_in + 0.5 (U1 vx_in^2 + Bcc1^2 + Blg1^2 + Blg2^2) (:833-837)
+  IN_BXF,               // face Bx: ghost faces copy face 1, or face n+1 into n+2 (:827-831)
+  IN_B2, IN_B3,         // BBRV(7..8,*,side): inflow By, Bz (also Bcc 2,3 and Blg)
+  IN_DXLAG,             // dxlagM = dx(0) or dx(n+1) (:951-962)
+  IN_BCC1,              // Bcc x copies cell 1 or cell n (:971-988)
+  IN_VFC,               // Vfc copies cell 1 or cell n (:1018-1036)
+  IN_SPEC,              // + s: BBRV_cm(s) * U1(ghost), interior y,z only (:1052-1080)
+};
+
+struct InflowBC {
+  double rho_ref;          // BBRV(1,*,*)
+  double v[2][3];          // side 0 = left (x = 0), 1 = right: BBRV(2..4,1,side)
+  double p[2];             // BBRV(5,1,side)
+  double b[2][3];          // BBRV(6..8,1,side)
+  double cm[8];            // BBRV_cm in the species slot order below
+};
+
 struct Params {
   int nx, ny, nz;
   double CFL, facdep, tfinal;
-  int bc[6];          // BCx1,BCx2,BCy1,BCy2,BCz1,BCz2: 1 = free, otherwise periodic
+  int bc[6];          // BCx1,BCx2,BCy1,BCy2,BCz1,BCz2: 1 = free, 4 = inflow (x only), otherwise periodic
   double pmin, pmax, rmin;
   double kb, Kcond;
   int ifthrm;         // 2: KI source + thermal dt limit; 0: neither
@@ -57,6 +85,8 @@ struct Mhd3D {
   std::vector<double> Bcc[4], Blg[3], Vfc[4], EMF[4];
   std::vector<double> dnc, xlag, dxlagM;
   double ndmin[8];
+  InflowBC in{};
+  std::vector<float> dtf;   // DTF(-1..nx+2, -1..ny+2, -1..nz+2), REAL*4 like the reference
 
   size_t id(int i, int j, int k) const {
     return (size_t)(i + 1) + (size_t)sx * ((size_t)(j + 1) + (size_t)sy * (size_t)(k + 1));
@@ -89,9 +119,55 @@ struct Mhd3D {
   // included, like the MPI_TYPE_VECTOR strides (:812, :892, :910).
   // 'interior_only_transverse' reproduces the species copy of the free
   // boundary, which the reference restricts to JY,KZ = 1..N (:1057).
-  void fill_dir(std::vector<double> &a, int d, int nol, bool species = false) {
+  double dtf_at(int II, int j, int k) const { return (double)dtf[id(II, j, k)]; }
+  // the value an inflow ghost cell g (x index, side 0 left / 1 right) of the
+  // row (j,k) receives under rule r; 'a' is the array being filled
+  double inflow_value(int r, int side, int g, int j, int k, std::vector<double> &a) {
+    const size_t c = id(g, j, k);
+    const double *v = in.v[side];
+    switch (r) {
+      case IN_RHO: {
+        const double L = DX(0, 0) * Nx * 1;   // dx(0)*Ncellx*NSPLTx with one block
+        double xp;
+        if (side == 0) {
+          xp = X(0, 0) - 0.5 * DX(0, 0) + g * DX(0, 0) - time * in.v[0][0];
+          int nn = (int)(std::fabs(xp) / L) + 1;
+          xp = xp + L * nn;
+        } else {
+          xp = 0.5 * (X(0, g - 1) + X(0, g)) - time * in.v[1][0];
+          int nn = (int)(std::fabs(xp) / L);
+          xp = xp - L * nn;
+        }
+        int II = (int)(xp / DX(0, 0)) + 1;
+        return dtf_at(II, j, k);
+      }
+      case IN_V1: return v[0];
+      case IN_V2: return v[1];
+      case IN_V3: return v[2];
+      case IN_M1: return U[1][c] * v[0];
+      case IN_M2: return in.rho_ref * v[1];
+      case IN_M3: return in.rho_ref * v[2];
+      case IN_P: return in.p[side];
+      case IN_E:
+        return in.p[side] * 1.5 + 0.5 * (U[1][c] * (v[0] * v[0]) + Bcc[1][c] * Bcc[1][c] + Blg[1][c] * Blg[1][c] +
+                                         Blg[2][c] * Blg[2][c]);
+      case IN_BXF: return side == 0 ? a[id(1, j, k)] : a[id(Nx + 1, j, k)];
+      case IN_B2: return in.b[side][1];
+      case IN_B3: return in.b[side][2];
+      case IN_DXLAG: return side == 0 ? DX(0, 0) : DX(0, Nx + 1);
+      case IN_BCC1:
+      case IN_VFC: return side == 0 ? a[id(1, j, k)] : a[id(Nx, j, k)];
+      default: return in.cm[r - IN_SPEC] * U[1][c];   // IN_SPEC + s
+    }
+  }
+
+  void fill_dir(std::vector<double> &a, int d, int nol, bool species = false, int rule = IN_KEEP) {
     int N = Nd(d);
     int b1 = P.bc[2 * d], b2 = P.bc[2 * d + 1];
+    if (d == 0 && (b1 == 4 || b2 == 4)) {
+      fill_x_inflow(a, nol, species, rule);
+      return;
+    }
     int ext[3] = {sx, sy, sz};
     int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
     for (int q2 = -1; q2 < ext[o2] - 1; q2++)
@@ -112,14 +188,49 @@ struct Mhd3D {
           for (int g = N + 1; g <= N + nol; g++) at(g) = at(N);
       }
   }
+  // x exchange with an inflow side: the periodic receive only on a side
+  // that is not BC=4 (its neighbour exists), then the BC=4 assignment.  A
+  // face array with rule IN_BXF gets faces 1-nol..0 and n+2..n+nol.
+  void fill_x_inflow(std::vector<double> &a, int nol, bool species, int rule) {
+    int N = Nx;
+    int b1 = P.bc[0], b2 = P.bc[1];
+    for (int k = -1; k <= Nz + 2; k++)
+      for (int j = -1; j <= Ny + 2; j++) {
+        auto at = [&](int i) -> double & { return a[id(i, j, k)]; };
+        bool tr_in = (j >= 1 && j <= Ny && k >= 1 && k <= Nz);
+        if (b1 != 4) {
+          for (int g = 1 - nol; g <= 0; g++) at(g) = at(g + N);
+          if (b1 == 1 && (!species || tr_in))
+            for (int g = 1 - nol; g <= 0; g++) at(g) = at(1);
+        } else if (rule != IN_KEEP && (!species || tr_in)) {
+          for (int g = 1 - nol; g <= 0; g++) at(g) = inflow_value(rule, 0, g, j, k, a);
+        }
+        if (b2 != 4) {
+          for (int g = N + 1; g <= N + nol; g++) at(g) = at(g - N);
+          if (b2 == 1 && (!species || tr_in))
+            for (int g = N + 1; g <= N + nol; g++) at(g) = at(N);
+        } else if (rule != IN_KEEP && (!species || tr_in)) {
+          for (int g = (rule == IN_BXF ? N + 2 : N + 1); g <= N + nol; g++) at(g) = inflow_value(rule, 1, g, j, k, a);
+        }
+      }
+  }
   // dirs: bit0 = x, bit1 = y, bit2 = z, applied in x, y, z order
-  void fill(std::vector<double> &a, int dirs, int nol, bool species = false) {
+  void fill(std::vector<double> &a, int dirs, int nol, int rule = IN_KEEP) {
     for (int d = 0; d < 3; d++)
-      if (dirs & (1 << d)) fill_dir(a, d, nol, species);
+      if (dirs & (1 << d)) fill_dir(a, d, nol, false, rule);
   }
   void fill_species(int dirs, int nol) {
-    for (int s = 0; s < 8; s++) fill(sp[s], dirs, nol, true);
+    for (int s = 0; s < 8; s++)
+      for (int d = 0; d < 3; d++)
+        if (dirs & (1 << d)) fill_dir(sp[s], d, nol, true, IN_SPEC + s);
   }
+  // the BC=4 rule of U(:,f) at a BC_MPI exchange in mode 1 (primitive) or 2
+  static int rule_of(int f, int mode) {
+    static const int m1[9] = {IN_KEEP, IN_RHO, IN_V1, IN_V2, IN_V3, IN_P, IN_BXF, IN_B2, IN_B3};
+    static const int m2[9] = {IN_KEEP, IN_RHO, IN_M1, IN_M2, IN_M3, IN_E, IN_BXF, IN_B2, IN_B3};
+    return mode == 1 ? m1[f] : m2[f];
+  }
+  void fillU(int f, int dirs, int nol, int mode) { fill(U[f], dirs, nol, rule_of(f, mode)); }
 
   // ---------------------------------------------------------------- helpers
   double gam_of(size_t c) {
@@ -195,7 +306,7 @@ struct Mhd3D {
     int BN = 6 + d;
 
     // ===== RHS (:1330-1467)
-    fill(U[1], dirbit, 2); fill(U[VN], dirbit, 2); fill(U[5], dirbit, 2);   // BC_MPI(2,1) :1355
+    fillU(1, dirbit, 2, 1); fillU(VN, dirbit, 2, 1); fillU(5, dirbit, 2, 1);   // BC_MPI(2,1) :1355
     fill_species(dirbit, 2);                                                  // :1357
 #pragma omp parallel for collapse(2) schedule(static)
     for (int Lnum = 1; Lnum <= Ncl; Lnum++)
@@ -264,12 +375,12 @@ struct Mhd3D {
       }
 
     // ===== MOC (:1939-2098)
-    fill(U[1], dirbit, 2); fill(U[VT1], dirbit, 2); fill(U[VT2], dirbit, 2); fill(U[BN], dirbit, 2);  // :1960
+    fillU(1, dirbit, 2, 1); fillU(VT1, dirbit, 2, 1); fillU(VT2, dirbit, 2, 1); fillU(BN, dirbit, 2, 1);  // :1960
     for (int Lnum = 1; Lnum <= Ncl; Lnum++)
       for (int Mnum = 1; Mnum <= Ncm; Mnum++)
         for (int i = 1; i <= N; i++)
           dxlagM[pidx(d, i, Mnum, Lnum)] = xlag[pidx(d, i, Mnum, Lnum)] - xlag[pidx(d, i - 1, Mnum, Lnum)];
-    fill(dxlagM, dirbit, 2); fill(Blg[1], dirbit, 2); fill(Blg[2], dirbit, 2);   // :1974
+    fill(dxlagM, dirbit, 2, IN_DXLAG); fill(Blg[1], dirbit, 2, IN_B2); fill(Blg[2], dirbit, 2, IN_B3);   // :1974
 #pragma omp parallel for collapse(2) schedule(static)
     for (int Lnum = 1; Lnum <= Ncl; Lnum++)
       for (int Mnum = 1; Mnum <= Ncm; Mnum++) {
@@ -349,8 +460,8 @@ struct Mhd3D {
       }
 
     // ===== REMAP (:1556-1686)
-    fill(Blg[1], dirbit, 2); fill(Blg[2], dirbit, 2);                         // :1572 (mode 2)
-    for (int f = 1; f <= 5; f++) fill(U[f], dirbit, 2);                       // :1581 (mode 2)
+    fill(Blg[1], dirbit, 2, IN_B2); fill(Blg[2], dirbit, 2, IN_B3);           // :1572 (mode 2)
+    for (int f = 1; f <= 5; f++) fillU(f, dirbit, 2, 2);                      // :1581 (mode 2)
     fill_species(dirbit, 2);                                                  // :1594
 #pragma omp parallel for collapse(2) schedule(static)
     for (int Lnum = 1; Lnum <= Ncl; Lnum++)
@@ -437,9 +548,9 @@ struct Mhd3D {
   // ------------------------------------------------------------- CT
   // CC(mode) (MCF3DSGincfca3.f90:2115-2183) and CCT (:2186-2445)
   void CC1() {
-    fill(U[2], 1, 2); fill(U[7], 1, 2); fill(U[8], 1, 2);     // :2123
-    fill(U[3], 2, 2); fill(U[6], 2, 2); fill(U[8], 2, 2);     // :2124
-    fill(U[4], 4, 2); fill(U[6], 4, 2); fill(U[7], 4, 2);     // :2125
+    fillU(2, 1, 2, 1); fillU(7, 1, 2, 1); fillU(8, 1, 2, 1);   // :2123
+    fillU(3, 2, 2, 1); fillU(6, 2, 2, 1); fillU(8, 2, 2, 1);   // :2124
+    fillU(4, 4, 2, 1); fillU(6, 4, 2, 1); fillU(7, 4, 2, 1);   // :2125
     for (int k = 1; k <= Nz; k++)
       for (int j = 1; j <= Ny; j++)
         for (int i = 1; i <= Nx + 1; i++)
@@ -457,10 +568,10 @@ struct Mhd3D {
                                 (DX(2, k - 1) + DX(2, k));
     // BC_MPI_OT(2,1) with N_MPI(13)=1 and iwx=iwy=iwz=1 (:2135, :1018-1036,
     // :1127-1135, :1205-1213): x moves Vfc2,3; y moves Vfc1,3; z moves Vfc1,2
-    fill_dir(Vfc[2], 0, 2); fill_dir(Vfc[3], 0, 2);
+    fill_dir(Vfc[2], 0, 2, false, IN_VFC); fill_dir(Vfc[3], 0, 2, false, IN_VFC);
     fill_dir(Vfc[1], 1, 2); fill_dir(Vfc[3], 1, 2);
     fill_dir(Vfc[1], 2, 2); fill_dir(Vfc[2], 2, 2);
-    fill(U[5], 7, 2);                                           // :2137
+    fillU(5, 7, 2, 1);                                          // :2137
   }
 
   // VLIMIT on a face array (branches 14-16, 6-8) along direction d for the
@@ -494,7 +605,7 @@ struct Mhd3D {
   // CC(2) + CCT for one edge direction e (0: Ez from x/y, 1: Ex from y/z,
   // 2: Ey from z/x), :2140-2157 and :2186-2445.
   void CCT(int e, double dt) {
-    if (e == 0) fill(U[1], 7, 2);   // :2142, only in the iwx branch
+    if (e == 0) fillU(1, 7, 2, 1);   // :2142, only in the iwx branch
     // dnc, edge density
     if (e == 0) {
       for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny + 1; j++) for (int i = 1; i <= Nx + 1; i++)
@@ -693,7 +804,7 @@ struct Mhd3D {
       Bcc[2][a] = 0.5 * (U[7][a] + U[7][id(i, j + 1, k)]);
       Bcc[3][a] = 0.5 * (U[8][a] + U[8][id(i, j, k + 1)]);
     }
-    for (int c = 1; c <= 3; c++) fill(Bcc[c], 7, 2);
+    fill(Bcc[1], 7, 2, IN_BCC1); fill(Bcc[2], 7, 2, IN_B2); fill(Bcc[3], 7, 2, IN_B3);
   }
 
   void CT(double dt) {   // EVOLVE:639-649
@@ -735,7 +846,7 @@ struct Mhd3D {
 
   void SOURCE(double dt) {   // thermal branch ifthrm=2, :2477-2572
     if (P.ifthrm != 2) return;
-    fill(U[1], 7, 1); fill(U[5], 7, 1);                              // :2484
+    fillU(1, 7, 1, 1); fillU(5, 7, 1, 1);                            // :2484
     fill_species(7, 1);                                              // :2486
     std::vector<double> Tn(ncell), Pn(ncell), Qx(ncell), Qy(ncell), Qz(ncell);
     auto ntot = [&](size_t c) { return sp[SP][c] + sp[SH][c] + sp[SH2][c] + sp[SHE][c] + sp[SHEP][c]; };
@@ -762,7 +873,7 @@ struct Mhd3D {
     fluxes();
     for (int pass = 0; pass < 2; pass++) {
       if (pass == 1) {
-        fill(U[5], 7, 1);                                           // :2528
+        fillU(5, 7, 1, 1);                                          // :2528
         temps();
         fluxes();
       }
@@ -850,7 +961,7 @@ struct Mhd3D {
   // edge ranks.  Both edges are damped here, each from the pre-damping
   // velocities, which is what any run with NSPLTx >= 2 does.
   void DISSIP() {
-    fill(U[2], 7, 2); fill(U[3], 7, 2); fill(U[4], 7, 2);
+    fillU(2, 7, 2, 1); fillU(3, 7, 2, 1); fillU(4, 7, 2, 1);
     int offs[2] = {0, Nx - 10};
     std::vector<double> divv[2];
     for (int e = 0; e < 2; e++) {
@@ -949,6 +1060,23 @@ double o3d_step(void *h, double tsave, int *st) {
 }
 
 void o3d_destroy(void *h) { delete static_cast<Mhd3D *>(h); }
+
+// BC=4 inflow data: in = rho_ref, v[2][3], p[2], b[2][3], cm[8] (species
+// slots H,p,H2,He,He+,C,C+,CO); dtf = the DTF reservoir as REAL*4 values in
+// the padded layout of U (DTF(-1..nx+2,-1..ny+2,-1..nz+2)), or NULL for a
+// uniform reservoir of density 'uniform' (the shipped code's DTF = dinit1).
+void o3d_set_inflow(void *h, const double *in, const float *dtf, double uniform) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  InflowBC &b = m->in;
+  b.rho_ref = in[0];
+  for (int s = 0; s < 2; s++) for (int c = 0; c < 3; c++) b.v[s][c] = in[1 + 3 * s + c];
+  b.p[0] = in[7]; b.p[1] = in[8];
+  for (int s = 0; s < 2; s++) for (int c = 0; c < 3; c++) b.b[s][c] = in[9 + 3 * s + c];
+  for (int q = 0; q < 8; q++) b.cm[q] = in[15 + q];
+  size_t n = m->ncell;
+  m->dtf.assign(n, (float)uniform);
+  if (dtf) memcpy(m->dtf.data(), dtf, n * sizeof(float));
+}
 
 // The plain integrator's answer for one surrogate input point: with the KI
 // density N = 10^x0, T = 10^x1 (1e3 K) and dt/t_cool = 10^x2, solve

@@ -59,6 +59,7 @@ def lib():
         L.o3d_step.restype = ctypes.c_double
         L.o3d_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
         L.o3d_destroy.argtypes = [ctypes.c_void_p]
+        L.o3d_set_inflow.argtypes = [ctypes.c_void_p, _P, ctypes.c_void_p, ctypes.c_double]
         L.o3d_ki_label.restype = ctypes.c_double
         L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
@@ -151,6 +152,17 @@ class Oracle3D:
 
     def set_order(self, ifevo):
         lib().o3d_set_order(self.h, ifevo)
+
+    def set_inflow(self, inflow, reservoir=None, uniform=0.0):
+        """BC=4 data: `inflow` is the packed vector of problems.Inflow.vector()
+        and `reservoir` the DTF array (nz+4, ny+4, nx+4) float32, or None for
+        a uniform reservoir of density `uniform`."""
+        v = np.ascontiguousarray(inflow, dtype=np.float64)
+        if reservoir is None:
+            lib().o3d_set_inflow(self.h, _ptr(v), None, ctypes.c_double(uniform))
+        else:
+            r = np.ascontiguousarray(reservoir, dtype=np.float32)
+            lib().o3d_set_inflow(self.h, _ptr(v), r.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(uniform))
 
     @property
     def time(self):
