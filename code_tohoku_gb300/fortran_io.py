@@ -30,6 +30,8 @@ _SIGS = {
     "mhd_io_read_restart": [ctypes.c_char_p, ctypes.POINTER(_Grid), _D, _D, _D],
     "mhd_io_write_plane": [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_Grid), _D, _D, _D, _D],
     "mhd_io_format_d25_17": [ctypes.c_double, ctypes.c_int, ctypes.c_char_p],
+    "mhd_io_write_reservoir": [ctypes.c_char_p, ctypes.POINTER(_Grid), ctypes.c_void_p],
+    "mhd_io_read_reservoir": [ctypes.c_char_p, ctypes.POINTER(_Grid), ctypes.c_void_p, ctypes.c_double],
     "mhd_io_write_time_dat": [ctypes.c_char_p, _D, ctypes.c_int, ctypes.c_int],
     "mhd_io_write_tsave": [ctypes.c_char_p, ctypes.c_double, ctypes.c_int, ctypes.c_int],
     "mhd_io_format_info_line": [ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_char_p],
@@ -115,6 +117,24 @@ def write_plane(directory, nunit2d, U, bcc, species, phi=None, nsplit=(1, 1, 1))
     g = _grid(sh, nsplit)
     _ck(_L().mhd_io_write_plane(os.fsencode(directory), nunit2d, ctypes.byref(g), _p(U), _p(bcc), _p(species),
                                 _p(phi)), "write_plane")
+
+
+def write_reservoir(directory, dtf, nsplit=(1, 1, 1)):
+    """The DTF reservoir (float32, padded state shape) as per-rank D###.dat."""
+    d = np.ascontiguousarray(dtf, dtype=np.float32)
+    g = _grid(d.shape, nsplit)
+    _ck(_L().mhd_io_write_reservoir(os.fsencode(directory), ctypes.byref(g), d.ctypes.data_as(ctypes.c_void_p)),
+        "write_reservoir")
+
+
+def read_reservoir(directory, shape, nsplit=(1, 1, 1), ghost_density=0.0):
+    """Per-rank D###.dat into the padded reservoir for mhd_set_inflow (periodic
+    y/z ghosts, ghost_density in the x ghosts)."""
+    d = np.zeros(tuple(shape), dtype=np.float32)
+    g = _grid(d.shape, nsplit)
+    _ck(_L().mhd_io_read_reservoir(os.fsencode(directory), ctypes.byref(g), d.ctypes.data_as(ctypes.c_void_p),
+                                   float(ghost_density)), "read_reservoir")
+    return d
 
 
 def format_d25_17(v, with_1p=True):

@@ -58,6 +58,17 @@ int mhd_io_read_restart(const char *dir, const mhd_io_grid *g, double *U, double
 int mhd_io_write_plane(const char *dir, int nunit2d, const mhd_io_grid *g, const double *U, const double *bcc,
                        const double *species, const double *phi);
 
+/* The DTF density reservoir of the inflow boundary as the density
+ * generator writes it (GenDen/IGEN1.f90:156-161) and INITIA reads it
+ * (MCF3DSGincfca3.f90:404-432): D%03d.dat per rank, for k = 1..nz, j = 1..ny
+ * of the rank's block one record of its nx REAL*4 values.  write: every
+ * rank's file from the padded single-domain array (the layout mhd_set_inflow
+ * takes); read: all files into that array, then the two periodic ghost
+ * layers in y and z (the reference's exchanges of DTF) and ghost_density in
+ * the x ghosts (DTF's initial value there, dinit1). */
+int mhd_io_write_reservoir(const char *dir, const mhd_io_grid *g, const float *dtf);
+int mhd_io_read_reservoir(const char *dir, const mhd_io_grid *g, float *dtf, double ghost_density);
+
 /* one value in the D25.17 edit descriptor: with_1p = 1 gives 1P,D25.17 (the
  * 3D code's time.DAT / tsave.DAT), 0 gives D25.17 (the 1D code's).  out must
  * hold 26 bytes. */

@@ -145,3 +145,22 @@ def test_reads_shipped_input3d_deck(golden_dir):
     assert (d.cfl, d.facdep, d.maxstp, d.nitera, d.tfinal) == (0.49, 1.0, 4, 5000, 100.0)
     assert d.bc == (4, 4, 3, 3, 3, 3)
     assert (d.ifchem, d.ifthrm, d.ifrad, d.ifgrv) == (2, 2, 0, 0)
+
+
+def test_reservoir_files_round_trip(tmp_path):
+    rng = np.random.default_rng(9)
+    sh = (NZ + 4, NY + 4, NX + 4)
+    dtf = rng.random(sh).astype(np.float32)
+    fio.write_reservoir(str(tmp_path), dtf, (2, 3, 1))
+    bx, by, bz = NX // 2, NY // 3, NZ
+    for r in range(6):
+        IS, JS = r % 2, r // 2
+        recs = records(os.path.join(tmp_path, f"D{r:03d}.dat"), "<f4")
+        assert len(recs) == bz * by
+        np.testing.assert_array_equal(recs[0], dtf[2, JS * by + 2, IS * bx + 2: IS * bx + 2 + bx])
+    back = fio.read_reservoir(str(tmp_path), sh, (2, 3, 1), ghost_density=1.25)
+    c = (slice(2, NZ + 2), slice(2, NY + 2), slice(2, NX + 2))
+    np.testing.assert_array_equal(back[c], dtf[c])
+    assert (back[:, :, :2] == np.float32(1.25)).all() and (back[:, :, -2:] == np.float32(1.25)).all()
+    np.testing.assert_array_equal(back[2:NZ + 2, 0, 2:NX + 2], back[2:NZ + 2, NY, 2:NX + 2])     # y wrap
+    np.testing.assert_array_equal(back[NZ + 3, 2:NY + 2, 2:NX + 2], back[3, 2:NY + 2, 2:NX + 2])  # z wrap
