@@ -168,6 +168,16 @@ DM_HD double exp10(double y) {
   return exp_hl(p, e + y * LN10_LO);
 }
 
+// x**y for x >= 0 as exp(y log x) with the functions above: the real powers
+// the reference takes of positive quantities (temperatures, rates, column
+// terms); 0**y is 0 for y > 0 and +inf for y < 0, as libm gives.
+DM_HD double pow(double x, double y) {
+  if (x == 0.0) return y > 0.0 ? 0.0 : (y < 0.0 ? bits_to_double(0x7ff0000000000000ull) : 1.0);
+  double p, e;
+  two_prod(y, detmath::log(x), p, e);
+  return exp_hl(p, e);
+}
+
 // Fortran intrinsic semantics used by the reference, written once so the
 // CPU restatement and the GPU kernels agree on signed zeros:
 //   SIGN(a,b) = |a| with the sign bit of b (gfortran follows copysign),

@@ -97,6 +97,12 @@ cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], dou
   return cudaGetLastError();
 }
 
+cudaError_t chem_step_fp32(const Grid &g, const Phys &ph, const Fields &f, double dt, int *err, cudaStream_t s) {
+  long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+  chem32_kernel<<<blocks_for(n, 128), 128, 0, s>>>(g, ph, f, d2f(dt), err);
+  return cudaGetLastError();
+}
+
 cudaError_t source_fp32(const Source32Args &a, cudaStream_t s) {
   long long n = (long long)a.g.n[0] * a.g.n[1] * a.g.n[2];
   source32_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);

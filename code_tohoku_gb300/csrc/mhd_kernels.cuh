@@ -58,6 +58,7 @@ struct InflowDev {
 struct Phys {
   double facdep, pmin, pmax, rmin, kb, kcond, cfl, tfinal;
   int ifthrm;
+  int ifchem;              // 2: species cooling + chemistry network; 0: KI cooling
   double ndmin[8];
   InflowDev in;
 };
@@ -84,6 +85,7 @@ struct Fields {
   double *U[8];
   double *sp[8];
   double *bcc[3];
+  double *nde, *ndtot;     // electron / particle densities of the chemistry (ifchem = 2)
 };
 
 __host__ __device__ inline long long gidx(const Grid &g, int i, int j, int k) {
@@ -274,6 +276,19 @@ __device__ __forceinline__ double gmi1_of(double H, double p, double He, double 
 }
 
 __device__ __forceinline__ void flag(int *err, int bit) { atomicOr(err, bit); }
+
+}  // namespace mhd
+#include "mhd_chem.cuh"
+namespace mhd {
+
+template <class R, class Load>
+__device__ __forceinline__ CellSpecies<R> cell_species(const Fields &f, long long a, Load &&ld) {
+  CellSpecies<R> c;
+  c.H = ld(f.sp[0][a]); c.p = ld(f.sp[1][a]); c.H2 = ld(f.sp[2][a]); c.He = ld(f.sp[3][a]);
+  c.Hep = ld(f.sp[4][a]); c.C = ld(f.sp[5][a]); c.Cp = ld(f.sp[6][a]); c.CO = ld(f.sp[7][a]);
+  c.ne = ld(f.nde[a]); c.nt = ld(f.ndtot[a]);
+  return c;
+}
 
 // ============================================================ ghost fill
 // One direction of one BC_MPI / BC_MPI_OT exchange for up to 8 arrays.
@@ -944,14 +959,22 @@ __device__ __forceinline__ float fcool_ki(float T, float NN) {
   return (NN * NN * (Laml + Lamc) - NN) * 3.94656e1f;
 }
 
+// the cooling function of the run at temperature T of cell a: the KI form
+// (NN = rho/1.27) or, with ifchem = 2, the species form
+__device__ __forceinline__ double cool_of(const Phys &ph, const Fields &f, long long a, double T) {
+  if (ph.ifchem == 2) return fcool_species<double>(T, cell_species<double>(f, a, [](double v) { return v; }));
+  return fcool_ki(T, f.U[0][a] / 1.27);
+}
+
 // IMC, log-space bisection for P + Lambda(P) dt (gamma-1) = P_old, at most
 // 30 iterations (:2898-2921).  The loop bound is the reference's.
-__device__ __forceinline__ double imc(double Pold, double n, double dt, double g1c, double NN, double kb) {
+template <class Cool>
+__device__ __forceinline__ double imc_f(double Pold, double n, double dt, double g1c, double kb, Cool &&cool) {
   double Pu = 1.e10, Pd = 1.e-10, Pm = 1.e1, Pmold = -1.0;
   double nkbi = 1.0 / (kb * n);
   for (int kkk = 1; kkk <= 30; kkk++) {
     double T = Pm * nkbi;
-    double CooL = fcool_ki(T, NN);
+    double CooL = cool(T);
     double fev = Pm + CooL * dt * g1c - Pold;
     double iud = fsgn(1.0, fev);
     Pd = fmx(-iud * Pm, Pd);
@@ -961,6 +984,9 @@ __device__ __forceinline__ double imc(double Pold, double n, double dt, double g
     Pmold = Pm;
   }
   return Pm;
+}
+__device__ __forceinline__ double imc(double Pold, double n, double dt, double g1c, double NN, double kb) {
+  return imc_f(Pold, n, dt, g1c, kb, [&](double T) { return fcool_ki(T, NN); });
 }
 
 struct SourceArgs {
@@ -1014,7 +1040,7 @@ __device__ __forceinline__ void cell_dt_limits(const Grid &g, const Phys &ph, co
     double g1c = gmi1_of(H, pr, He, Hep, H2);
     double alpha = g1c * ph.kcond * sqrt(fmn(Tn, 15.0));
     alpha = 0.4 * Nn * ph.kb / alpha * (dl * dl);
-    double CooL = fcool_ki(Tn, rho / 1.27);
+    double CooL = cool_of(ph, f, a, Tn);
     double tauC = p5 / g1c / fabs(CooL);
     tauC = fmx(0.2 * tauC, 2.5e-4);
     s_min = fmn(s_min, tauC);
@@ -1055,8 +1081,8 @@ __global__ void source_kernel(SourceArgs A) {
   double Qzm = flux(Tn(a - sz), T0, dz[k], dz[k + 1]);
   const Fields &f = A.f;
   double g1c = gmi1_of(f.sp[0][a], f.sp[1][a], f.sp[3][a], f.sp[4][a], f.sp[2][a]);
-  double NN = f.U[0][a] / 1.27;
-  double CooL = fcool_ki(T0, NN);
+  double CooL = cool_of(A.ph, f, a, T0);
+  auto cool = [&](double T) { return cool_of(A.ph, f, a, T); };
   double Pn = A.pold[a];
   double pnew;
   bool skip = A.skip && A.skip[a];
@@ -1064,14 +1090,14 @@ __global__ void source_kernel(SourceArgs A) {
     if (skip) pnew = A.pout[a];
     else if (dt <= 0.2 * Pn / (g1c * fabs(CooL))) pnew = pin[a] - g1c * CooL * dt * 0.5;
     else {
-      pnew = imc(pin[a], ntot_imc(f, a), dt * 0.5, g1c, NN, kb);
+      pnew = imc_f(pin[a], ntot_imc(f, a), dt * 0.5, g1c, kb, cool);
       atomicAdd(A.imc_count, 1ull);
     }
   } else {
     if (skip) pnew = A.pout[a];
     else if (dt <= 0.2 * Pn / (g1c * fabs(CooL))) pnew = Pn - g1c * CooL * dt;
     else {
-      pnew = imc(Pn, ntot_imc(f, a), dt, g1c, NN, kb);
+      pnew = imc_f(Pn, ntot_imc(f, a), dt, g1c, kb, cool);
       atomicAdd(A.imc_count, 1ull);
     }
   }
@@ -1085,6 +1111,35 @@ __global__ void source_kernel(SourceArgs A) {
   pnew = fmn(pnew, A.ph.pmax);
   A.pout[a] = pnew;
   if (!(pnew == pnew)) flag(A.err, ERRB_NONFINITE);
+}
+
+// the chemistry network of every interior cell after the thermal update
+// (ifchem = 2, :2576-2776): species, nde, ndtot, and rho = sum m n
+__global__ void chem_kernel(Grid g, Phys ph, Fields f, double dt, int *err) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  if (t >= (long long)nx * ny * nz) return;
+  long long a = gidx(g, 1 + (int)(t % nx), 1 + (int)((t / nx) % ny), 1 + (int)(t / ((long long)nx * ny)));
+  CellSpecies<double> c = cell_species<double>(f, a, [](double v) { return v; });
+  const double (&mn)[8] = ph.ndmin;
+  chem_network<double>(c, f.U[4][a], ph.kb, dt, mn);
+  f.sp[0][a] = c.H; f.sp[1][a] = c.p; f.sp[2][a] = c.H2; f.sp[3][a] = c.He;
+  f.sp[4][a] = c.Hep; f.sp[5][a] = c.C; f.sp[6][a] = c.Cp; f.sp[7][a] = c.CO;
+  f.nde[a] = c.ne;
+  f.ndtot[a] = c.nt;
+  double rho = 1.0 * c.p + 1.0 * c.H + 2.0 * c.H2 + 4.0 * c.He + 4.0 * c.Hep;   // mH, mH2, mHe
+  f.U[0][a] = rho;
+  if (!(rho == rho)) flag(err, ERRB_NONFINITE);
+}
+
+// nde and ndtot from the species of cells 1..n+1 (INITIA :471-474)
+__global__ void chem_totals_kernel(Grid g, Fields f) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int nx = g.n[0] + 1, ny = g.n[1] + 1, nz = g.n[2] + 1;
+  if (t >= (long long)nx * ny * nz) return;
+  long long a = gidx(g, 1 + (int)(t % nx), 1 + (int)((t / nx) % ny), 1 + (int)(t / ((long long)nx * ny)));
+  f.nde[a] = f.sp[1][a] + f.sp[4][a] + f.sp[6][a];
+  f.ndtot[a] = f.sp[1][a] + f.sp[0][a] + 2.0 * f.sp[2][a] + f.sp[3][a] + f.sp[4][a];
 }
 
 // ============================================================ dt
@@ -1120,7 +1175,7 @@ __global__ void dt_kernel(Grid g, Phys ph, Fields f, unsigned long long *out /* 
       double g1c = gmi1_of(H, pr, He, Hep, H2);
       double alpha = g1c * ph.kcond * sqrt(fmn(Tn, 15.0));
       alpha = 0.4 * Nn * ph.kb / alpha * (dl * dl);
-      double CooL = fcool_ki(Tn, rho / 1.27);
+      double CooL = cool_of(ph, f, a, Tn);
       double tauC = p5 / g1c / fabs(CooL);
       tauC = fmx(0.2 * tauC, 2.5e-4);
       s_min = fmn(s_min, tauC);

@@ -43,7 +43,7 @@ class _Params(ctypes.Structure):
                 ("pmin", ctypes.c_double), ("pmax", ctypes.c_double), ("rmin", ctypes.c_double),
                 ("kb", ctypes.c_double), ("kcond", ctypes.c_double),
                 ("ifthrm", ctypes.c_int), ("dissip", ctypes.c_int), ("precision", ctypes.c_int),
-                ("cooling", ctypes.c_int), ("device", ctypes.c_int)]
+                ("cooling", ctypes.c_int), ("device", ctypes.c_int), ("ifchem", ctypes.c_int)]
 
 
 class _Diag(ctypes.Structure):
@@ -207,6 +207,7 @@ def params_struct(p: MhdParams, precision=PREC_FP64, cooling=COOL_EXACT, device=
     s.kb, s.kcond = p.kb, p.kcond
     s.ifthrm, s.dissip = p.ifthrm, p.dissip
     s.precision, s.cooling, s.device = precision, cooling, device
+    s.ifchem = getattr(p, "ifchem", 0)
     return s
 
 

@@ -56,6 +56,7 @@ class MhdParams:
     kcond: float = KCOND
     ifthrm: int = 2
     dissip: int = 1
+    ifchem: int = 0     # 2: chemistry network + species cooling (the shipped deck's); 0: KI cooling
 
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)

@@ -70,6 +70,9 @@ typedef struct mhd_params {
   int precision;               /* MHD_PREC_FP64 or MHD_PREC_FP32            */
   int cooling;                 /* MHD_COOL_EXACT or MHD_COOL_SURROGATE      */
   int device;                  /* CUDA device ordinal                       */
+  int ifchem;                  /* 2: the reference's chemistry network and
+                                  species cooling (:2576-2776, :2825-2880);
+                                  0: the KI cooling function                */
 } mhd_params;
 
 /* Inflow boundary data (BC code 4 on an x side): the values a ghost cell on

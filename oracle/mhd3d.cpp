@@ -68,7 +68,9 @@ struct Params {
   int bc[6];          // BCx1,BCx2,BCy1,BCy2,BCz1,BCz2: 1 = free, 4 = inflow (x only), otherwise periodic
   double pmin, pmax, rmin;
   double kb, Kcond;
-  int ifthrm;         // 2: KI source + thermal dt limit; 0: neither
+  int ifthrm;         // 2: thermal source + thermal dt limit; 0: neither
+  int ifchem;         // 2: chemistry network and the species cooling function
+                      //    (SOURCE :2576-2776, Fcool :2825-2880); 0: KI cooling
   int dissip;         // 1: DISSIP edge damping (MCF3DSGincfca3.f90:3143-3173)
   int nspecies;       // 8 (all species carried)
 };
@@ -86,6 +88,10 @@ struct Mhd3D {
   std::vector<double> dnc, xlag, dxlagM;
   double ndmin[8];
   InflowBC in{};
+  // electron and total particle densities, per cell (:471-474): set by INITIA
+  // and by the chemistry network only, never advected (Fcool and RATES read
+  // them as they were after the last chemistry update)
+  std::vector<double> nde, ndtot;
   std::vector<float> dtf;   // DTF(-1..nx+2, -1..ny+2, -1..nz+2), REAL*4 like the reference
 
   size_t id(int i, int j, int k) const {
@@ -101,6 +107,7 @@ struct Mhd3D {
     sx = Nx + 4; sy = Ny + 4; sz = Nz + 4;
     ncell = (size_t)sx * sy * sz;
     for (int f = 1; f <= 8; f++) U[f].assign(ncell, 0.0);
+    nde.assign(ncell, 0.0); ndtot.assign(ncell, 0.0);
     for (int s = 0; s < 8; s++) sp[s].assign(ncell, 0.0);
     for (int c = 1; c <= 3; c++) { Bcc[c].assign(ncell, 0.0); Vfc[c].assign(ncell, 0.0); EMF[c].assign(ncell, 0.0); }
     for (int c = 1; c <= 2; c++) Blg[c].assign(ncell, 0.0);
@@ -817,7 +824,285 @@ struct Mhd3D {
   }
 
   // ---------------------------------------------------------- source
-  double Fcool(double T, size_t c) { return FcoolN(T, U[1][c] / 1.27); }
+  double Fcool(double T, size_t c) { return P.ifchem == 2 ? FcoolSpecies(T, c) : FcoolN(T, U[1][c] / 1.27); }
+
+  // ----------------------------------------- chemistry (ifchem = 2)
+  // Column densities (Ntot, NH2, NnC, NCO, tCII) come from SHIELD, which
+  // runs only with ifrad = 2; with ifrad = 0 (the shipped deck) they keep
+  // their INITIA value 0 (:476-477), and so they are 0 here.
+  static constexpr double G0 = 1.0, xo = 3.2e-4, dv = 2.0, Tgr = 5.e-3;   // :28
+  static double pw(double x, double y) { return detmath::pow(x, y); }
+  static double fesc(double tau) {   // :2882-2887
+    return (0.5 + fsign(0.5, 0.1 - 1.e-16 - tau)) * (0.5 - 0.585 * tau + 0.4563 * (tau * tau)) +
+           (0.5 + fsign(0.5, 11.9025 - (tau - 3.55) * (tau - 3.55))) * (1.0 - detmath::exp(-2.34 * tau)) /
+               (4.68 * tau + 1.e-8) +
+           (0.5 + fsign(0.5, tau - 7.0)) /
+               (4.0 * tau * std::sqrt(detmath::log(fmax2(tau * 0.56419, 4.0))) + 1.e-8);
+  }
+  static void LEVC2(double T, double b21, double ndHv, double ndH2v, double ndev, double ndCpv, double &n1,
+                    double &n2) {   // :2889-2895
+    double c21 = 8.854e-8 * ndev / std::sqrt(T) + 9.399e-10 * pw(T, 0.07) * (ndHv + ndH2v);
+    double c12 = 2.0 * c21 * detmath::exp(-0.092 / T);
+    double A21 = 2.4e-6 * b21;
+    n2 = ndCpv * c12 / (c12 + c21 + A21);
+    n1 = ndCpv * (c21 + A21) / (c12 + c21 + A21);
+  }
+  // Fcool (:2825-2880): Ly-alpha, CII, OI, dust recombination and CO
+  // cooling minus photo-electric, cosmic-ray and photo-destruction heating
+  double FcoolSpecies(double T, size_t c) {
+    const double Ntot1 = 0.0, Ntot2 = 0.0, NH21 = 0.0, NH22 = 0.0, NCO1 = 0.0, NCO2 = 0.0, tC1 = 0.0, tC2 = 0.0;
+    const double H = sp[SH][c], p = sp[SP][c], H2 = sp[SH2][c], He = sp[SHE][c], Hep = sp[SHEP][c];
+    const double Cp = sp[SCP][c], CO = sp[SCO][c], ne = nde[c], nt = ndtot[c];
+    double Av1 = 1.63542e-3 * Ntot1, x1 = 6.1714e3 * NH21;
+    double Av2 = 1.63542e-3 * Ntot2, x2 = 6.1714e3 * NH22;
+    double ATN1 = (detmath::exp(-2.5 * Av1) + detmath::exp(-2.5 * Av2)) * 0.5;
+    double ATN2 = (detmath::exp(-3.77358 * Av1) + detmath::exp(-3.77358 * Av2)) * 0.5;
+    double pha = G0 * std::sqrt(1.e3 * T) * ATN1 / ne;
+    double Laml = H * ne * 1.44049e9 * detmath::exp(-1.184e2 / T);
+    Laml = Laml + p * ne * 1.48e6 * detmath::exp(-8.e1 / T);
+    double fesC1 = fesc(tC1), fesC2 = fesc(tC2);
+    double b21 = fesC1 + fesC2;
+    double n1, n2;
+    LEVC2(T, b21, H, H2, ne, Cp, n1, n2);
+    double Lamc = 6.0157e7 * n2 * b21;
+    double tO1 = 3.40057e-6 * Ntot1 / xo, tO2 = 3.40057e-6 * Ntot2 / xo;
+    double fesO1 = fesc(tO1), fesO2 = fesc(tO2);
+    double Lamo = (fmax2(nt * xo - CO, 0.0) / xo) * (H + 0.5 * H2) * 1.23916e1 * pw(T, 0.4) * detmath::exp(-0.228 / T);
+    Lamo = Lamo * (fesO1 + fesO2);
+    double Lamd = ne * nt * 6.06236 * pw(T, 0.94) * pw(pha, 0.462628 / pw(T, 6.8e-2));
+    double ncr = 3.3e6 * pw(T, 0.75) / (H + p + H2 + He + Hep);
+    double tau1 = 1.33194e1 * NCO1 / (T * dv), tau2 = 1.33194e1 * NCO2 / (T * dv);
+    double q1 = tau1 * 0.36788, q2 = tau2 * 0.36788;
+    double ct1 = tau1 * std::sqrt(6.283 * detmath::log(2.13 + q1 * q1));
+    double ct2 = tau2 * std::sqrt(6.283 * detmath::log(2.13 + q2 * q2));
+    double ym1 = detmath::log(1.0 + ct1 / (1.0 + 1.e1 * ncr)), ym2 = detmath::log(1.0 + ct2 / (1.0 + 1.e1 * ncr));
+    double fes = (2.0 + ym1 + 0.6 * (ym1 * ym1)) / (1.0 + ct1 + ncr + 1.5 * std::sqrt(ncr)) +
+                 (2.0 + ym2 + 0.6 * (ym2 * ym2)) / (1.0 + ct2 + ncr + 1.5 * std::sqrt(ncr));
+    double LCOr = CO * 1.91505e10 * (T * T) * fes;
+    double LCOH = H * CO * 7.96086e4 * std::sqrt(T) * detmath::exp(-pw(2.0 / T, 3.43)) * detmath::exp(-3.08 / T);
+    double LCOH2 = H2 * CO * 3.60834e4 * T * detmath::exp(-pw(3.14e2 / T, 0.333)) * detmath::exp(-3.08 / T);
+    double Gampe = nt * 2.56526e3 * G0 * ATN1 *
+                   (7.382e-3 * pw(T, 0.7) / (1.0 + 2.e-4 * pha) + 4.9e-2 / (1.0 + 4.e-3 * pw(pha, 0.73)));
+    double Gamcr = (H + He + H2) * 1.89435;
+    double s1 = 1.0 + x1 / dv, s2 = 1.0 + x2 / dv;
+    double SHLD1 = 0.965 / (s1 * s1) + 0.035 / std::sqrt(1.0 + x1) * detmath::exp(-8.5e-4 * std::sqrt(1.0 + x1));
+    double SHLD2 = 0.965 / (s2 * s2) + 0.035 / std::sqrt(1.0 + x2) * detmath::exp(-8.5e-4 * std::sqrt(1.0 + x2));
+    double Gampd = H2 * 4.16362e4 * G0 * ATN2 * (SHLD1 + SHLD2) * 0.5;
+    return Laml + Lamc + Lamo + Lamd + LCOr + LCOH + LCOH2 - Gampe - Gamcr - Gampd;
+  }
+  struct Rates {
+    double zeta, kHrec, kHerec, kH2, kH2ph, kH2dH, kH2de, kCO, kCOph, kCi, kCrec, kCOde, kCOdH, kHie, kHeie,
+        kCie, kHiH, kHeiH, kCiH, kCOdHep, kH2dHep;
+  };
+  // RATES (:3037-3131) at temperature T of cell c
+  Rates RATES(double T, size_t c) {
+    const double Ntot1 = 0.0, Ntot2 = 0.0, NH21 = 0.0, NH22 = 0.0, NCO1 = 0.0, NCO2 = 0.0, NnC1 = 0.0, NnC2 = 0.0;
+    Rates r;
+    double Av1 = 1.63542e-3 * Ntot1, x1 = 6.1714e3 * NH21;
+    double Av2 = 1.63542e-3 * Ntot2, x2 = 6.1714e3 * NH22;
+    double ATN2 = (detmath::exp(-3.77358 * Av1) + detmath::exp(-3.77358 * Av2)) * 0.5;
+    double ATN3 = (detmath::exp(-2.3585 * Av1) + detmath::exp(-2.3585 * Av2)) * 0.5;
+    double ATN4 = fmin2(1.0, pw(3.0857e1 * NH21, -3.e-2) * detmath::exp(-1.54285e-3 * NH21)) +
+                  fmin2(1.0, pw(3.0857e1 * NH22, -3.e-2) * detmath::exp(-1.54285e-3 * NH22));
+    ATN4 = ATN4 * 0.5;
+    const double e06 = (double)0.6f;   // the literal 0.6 is REAL*4 in the reference (:3068)
+    double ATN5 = (0.5 - fsign(0.5, NCO1 - 1.40995e-3)) * detmath::exp(-1.0 * pw(1.02857e3 * NCO1, e06)) +
+                  (0.5 + fsign(0.5, NCO1 - 1.40995e-3)) *
+                      fmin2(pw(3.75439e3 * NCO1 + 1.e-100, -0.75), pw(7.3469e1 * NCO1 + 1.e-100, -1.3));
+    ATN5 = ATN5 + (0.5 - fsign(0.5, NCO2 - 1.40995e-3)) * detmath::exp(-1.0 * pw(1.02857e3 * NCO2, e06)) +
+           (0.5 + fsign(0.5, NCO2 - 1.40995e-3)) *
+               fmin2(pw(3.75439e3 * NCO2 + 1.e-100, -0.75), pw(7.3469e1 * NCO2 + 1.e-100, -1.3));
+    ATN5 = ATN5 * 0.5;
+    r.zeta = 9.4671e-4;
+    double kh = (0.5 + fsign(0.5, 15.78 - T)) * 0.45 * detmath::log(1.578e2 / T) +
+                (0.5 - fsign(0.5, 15.78 - T)) * 0.4 * std::sqrt(1.578e2 / T);
+    r.kHrec = 2.05572e1 * pw(T, -0.5) * kh;
+    r.kHerec = 6.37623e1 * pw(T, -0.672);
+    r.kH2 = 3.4569e-3 * std::sqrt(T) / (1.0 + 1.26491 * std::sqrt(T + Tgr) + 2.0 * T + 8.0 * (T * T));
+    double s1 = 1.0 + x1 / dv, s2 = 1.0 + x2 / dv;
+    double SHLD1 = 0.965 / (s1 * s1) + 0.035 / std::sqrt(1.0 + x1) * detmath::exp(-8.5e-4 * std::sqrt(1.0 + x1));
+    double SHLD2 = 0.965 / (s2 * s2) + 0.035 / std::sqrt(1.0 + x2) * detmath::exp(-8.5e-4 * std::sqrt(1.0 + x2));
+    r.kH2ph = 1.04138e3 * G0 * ATN2 * (SHLD1 + SHLD2) * 0.5;
+    r.kH2dH = 1.07294e5 * detmath::exp(-4.39e1 / T);
+    r.kH2de = 1.133e6 * pw(T, 0.35) * detmath::exp(-1.02e2 / T);
+    r.kCO = 1.57785e-2 / (1.0 + G0 * ATN3 / (sp[SH2][c] * xo));
+    r.kCOph = 3.155e3 * G0 * ATN3 * ATN4 * ATN5;
+    double SHLC1 = detmath::exp(-2.6 * Av1 - 3.0857e1 * NnC1 - 4.33743413e-4 * NH21) / (1.0 + 4.33743413e-4 * NH21);
+    double SHLC2 = detmath::exp(-2.6 * Av2 - 3.0857e1 * NnC2 - 4.33743413e-4 * NH22) / (1.0 + 4.33743413e-4 * NH22);
+    r.kCi = 3.97 * r.zeta + 6.62697e3 * G0 * (SHLC1 + SHLC2) * 0.5;
+    r.kCrec = 2.69267e1 * pw(T, -0.62) * (1.0 + 1.e-4 * std::sqrt(nde[c]) / (T * T));
+    r.kCOde = 1.4e4 * pw(T, -0.5) * detmath::exp(-1.14e2 / T);
+    r.kCOdH = 1.91858e3 * pw(T, -0.5) * detmath::exp(-7.77e1 / T);
+    r.kHie = 5.76e4 * std::sqrt(T) * detmath::exp(-1.58e2 / T);
+    r.kHeie = 2.76e4 * pw(T, 0.43) * detmath::exp(-2.85e2 / T);
+    r.kCie = 1.74e5 * pw(T, 0.4) * detmath::exp(-1.31e2 / T);
+    r.kHiH = 9.79 * std::sqrt(T) * detmath::exp(-1.58e2 / T);
+    r.kHeiH = 4.57 * pw(T, 0.43) * detmath::exp(-2.85e2 / T);
+    r.kCiH = 3.01e1 * pw(T, 0.4) * detmath::exp(-1.31e2 / T);
+    r.kH2dHep = 1.1676 * detmath::exp(-0.035 / T);
+    r.kCOdHep = 5.0491e4;
+    return r;
+  }
+  static double Omexp(double eps) {   // 1 - exp(-eps), series below 1e-4 (:3134-3140)
+    double e2 = eps * eps;
+    return (0.5 + fsign(0.5, eps - 1.e-4)) * (1.0 - detmath::exp(-eps)) +
+           (0.5 - fsign(0.5, eps - 1.e-4)) *
+               (eps - 0.5 * e2 + 0.16666666666666667 * (e2 * eps) - 4.16666666666666667e-2 * (e2 * e2));
+  }
+  // the chemistry network of one cell over dt (:2580-2770)
+  void CHEM_cell(size_t c, double dt) {
+    double &H = sp[SH][c], &p = sp[SP][c], &H2 = sp[SH2][c], &He = sp[SHE][c], &Hep = sp[SHEP][c];
+    double &C = sp[SC][c], &Cp = sp[SCP][c], &CO = sp[SCO][c];
+    double &ne = nde[c], &nt = ndtot[c];
+    double pold = p, Hold = H, H2old = H2, Heold = He, Hepold = Hep, Cold = C, Cpold = Cp, COold = CO;
+    double T = U[5][c] / P.kb / (pold + Hold + H2old + Heold + Hepold);
+    Rates k = RATES(T, c);
+    double t1, t2, t3, om;
+    // H recombination & ionization by CR
+    t1 = k.kHrec * ne;
+    t2 = detmath::exp(-dt * (k.zeta + t1));
+    t3 = 1.0 / (k.zeta + t1);
+    om = Omexp(dt * (k.zeta + t1));
+    H = (t1 * Hold + k.zeta * Hold * t2 + t1 * pold * om) * t3;
+    p = (k.zeta * pold + t1 * pold * t2 + k.zeta * Hold * om) * t3;
+    Hold = H; pold = p; ne = p + Hep + Cp;
+    // He recombination & ionization by CR
+    t1 = k.kHerec * ne;
+    t2 = detmath::exp(-dt * (k.zeta + t1));
+    t3 = 1.0 / (k.zeta + t1);
+    om = Omexp(dt * (k.zeta + t1));
+    He = (t1 * Heold + k.zeta * Heold * t2 + t1 * Hepold * om) * t3;
+    Hep = (k.zeta * Hepold + t1 * Hepold * t2 + k.zeta * Heold * om) * t3;
+    Heold = He; Hepold = Hep; ne = p + Hep + Cp;
+    // H2 formation & dissociation by UV & electron collision
+    t1 = k.kH2ph + k.kH2de * ne;
+    t2 = t1 + 2.0 * k.kH2 * nt;
+    t3 = detmath::exp(-dt * t2);
+    om = Omexp(dt * t2);
+    H = (Hold + 2.0 * H2old * om) * t1 + 2.0 * k.kH2 * Hold * nt * t3;
+    H = H / t2;
+    H2 = (2.0 * H2old + Hold * om) * k.kH2 * nt + t1 * H2old * t3;
+    H2 = H2 / t2;
+    Hold = H; H2old = H2;
+    // H2 dissociation by H collision
+    t1 = Hold + 2.0 * H2old;
+    t2 = detmath::exp(-dt * t1 * k.kH2dH);
+    t3 = 1.0 / (Hold + 2.0 * H2old * t2);
+    H = Hold * t1 * t3;
+    H2 = H2old * t1 * t2 * t3;
+    Hold = H; H2old = H2;
+    // CO formation
+    t1 = detmath::exp(-dt * k.kCO * nt);
+    om = Omexp(dt * k.kCO * nt);
+    CO = COold + om * Cpold;
+    Cp = t1 * Cpold;
+    COold = CO; Cpold = Cp; ne = p + Hep + Cp;
+    // CO dissociation by UV & electron collision & H collision
+    t1 = detmath::exp(-dt * (k.kCOph + k.kCOde * ne + k.kCOdH * Hold));
+    om = Omexp(dt * (k.kCOph + k.kCOde * ne + k.kCOdH * Hold));
+    C = Cold + om * COold;
+    CO = t1 * COold;
+    Cold = C; COold = CO;
+    // C recombination & ionization by CR & UV
+    t1 = k.kCrec * ne;
+    t2 = detmath::exp(-dt * (k.kCi + t1));
+    t3 = 1.0 / (k.kCi + t1);
+    om = Omexp(dt * (k.kCi + t1));
+    C = (t1 * Cold + k.kCi * Cold * t2 + t1 * Cpold * om) * t3;
+    Cp = (k.kCi * Cpold + t1 * Cpold * t2 + k.kCi * Cold * om) * t3;
+    Cold = C; Cpold = Cp; ne = p + Hep + Cp;
+    // H, He, C ionization by e collision
+    H = Hold * detmath::exp(-dt * k.kHie * ne);
+    He = Heold * detmath::exp(-dt * k.kHeie * ne);
+    C = Cold * detmath::exp(-dt * k.kCie * ne);
+    om = Omexp(dt * k.kHie * ne); p = om * Hold + pold;
+    om = Omexp(dt * k.kHeie * ne); Hep = om * Heold + Hepold;
+    om = Omexp(dt * k.kCie * ne); Cp = om * Cold + Cpold;
+    Hold = H; Heold = He; Cold = C;
+    pold = p; Hepold = Hep; Cpold = Cp;
+    ne = p + Hep + Cp;
+    // H, He, C ionization by H or H2 or p collision
+    t1 = 1.0 / (1.0 + k.kHiH * dt * Hold);
+    H = Hold * t1;
+    p = pold + t1 * k.kHiH * dt * (Hold * Hold);
+    t1 = H + p + H2old;
+    He = Heold * detmath::exp(-dt * k.kHeiH * t1);
+    C = Cold * detmath::exp(-dt * k.kCiH * t1);
+    om = Omexp(dt * k.kHeiH * t1); Hep = om * Heold + Hepold;
+    om = Omexp(dt * k.kCiH * t1); Cp = om * Cold + Cpold;
+    Hold = H; Heold = He; Cold = C;
+    pold = p; Hepold = Hep; Cpold = Cp;
+    ne = p + Hep + Cp;
+    // H2 dissociation by He+ recombination
+    t1 = Hepold - H2old;
+    if (t1 >= 0.0) {
+      t3 = detmath::exp(-dt * k.kH2dHep * t1);
+      t2 = 1.0 / (Hepold - H2old * t3);
+      Hep = Hepold * t1 * t2;
+      H2 = H2old * t1 * t2 * t3;
+      t3 = Hepold * (1.0 - t1 * t2);
+      p = pold + t3;
+      H = Hold + t3;
+      He = Heold + t3;
+    } else {
+      t3 = detmath::exp(dt * k.kH2dHep * t1);
+      t2 = 1.0 / (Hepold * t3 - H2old);
+      Hep = Hepold * t1 * t2 * t3;
+      H2 = H2old * t1 * t2;
+      t3 = Hepold * (1.0 - t1 * t2 * t3);
+      p = pold + t3;
+      H = Hold + t3;
+      He = Heold + t3;
+    }
+    Hold = H; pold = p; H2old = H2;
+    Heold = He; Hepold = Hep;
+    // CO dissociation by He+ recombination
+    t1 = Hepold - COold;
+    if (t1 >= 0.0) {
+      t3 = detmath::exp(-dt * k.kCOdHep * t1);
+      t2 = 1.0 / (Hepold - COold * t3);
+      Hep = Hepold * t1 * t2;
+      CO = COold * t1 * t2 * t3;
+      t3 = Hepold * (1.0 - t1 * t2);
+      Cp = Cpold + t3;
+      He = Heold + t3;
+    } else {
+      t3 = detmath::exp(dt * k.kCOdHep * t1);
+      t2 = 1.0 / (Hepold * t3 - COold);
+      Hep = Hepold * t1 * t2 * t3;
+      CO = COold * t1 * t2;
+      t3 = Hepold * (1.0 - t1 * t2 * t3);
+      Cp = Cpold + t3;
+      He = Heold + t3;
+    }
+    H = fmax2(ndmin[SH], H);   // dmax1(ndHmin, ndH) (:2759-2766)
+    p = fmax2(ndmin[SP], p);
+    H2 = fmax2(ndmin[SH2], H2);
+    He = fmax2(ndmin[SHE], He);
+    Hep = fmax2(ndmin[SHEP], Hep);
+    C = fmax2(ndmin[SC], C);
+    Cp = fmax2(ndmin[SCP], Cp);
+    CO = fmax2(ndmin[SCO], CO);
+    ne = p + Hep + Cp;
+    nt = p + H + 2.0 * H2 + He + Hep;
+    U[1][c] = 1.0 * p + 1.0 * H + 2.0 * H2 + 4.0 * He + 4.0 * Hep;   // mH, mH2, mHe
+  }
+  void CHEM(double dt) {
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny; j++)
+        for (int i = 1; i <= Nx; i++) CHEM_cell(id(i, j, k), dt);
+  }
+  // nde, ndtot from the species (INITIA :471-474), cells 1..n+1
+  void init_chem_totals() {
+    for (int k = 1; k <= Nz + 1; k++)
+      for (int j = 1; j <= Ny + 1; j++)
+        for (int i = 1; i <= Nx + 1; i++) {
+          size_t c = id(i, j, k);
+          nde[c] = sp[SP][c] + sp[SHEP][c] + sp[SCP][c];
+          ndtot[c] = sp[SP][c] + sp[SH][c] + 2.0 * sp[SH2][c] + sp[SHE][c] + sp[SHEP][c];
+        }
+  }
   static double FcoolN(double T, double NN) {   // KI form, KIcool/1DMHDwCC3.f90:1166-1173
     double AbsL = 3.94656e1, T0 = 1.0e3;
     double Laml = 1.0e7 * detmath::exp(-1.184e5 / (T * T0 + 1.0e3));
@@ -827,12 +1112,13 @@ struct Mhd3D {
   }
 
   // IMC (:2898-2921) with the KI density NN of the cell
-  static void IMC(double &Pv, double n, double dt, double g1c, double NN, double kb) {
+  template <class Cool>
+  static void IMCf(double &Pv, double n, double dt, double g1c, double kb, Cool &&cool) {
     double Pu = 1.e10, Pd = 1.e-10, Pm = 1.e1, Pmold = -1.0;
     double nkbi = 1.0 / (kb * n);
     for (int kkk = 1; kkk <= 30; kkk++) {
       double T = Pm * nkbi;
-      double CooL = FcoolN(T, NN);
+      double CooL = cool(T);
       double fev = Pm + CooL * dt * g1c - Pv;
       double iud = fsign(1.0, fev);
       Pd = fmax2(-iud * Pm, Pd);
@@ -843,9 +1129,20 @@ struct Mhd3D {
     }
     Pv = Pm;
   }
+  static void IMC(double &Pv, double n, double dt, double g1c, double NN, double kb) {
+    IMCf(Pv, n, dt, g1c, kb, [&](double T) { return FcoolN(T, NN); });
+  }
+  // IMC of cell c with the cooling function of the run
+  void IMC_cell(double &Pv, double n, double dt, double g1c, size_t c) {
+    if (P.ifchem == 2) IMCf(Pv, n, dt, g1c, P.kb, [&](double T) { return FcoolSpecies(T, c); });
+    else IMC(Pv, n, dt, g1c, U[1][c] / 1.27, P.kb);
+  }
 
-  void SOURCE(double dt) {   // thermal branch ifthrm=2, :2477-2572
-    if (P.ifthrm != 2) return;
+  void SOURCE(double dt) {   // thermal branch ifthrm=2 (:2477-2572), then chemistry ifchem=2
+    if (P.ifthrm == 2) SOURCE_thermal(dt);
+    if (P.ifchem == 2) CHEM(dt);
+  }
+  void SOURCE_thermal(double dt) {
     fillU(1, 7, 1, 1); fillU(5, 7, 1, 1);                            // :2484
     fill_species(7, 1);                                              // :2486
     std::vector<double> Tn(ncell), Pn(ncell), Qx(ncell), Qy(ncell), Qz(ncell);
@@ -886,14 +1183,14 @@ struct Mhd3D {
           if (dt <= 0.2 * Pn[a] / (g1c * std::fabs(CooL))) {
             U[5][a] = U[5][a] - g1c * CooL * dt * 0.5;
           } else {
-            IMC(U[5][a], nimc(a), dt * 0.5, g1c, U[1][a] / 1.27, P.kb);
+            IMC_cell(U[5][a], nimc(a), dt * 0.5, g1c, a);
           }
         } else {
           if (dt <= 0.2 * Pn[a] / (g1c * std::fabs(CooL))) {
             U[5][a] = Pn[a] - g1c * CooL * dt;
           } else {
             double pv = Pn[a];
-            IMC(pv, nimc(a), dt, g1c, U[1][a] / 1.27, P.kb);
+            IMC_cell(pv, nimc(a), dt, g1c, a);
             U[5][a] = pv;
           }
         }
@@ -925,7 +1222,7 @@ struct Mhd3D {
     }
     return tCFL;
   }
-  double Stblty() {   // :2784-2822 with the KI Fcool
+  double Stblty() {   // :2784-2822 with the cooling function of the run
     double tLMT = P.tfinal;
     for (int k = 1; k <= Nz; k++) for (int j = 1; j <= Ny; j++) for (int i = 1; i <= Nx; i++) {
       size_t a = id(i, j, k);
@@ -1001,7 +1298,7 @@ struct Mhd3D {
 
 extern "C" {
 
-// params (doubles): nx,ny,nz, CFL,facdep,tfinal, bc[6], pmin,pmax,rmin, kb,Kcond, ifthrm, dissip
+// params (doubles): nx,ny,nz, CFL,facdep,tfinal, bc[6], pmin,pmax,rmin, kb,Kcond, ifthrm, dissip, ifchem
 void *o3d_create(const double *p) {
   Params P{};
   P.nx = (int)p[0]; P.ny = (int)p[1]; P.nz = (int)p[2];
@@ -1010,6 +1307,7 @@ void *o3d_create(const double *p) {
   P.pmin = p[12]; P.pmax = p[13]; P.rmin = p[14];
   P.kb = p[15]; P.Kcond = p[16];
   P.ifthrm = (int)p[17]; P.dissip = (int)p[18];
+  P.ifchem = (int)p[19];
   P.nspecies = 8;
   Mhd3D *m = new Mhd3D();
   m->init(P);
@@ -1029,6 +1327,7 @@ void o3d_upload(void *h, const double *U, const double *sp, const double *coords
     memcpy(m->xc[d].data(), coords + off, n * sizeof(double)); off += n;
     memcpy(m->dxc[d].data(), coords + off, n * sizeof(double)); off += n;
   }
+  m->init_chem_totals();
   m->CC4();
 }
 

@@ -107,7 +107,7 @@ class Oracle3D:
     def __init__(self, params):
         p = params
         v = [p.nx, p.ny, p.nz, p.cfl, p.facdep, p.tfinal, *p.bc, p.pmin, p.pmax, p.rmin,
-             p.kb, p.kcond, p.ifthrm, p.dissip]
+             p.kb, p.kcond, p.ifthrm, p.dissip, getattr(p, "ifchem", 0)]
         self.params = p
         self.shape = (p.nz + 4, p.ny + 4, p.nx + 4)
         self.h = lib().o3d_create(_ptr(np.array(v, dtype=np.float64)))

@@ -45,6 +45,11 @@ def test_create_rejects_bad_arguments():
     p = native.params_struct(MhdParams(2, 8, 8))
     assert L.mhd_create(ctypes.byref(p), ctypes.byref(h)) == 1   # grid too small
     assert L.mhd_create(None, ctypes.byref(h)) == 1
+    p = native.params_struct(MhdParams(8, 8, 8, ifchem=1))
+    assert L.mhd_create(ctypes.byref(p), ctypes.byref(h)) == 1   # ifchem is 0 or 2
+    p = native.params_struct(MhdParams(8, 8, 8, ifchem=2), precision=native.PREC_FP32,
+                             cooling=native.COOL_SURROGATE)
+    assert L.mhd_create(ctypes.byref(p), ctypes.byref(h)) == 1   # surrogate is KI-only
 
 
 def test_create_without_gpu_reports_no_device():
