@@ -8,20 +8,38 @@
 #include "mhd_sweep_impl.cuh"
 
 namespace mhd {
-// Sweep launch shape: 288 threads (9 warps) and two CTAs per SM.  Every
-// phase of the kernel loops over n, n+1 or n+2 positions of P pencils;
-// with 288 threads all three counts take the same number of trips for the
-// pencil lengths used here, so no phase runs a nearly empty last trip.
-// P pencils per CTA are chosen so that two CTAs fit in the SM's shared memory.
-constexpr int kSweepThreads = 288;
-constexpr int kSweepMinBlocks = 2;
-constexpr size_t kSweepSmemPerCta = 113 * 1024;
+// Sweep launch shape: two CTAs per SM (the pencil buffers of P = 4 pencils
+// of 256 cells take 92 KB), 384 threads for the x sweep and 576 for the y
+// and z sweeps.  Measured at 256^3 on GB300 (ms per sweep x / y / z):
+// 288 threads 2.91 / 3.57 / 3.70; 384: 2.36 / 2.96 / 3.17; 576: 2.42 /
+// 2.68 / 3.13.  More warps per SM hide the shared-memory and global-load
+// latency of the phases; the x sweep's contiguous rows need fewer.  The
+// register budget this leaves (80 / 56 per thread) holds the kernel without
+// spills because the global-load phases are not unrolled (see
+// MHD_SWEEP_GLOBAL_UNROLL).  The thread counts can be overridden at build
+// time for experiments.
+#ifndef MHD_SWEEP_THREADS_X
+#define MHD_SWEEP_THREADS_X 384
+#endif
+#ifndef MHD_SWEEP_THREADS_YZ
+#define MHD_SWEEP_THREADS_YZ 576
+#endif
+#ifndef MHD_SWEEP_MIN_BLOCKS
+#define MHD_SWEEP_MIN_BLOCKS 2
+#endif
+#ifndef MHD_SWEEP_MAX_PENCILS
+#define MHD_SWEEP_MAX_PENCILS 4
+#endif
+template <int DIR>
+constexpr int sweep_threads() { return DIR == 0 ? MHD_SWEEP_THREADS_X : MHD_SWEEP_THREADS_YZ; }
+constexpr int kSweepMinBlocks = MHD_SWEEP_MIN_BLOCKS;
+constexpr size_t kSweepSmemPerCta = (227 * 1024) / MHD_SWEEP_MIN_BLOCKS - 1024;
 
 template <int DIR, int P>
 static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
   const Grid &g = a.g;
   size_t smem = sweep32_smem_bytes(g.n[DIR], P);
-  auto k = sweep32_kernel<DIR, P, kSweepThreads, kSweepMinBlocks>;
+  auto k = sweep32_kernel<DIR, P, sweep_threads<DIR>(), kSweepMinBlocks>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // x sweep: P adjacent y rows per CTA; y and z sweeps: P adjacent x columns
@@ -31,7 +49,7 @@ static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
   if (DIR == 0) grid = dim3(g.n[1] / P, g.n[2]);
   else if (DIR == 1) grid = dim3(xgroups, g.n[2]);
   else grid = dim3(xgroups, g.n[1]);
-  k<<<grid, kSweepThreads, smem, s>>>(a);
+  k<<<grid, sweep_threads<DIR>(), smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -39,7 +57,8 @@ template <int DIR>
 static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
   // the x sweep needs P to divide ny; the y and z sweeps pad their groups
   const int nb = (DIR == 0) ? a.g.n[1] : 4;
-  if (nb % 4 == 0 && sweep32_smem_bytes(a.g.n[DIR], 4) <= kSweepSmemPerCta) return launch32<DIR, 4>(a, s);
+  if (MHD_SWEEP_MAX_PENCILS >= 4 && nb % 4 == 0 && sweep32_smem_bytes(a.g.n[DIR], 4) <= kSweepSmemPerCta)
+    return launch32<DIR, 4>(a, s);
   if (nb % 2 == 0 && sweep32_smem_bytes(a.g.n[DIR], 2) <= kSweepSmemPerCta) return launch32<DIR, 2>(a, s);
   if (sweep32_smem_bytes(a.g.n[DIR], 1) > 227 * 1024) return cudaErrorInvalidValue;
   return launch32<DIR, 1>(a, s);
