@@ -66,8 +66,10 @@ enum { C_DX = 0, C_RDX, C_X2, C_COUNT };
 // shared header): the species sum H+p+He+He+ and the remap's T switch
 enum : int { IN_SSUM = 100, IN_SW = 101 };   // FP32 dx(i), 1/(x(i)-x(i-1)), x(i+1)-x(i-1)
 
-__host__ __device__ inline size_t sweep32_smem_bytes(int n, int P) {
-  size_t L = (size_t)n + 4;
+// Shared memory of one CTA: the buffers hold LS >= n+4 positions each (LS =
+// n+4 when the stride is a run-time value).
+__host__ __device__ inline size_t sweep32_smem_bytes(int n, int P, int LS = 0) {
+  size_t L = LS > 0 ? (size_t)LS : (size_t)n + 4;
   return (L * P * F_COUNT + L * C_COUNT) * sizeof(float);
 }
 
@@ -102,6 +104,21 @@ constexpr int kSmemUnroll = MHD_SWEEP_SMEM_UNROLL;
 #define MHD_SWEEP_GLOBAL_UNROLL 1
 #endif
 constexpr int kGlobalUnroll = MHD_SWEEP_GLOBAL_UNROLL;
+// Bit d set: the load phase of the direction-d sweep issues all loads of a
+// position in one pass; clear: one pass per field group.
+#ifndef MHD_SWEEP_MERGE_LOADS
+#define MHD_SWEEP_MERGE_LOADS 1
+#endif
+constexpr int kMergeLoads = MHD_SWEEP_MERGE_LOADS;
+// Bit d set: the finishing phases of the direction-d sweep load every FP64
+// value of a position before using any; clear: each value where it is used.
+// Measured at 256^3 (ms, x / y / z): hoisted 2.16 / 2.41 / 3.21, in place
+// 2.23 / 2.47 / 3.01 -- the z sweep, whose pencils cross a page every few
+// cells, is slower with more loads in flight.
+#ifndef MHD_SWEEP_HOIST_LOADS
+#define MHD_SWEEP_HOIST_LOADS 3
+#endif
+constexpr int kHoistLoads = MHD_SWEEP_HOIST_LOADS;
 
 // The P pencils of a CTA, addressed without a per-pencil table: pencil p
 // starts p transverse strides after pencil 0 (adjacent y rows for the x
@@ -140,13 +157,18 @@ struct PencilRun {
   }
 };
 
-template <int DIR, int P, int NT, int MINB>
+// LS > 0: every pencil buffer is LS positions long, a compile-time stride,
+// so each shared-memory access is one load or store at a constant offset
+// from a per-item base address; LS = 0: the stride is n+4, computed at run
+// time (any length).
+template <int DIR, int P, int NT, int MINB, int LS>
 __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   extern __shared__ float smf[];
   const Grid &g = A.g;
   const int N = g.n[DIR];
   const int L = N + 4;
-  const int LP = L * P;
+  const int LB = LS > 0 ? LS : L;   // buffer stride
+  const int LP = LB * P;
   float *cf = smf + (size_t)F_COUNT * LP;
   const float dt = (float)A.dt;
   const float facdep = (float)A.ph.facdep;
@@ -156,7 +178,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   PencilRun<DIR, P> pc(g);
   constexpr int C1 = (DIR + 1) % 3, C2 = (DIR + 2) % 3;
   auto Fb = [&](int b, int i, int p) -> float & { return smf[b * LP + (i + 1) * P + p]; };
-  auto cx = [&](int c, int i) -> float { return cf[c * L + i + 1]; };
+  auto cx = [&](int c, int i) -> float { return cf[c * LB + i + 1]; };
   const bool perL = g.bcl[DIR] != 1, perR = g.bcr[DIR] != 1;
   // BC=4 inflow sides of the x sweep (the other sweeps never exchange in x)
   const bool inL = DIR == 0 && A.ph.in.on[0], inR = DIR == 0 && A.ph.in.on[1];
@@ -223,38 +245,26 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   // ------------------------------------------------ A: load (+ ghosts)
   for (int t = tid; t < L; t += NT) {
     const double *xe = g.x[DIR];
-    cf[C_DX * L + t] = d2f(g.dx[DIR][t]);
-    cf[C_RDX * L + t] = d2f(rdx[t]);
-    cf[C_X2 * L + t] = (t >= 1 && t + 1 < L) ? d2f(xe[t + 1] - xe[t - 1]) : 1.0f;
+    cf[C_DX * LB + t] = d2f(g.dx[DIR][t]);
+    cf[C_RDX * LB + t] = d2f(rdx[t]);
+    cf[C_X2 * LB + t] = (t >= 1 && t + 1 < L) ? d2f(xe[t + 1] - xe[t - 1]) : 1.0f;
   }
-  unrolled<NT, kGlobalUnroll>(L * P, [&](int t) {
-    int i = t / P - 1, p = t % P;
-    long long a = pc.at(p, i);
-    Fb(F_B1, i, p) = d2f(__ldg(A.f.bcc[C1] + a));
-    Fb(F_B2, i, p) = d2f(__ldg(A.f.bcc[C2] + a));
-  });
-  unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
-    int i = 1 + t / P, p = t % P;
-    long long a = pc.at(p, i);
-    double u0 = __ldg(A.f.U[0] + a), un = __ldg(A.f.U[1 + DIR] + a), u1 = __ldg(A.f.U[1 + C1] + a),
-           u2 = __ldg(A.f.U[1 + C2] + a), u4 = __ldg(A.f.U[4] + a);
+  // the interior state of position i: flow variables ...
+  auto load_flow = [&](int i, int p, double u0, double un, double u1, double u2, double u4) {
     put(F_R, i, p, d2f(u0), IN_RHO);
     put(F_VN, i, p, d2f(un), IN_V1);
     put(F_VT1, i, p, d2f(u1), IN_V2);
     put(F_VT2, i, p, d2f(u2), IN_V3);
-    float pr = d2f(u4);
+    const float pr = d2f(u4);
     put(F_P, i, p, pr, IN_P);
     put_ghosts(F_T, i, p, pr, IN_P);
-  });
-  unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
-    int i = 1 + t / P, p = t % P;
-    long long a = pc.at(p, i);
-    double s0 = __ldg(A.f.sp[0] + a), s1 = __ldg(A.f.sp[1] + a), s2 = __ldg(A.f.sp[2] + a),
-           s3 = __ldg(A.f.sp[3] + a), s4 = __ldg(A.f.sp[4] + a), bn = __ldg(A.f.U[5 + DIR] + a);
+  };
+  // ... and species sums and the face-normal field (the face-field exchange
+  // rewrites the ghost faces, incl. face n+1; an inflow side copies face 1
+  // into faces -1, 0 and face n+1 into n+2)
+  auto load_species_face = [&](int i, int p, double s0, double s1, double s2, double s3, double s4, double bn) {
     put(F_S, i, p, d2f(s0) + d2f(s1) + d2f(s3) + d2f(s4), IN_SSUM);
     put(F_H2, i, p, d2f(s2), IN_SPEC + 2);
-    // the face-field exchange rewrites the ghost faces (incl. face n+1; an
-    // inflow side copies face 1 into faces -1, 0 and face n+1 into n+2)
     put(F_BN, i, p, d2f(bn), IN_BXF);
     if (pc.active(p)) for_ghosts(i, [&](int gi) { A.f.U[5 + DIR][pc.at(p, gi)] = bn; });
     if (inL && i == 1)
@@ -265,7 +275,54 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
       Fb(F_BN, N + 2, p) = d2f(bn1);
       A.f.U[5 + DIR][pc.at(p, N + 2)] = bn1;
     }
-  });
+  };
+  if ((kMergeLoads >> DIR) & 1) {
+    // one pass over positions -1..n+2: the transverse cell-centred field of
+    // every position and the state of the interior cells, all loads of a
+    // position issued together so that a thread waits for memory once per
+    // position rather than once per field group
+    unrolled<NT, kGlobalUnroll>(L * P, [&](int t) {
+      const int i = t / P - 1, p = t % P;
+      const long long a = pc.at(p, i);
+      const double c1 = __ldg(A.f.bcc[C1] + a), c2 = __ldg(A.f.bcc[C2] + a);
+      const bool inside = i >= 1 && i <= N;
+      double u0 = 0.0, un = 0.0, u1 = 0.0, u2 = 0.0, u4 = 0.0;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0, bn = 0.0;
+      if (inside) {
+        u0 = __ldg(A.f.U[0] + a); un = __ldg(A.f.U[1 + DIR] + a); u1 = __ldg(A.f.U[1 + C1] + a);
+        u2 = __ldg(A.f.U[1 + C2] + a); u4 = __ldg(A.f.U[4] + a);
+        s0 = __ldg(A.f.sp[0] + a); s1 = __ldg(A.f.sp[1] + a); s2 = __ldg(A.f.sp[2] + a);
+        s3 = __ldg(A.f.sp[3] + a); s4 = __ldg(A.f.sp[4] + a); bn = __ldg(A.f.U[5 + DIR] + a);
+      }
+      Fb(F_B1, i, p) = d2f(c1);
+      Fb(F_B2, i, p) = d2f(c2);
+      if (!inside) return;
+      load_flow(i, p, u0, un, u1, u2, u4);
+      load_species_face(i, p, s0, s1, s2, s3, s4, bn);
+    });
+  } else {
+    // three passes: transverse field (-1..n+2), flow state, species + face field
+    unrolled<NT, kGlobalUnroll>(L * P, [&](int t) {
+      const int i = t / P - 1, p = t % P;
+      const long long a = pc.at(p, i);
+      Fb(F_B1, i, p) = d2f(__ldg(A.f.bcc[C1] + a));
+      Fb(F_B2, i, p) = d2f(__ldg(A.f.bcc[C2] + a));
+    });
+    unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
+      const int i = 1 + t / P, p = t % P;
+      const long long a = pc.at(p, i);
+      const double u0 = __ldg(A.f.U[0] + a), un = __ldg(A.f.U[1 + DIR] + a), u1 = __ldg(A.f.U[1 + C1] + a),
+                   u2 = __ldg(A.f.U[1 + C2] + a), u4 = __ldg(A.f.U[4] + a);
+      load_flow(i, p, u0, un, u1, u2, u4);
+    });
+    unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
+      const int i = 1 + t / P, p = t % P;
+      const long long a = pc.at(p, i);
+      const double s0 = __ldg(A.f.sp[0] + a), s1 = __ldg(A.f.sp[1] + a), s2 = __ldg(A.f.sp[2] + a),
+                   s3 = __ldg(A.f.sp[3] + a), s4 = __ldg(A.f.sp[4] + a), bn = __ldg(A.f.U[5 + DIR] + a);
+      load_species_face(i, p, s0, s1, s2, s3, s4, bn);
+    });
+  }
   if (inL || inR) {
     const int bl[8] = {F_R, F_VN, F_VT1, F_VT2, F_P, F_T, F_S, F_H2};
     const int rl[8] = {IN_RHO, IN_V1, IN_V2, IN_V3, IN_P, IN_P, IN_SSUM, IN_SPEC + 2};
@@ -440,9 +497,22 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     int i = 1 + t / P, p = t % P;
     const bool act = pc.active(p);
     long long a = pc.at(p, i);
+    // FP64 inputs of the position: loaded here together (hoisted) or by
+    // get() where they are used
+    const double *src[8] = {A.f.U[0], A.f.U[1 + DIR], A.f.U[1 + C1], A.f.U[1 + C2],
+                            A.f.sp[0], A.f.sp[1], A.f.sp[2], A.f.sp[3]};
+    double pre[8];
+    if constexpr (((kHoistLoads >> DIR) & 1) != 0) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) pre[q] = __ldg(src[q] + a);
+    }
+    auto get = [&](int q) -> double {
+      if constexpr (((kHoistLoads >> DIR) & 1) != 0) return pre[q];
+      else return __ldg(src[q] + a);
+    };
+    const double r0 = get(0), rdxi = rdx[i + 1];
     const float rw = cx(C_RDX, i), dxl = Fb(F_DXL, i, p);
-    double r0 = __ldg(A.f.U[0] + a);
-    double r1 = r0 + rdx[i + 1] * (f2d(Fb(F_G2, i, p)) - f2d(Fb(F_G2, i - 1, p)));
+    double r1 = r0 + rdxi * (f2d(Fb(F_G2, i, p)) - f2d(Fb(F_G2, i - 1, p)));
     float rf = d2f(r1);
     float drho = (Fb(F_G2, i, p) - Fb(F_G2, i - 1, p)) * rw;
     if (!(rf > rfloor_f)) {   // density floor (:1293-1296)
@@ -453,17 +523,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     if (act) A.f.U[0][a] = r1;
     Fb(F_R, i, p) = rf;
     const float irf = fdiv(1.0f, rf);
-    auto mom = [&](int comp, int fb, float inc) {
-      double v0 = __ldg(A.f.U[1 + comp] + a);
+    auto mom = [&](int comp, double v0, int fb, float inc) {
       float v0f = d2f(v0);
       float dM = (inc + Fb(fb, i, p) - Fb(fb, i - 1, p)) * rw;
       float dv = (dM - drho * v0f) * irf;
       if (act) A.f.U[1 + comp][a] = v0 + f2d(dv);
       return v0f + dv;
     };
-    float vn = mom(DIR, F_G3, Fb(F_IMN, i, p));
-    float v1 = mom(C1, F_G4, Fb(F_G0, i, p));
-    float v2 = mom(C2, F_P, Fb(F_G1, i, p));
+    float vn = mom(DIR, get(1), F_G3, Fb(F_IMN, i, p));
+    float v1 = mom(C1, get(2), F_G4, Fb(F_G0, i, p));
+    float v2 = mom(C2, get(3), F_P, Fb(F_G1, i, p));
     Fb(F_VN, i, p) = vn;
     Fb(F_VT1, i, p) = v1;
     Fb(F_VT2, i, p) = v2;
@@ -473,10 +542,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     if (act && (!(vn == vn) || !(v1 == v1) || !(v2 == v2) || !(rf < 3e38f))) flag(A.err, ERRB_NONFINITE);
     // species 0..3: content n dx is unchanged by the Lagrangian step
     const float w = cx(C_DX, i) * fdiv(1.0f, dxl);
-    put(F_G0, i, p, d2f(__ldg(A.f.sp[0] + a)) * w, IN_SPEC + 0);
-    put(F_G1, i, p, d2f(__ldg(A.f.sp[1] + a)) * w, IN_SPEC + 1);
-    put(F_IMN, i, p, d2f(__ldg(A.f.sp[2] + a)) * w, IN_SPEC + 2);
-    put(F_H2, i, p, d2f(__ldg(A.f.sp[3] + a)) * w, IN_SPEC + 3);
+    put(F_G0, i, p, d2f(get(4)) * w, IN_SPEC + 0);
+    put(F_G1, i, p, d2f(get(5)) * w, IN_SPEC + 1);
+    put(F_IMN, i, p, d2f(get(6)) * w, IN_SPEC + 2);
+    put(F_H2, i, p, d2f(get(7)) * w, IN_SPEC + 3);
   });
   if (inL || inR) {
     const int bl[4] = {F_G0, F_G1, F_IMN, F_H2};
@@ -495,9 +564,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   });
   __syncthreads();
   // ------------------------- K: species 0-3 finish, 4-7 reconstruction
-  auto species_new = [&](int s, long long a, int i, int p, int fb, bool act) {
+  auto species_new = [&](int s, double n0, long long a, int i, int p, int fb, bool act) {
     const float rw = cx(C_RDX, i);
-    double n0 = __ldg(A.f.sp[s] + a);
     float dn = (Fb(fb, i, p) - Fb(fb, i - 1, p)) * rw;
     float nf = d2f(n0) + dn;   // remapped value, before the floor
     const double mn = A.ph.ndmin[s];
@@ -508,15 +576,24 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     int i = 1 + t / P, p = t % P;
     const bool act = pc.active(p);
     long long a = pc.at(p, i);
-    float S = species_new(0, a, i, p, F_G2, act) + species_new(1, a, i, p, F_G3, act) +
-              species_new(3, a, i, p, F_P, act);
-    float H2 = species_new(2, a, i, p, F_G4, act);
+    double pre[8];
+    if constexpr (((kHoistLoads >> DIR) & 1) != 0) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) pre[q] = __ldg(A.f.sp[q] + a);
+    }
+    auto get = [&](int q) -> double {
+      if constexpr (((kHoistLoads >> DIR) & 1) != 0) return pre[q];
+      else return __ldg(A.f.sp[q] + a);
+    };
+    float S = species_new(0, get(0), a, i, p, F_G2, act) + species_new(1, get(1), a, i, p, F_G3, act) +
+              species_new(3, get(3), a, i, p, F_P, act);
+    float H2 = species_new(2, get(2), a, i, p, F_G4, act);
     Fb(F_S, i, p) = S;
     const float w = cx(C_DX, i) * fdiv(1.0f, Fb(F_DXL, i, p));
-    put(F_G0, i, p, d2f(__ldg(A.f.sp[4] + a)) * w, IN_SPEC + 4);
-    put(F_G1, i, p, d2f(__ldg(A.f.sp[5] + a)) * w, IN_SPEC + 5);
-    put(F_IMN, i, p, d2f(__ldg(A.f.sp[6] + a)) * w, IN_SPEC + 6);
-    put(F_PA, i, p, d2f(__ldg(A.f.sp[7] + a)) * w, IN_SPEC + 7);
+    put(F_G0, i, p, d2f(get(4)) * w, IN_SPEC + 4);
+    put(F_G1, i, p, d2f(get(5)) * w, IN_SPEC + 5);
+    put(F_IMN, i, p, d2f(get(6)) * w, IN_SPEC + 6);
+    put(F_PA, i, p, d2f(get(7)) * w, IN_SPEC + 7);
     Fb(F_H2, i, p) = H2;
   });
   if (inL || inR) {
@@ -541,15 +618,25 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     int i = 1 + t / P, p = t % P;
     const bool act = pc.active(p);
     long long a = pc.at(p, i);
-    float S = Fb(F_S, i, p) + species_new(4, a, i, p, F_G2, act);
-    species_new(5, a, i, p, F_G3, act);
-    species_new(6, a, i, p, F_G4, act);
-    species_new(7, a, i, p, F_P, act);
+    const double *src[5] = {A.f.sp[4], A.f.sp[5], A.f.sp[6], A.f.sp[7], A.f.bcc[DIR]};
+    double pre[5];
+    if constexpr (((kHoistLoads >> DIR) & 1) != 0) {
+#pragma unroll
+      for (int q = 0; q < 5; q++) pre[q] = __ldg(src[q] + a);
+    }
+    auto get = [&](int q) -> double {
+      if constexpr (((kHoistLoads >> DIR) & 1) != 0) return pre[q];
+      else return __ldg(src[q] + a);
+    };
+    float S = Fb(F_S, i, p) + species_new(4, get(0), a, i, p, F_G2, act);
+    species_new(5, get(1), a, i, p, F_G3, act);
+    species_new(6, get(2), a, i, p, F_G4, act);
+    species_new(7, get(3), a, i, p, F_P, act);
     float H2 = Fb(F_H2, i, p);
     float g1 = fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
     float rf = Fb(F_R, i, p), vn = Fb(F_VN, i, p), v1 = Fb(F_VT1, i, p), v2 = Fb(F_VT2, i, p);
     float ekin = 0.5f * (vn * vn + v1 * v1 + v2 * v2) * rf;
-    float bn = d2f(__ldg(A.f.bcc[DIR] + a)), l1 = Fb(F_B1, i, p), l2 = Fb(F_B2, i, p);
+    float bn = d2f(get(4)), l1 = Fb(F_B1, i, p), l2 = Fb(F_B2, i, p);
     float emag = 0.5f * (bn * bn + l1 * l1 + l2 * l2);
     float pr = (Fb(F_T, i, p) - ekin - emag) * g1;
     pr = fminf(pmax, fmaxf(pmin, pr));
