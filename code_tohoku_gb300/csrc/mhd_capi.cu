@@ -35,6 +35,7 @@ struct mhd_handle {
   // velocities, face B, rho, T switch and EMFs for CT) and FP32 widths
   float *fblock = nullptr;
   float *temp32 = nullptr;
+  int *stiff_list = nullptr;             // SOURCE's stiff cells (FP32 form with a surrogate)
   float *vf32[3] = {nullptr, nullptr, nullptr};
   float *bf32[3] = {nullptr, nullptr, nullptr};
   float *rn32 = nullptr, *sw32 = nullptr;
@@ -44,7 +45,8 @@ struct mhd_handle {
   bool inflow_set = false;
   double *divv = nullptr;
   double *diag_part = nullptr;
-  unsigned long long *dtred = nullptr;   // [0] tCFL, [1] tLMT bits, [2] IMC, [3] surrogate, [4] fallback
+  unsigned long long *dtred = nullptr;   // [0] tCFL, [1] tLMT bits, [2] IMC, [3] surrogate, [4] fallback,
+                                         // [5] stiff-cell count
   float *sur_master = nullptr;           // FP32 surrogate parameters (device)
   SurNet *sur_net = nullptr;             // packed BF16 network (device)
   float sur_tol = 1e-3f;
@@ -205,7 +207,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   }
   h->own_stream = true;
   if (p->precision == MHD_PREC_FP32) {
-    const size_t nf = 12;
+    const size_t nf = 13;   // 12 FP32 arrays + the stiff-cell list of SOURCE
     size_t fbytes = nf * (size_t)g.ncell * sizeof(float);
     if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess) {
       cudaGetLastError();
@@ -219,6 +221,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     h->rn32 = fq; fq += g.ncell;
     h->sw32 = fq; fq += g.ncell;
     for (int c = 0; c < 3; c++) { h->emf32[c] = fq; fq += g.ncell; }
+    h->stiff_list = reinterpret_cast<int *>(fq); fq += g.ncell;
     cudaMemsetAsync(h->fblock, 0, fbytes, h->stream);
   }
   cudaMemsetAsync(h->block, 0, bytes, h->stream);
@@ -379,13 +382,18 @@ int source_thermal(mhd_handle *h, double dt) {
     a.W = (h->p.cooling == MHD_COOL_SURROGATE) ? h->sur_net : nullptr;
     a.tol = h->sur_tol;
     a.T = h->temp32;
+    a.stiff_list = h->stiff_list; a.stiff_count = h->dtred + 5;
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
+    // with a surrogate, source_fp32 launches a second (stiff-cell) kernel
+    const int extra = (a.W && h->ph.ifchem != 2) ? 1 : 0;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
     CK(source_fp32(a, h->stream));
+    h->launches += extra;
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
     CK(source_fp32(a, h->stream));
+    h->launches += extra;
     return MHD_OK;
   }
   SourceArgs a{};

@@ -135,7 +135,28 @@ cudaError_t chem_step_fp32(const Grid &g, const Phys &ph, const Fields &f, doubl
 
 cudaError_t source_fp32(const Source32Args &a, cudaStream_t s) {
   long long n = (long long)a.g.n[0] * a.g.n[1] * a.g.n[2];
-  source32_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(a);
+  const unsigned nb = (unsigned)((n + 127) / 128);
+  // the species cooling (ifchem = 2) runs without a surrogate (the network
+  // models the KI function only; mhd_create refuses the combination)
+  if (a.ph.ifchem == 2) {
+    source32_kernel<true, false><<<nb, 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  if (a.W == nullptr) {
+    source32_kernel<false, false><<<nb, 128, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  // with a surrogate: explicit cells here, stiff cells listed and solved by
+  // a second pass over whole warps of them
+  if (!a.stiff_list || !a.stiff_count) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(a.stiff_count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  source32_kernel<false, true><<<(unsigned)((n + kSourceDeferThreads - 1) / kSourceDeferThreads),
+                                 kSourceDeferThreads, 0, s>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const unsigned ns = (unsigned)min((long long)nb, 152LL * 16);
+  source32_stiff_kernel<<<ns, 128, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -62,6 +62,8 @@ struct Source32Args {
   unsigned long long *fb_count;    // surrogate rejected -> bisection
   const SurNet *W;                 // surrogate network (null: exact only)
   float tol;                       // residual tolerance for accepting it
+  int *stiff_list;                 // with a surrogate: cells left to the stiff pass
+  unsigned long long *stiff_count; // their number (zeroed before each pass)
 };
 
 }  // namespace mhd
@@ -80,109 +82,204 @@ __global__ void __launch_bounds__(256) temp32_kernel(long long ncell, Fields f, 
   T[t] = __fdividef(d2f(pin[t]), kb * n);
 }
 
-// One pass of the chosen-form SOURCE for one cell (thread per cell).  The
-// only FP64 operation is p_new = base + dp; conversions are integer ones.
-__global__ void __launch_bounds__(128) source32_kernel(Source32Args A) {
+// block size of the pass that defers stiff cells (one list append per block)
+constexpr int kSourceDeferThreads = 512;
+
+// One pass of the chosen-form SOURCE for one cell: the quantities of the
+// cell (source32_prep) and the pressure update from the cooling increment
+// (source32_finish).  The only FP64 operation is p_new = base + dp;
+// conversions are integer ones.
+template <bool CHEM>
+struct Cell32 {
+  long long a;
+  float T0, div, g1, NN, nimc, nkbi, dts, basef, CooL, dx0;
+  double base;
+  bool stiff;
+  CellSpecies<float> cs;
+};
+
+template <bool CHEM>
+__device__ __forceinline__ Cell32<CHEM> source32_prep(const Source32Args &A, long long t) {
   const Grid &g = A.g;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  bool valid = t < (long long)nx * ny * nz;
-  long long tt = valid ? t : 0;
-  int i = 1 + (int)(tt % nx);
-  int j = 1 + (int)((tt / nx) % ny);
-  int k = 1 + (int)(tt / ((long long)nx * ny));
-  long long a = gidx(g, i, j, k);
+  const int nx = g.n[0], ny = g.n[1];
+  const int i = 1 + (int)(t % nx);
+  const int j = 1 + (int)((t / nx) % ny);
+  const int k = 1 + (int)(t / ((long long)nx * ny));
+  Cell32<CHEM> c;
+  const long long a = gidx(g, i, j, k);
+  c.a = a;
   const float kb = d2f(A.ph.kb), Kc = d2f(A.ph.kcond);
   const float dt = d2f(A.dt);
   const Fields &f = A.f;
   const float *T = A.T;
   const float *dx = g.dxf[0], *dy = g.dxf[1], *dz = g.dxf[2];
-  long long sy = g.st[1], sz = g.st[2];
-  float T0 = T[a];
+  const long long sy = g.st[1], sz = g.st[2];
+  const float T0 = T[a];
   auto flux = [&](float Tl, float Tu, float dl, float du) {
     float rdu = __fdividef(1.0f, dl + du);
     float rt = sqrtf((dl * Tu + du * Tl) * rdu);
     return Kc * fminf(rt, 3.873f) * (Tu - Tl) * 2.0f * rdu;
   };
-  float dxm = dx[i], dx0 = dx[i + 1], dxp = dx[i + 2];
-  float dym = dy[j], dy0 = dy[j + 1], dyp = dy[j + 2];
-  float dzm = dz[k], dz0 = dz[k + 1], dzp = dz[k + 2];
-  float div = __fdividef(flux(T0, T[a + 1], dx0, dxp) - flux(T[a - 1], T0, dxm, dx0), dx0) +
-              __fdividef(flux(T0, T[a + sy], dy0, dyp) - flux(T[a - sy], T0, dym, dy0), dy0) +
-              __fdividef(flux(T0, T[a + sz], dz0, dzp) - flux(T[a - sz], T0, dzm, dz0), dz0);
-  float H = d2f(f.sp[0][a]), pr = d2f(f.sp[1][a]), H2 = d2f(f.sp[2][a]), He = d2f(f.sp[3][a]),
-        Hep = d2f(f.sp[4][a]);
-  float g1 = __fdividef(2.0f * (H + pr + He + Hep) + 2.0f * H2, 3.0f * (H + pr + He + Hep) + 5.0f * H2);
-  float NN = d2f(f.U[0][a]) * (1.0f / 1.27f);
+  const float dxm = dx[i], dx0 = dx[i + 1], dxp = dx[i + 2];
+  const float dym = dy[j], dy0 = dy[j + 1], dyp = dy[j + 2];
+  const float dzm = dz[k], dz0 = dz[k + 1], dzp = dz[k + 2];
+  c.div = __fdividef(flux(T0, T[a + 1], dx0, dxp) - flux(T[a - 1], T0, dxm, dx0), dx0) +
+          __fdividef(flux(T0, T[a + sy], dy0, dyp) - flux(T[a - sy], T0, dym, dy0), dy0) +
+          __fdividef(flux(T0, T[a + sz], dz0, dzp) - flux(T[a - sz], T0, dzm, dz0), dz0);
+  const float H = d2f(f.sp[0][a]), pr = d2f(f.sp[1][a]), H2 = d2f(f.sp[2][a]), He = d2f(f.sp[3][a]),
+              Hep = d2f(f.sp[4][a]);
+  c.g1 = __fdividef(2.0f * (H + pr + He + Hep) + 2.0f * H2, 3.0f * (H + pr + He + Hep) + 5.0f * H2);
+  c.NN = d2f(f.U[0][a]) * (1.0f / 1.27f);
   // the cooling function of the run: KI, or the species form (ifchem = 2)
-  const bool chem = A.ph.ifchem == 2;
-  CellSpecies<float> cs{};
-  if (chem) cs = cell_species<float>(f, a, [](double v) { return d2f(v); });
-  auto cool = [&](float T) { return chem ? fcool_species<float>(T, cs) : fcool_ki(T, NN); };
-  float CooL = cool(T0);
-  double Pn = A.pold[a];
-  float Pnf = d2f(Pn);
-  float h = (A.pass == 0) ? 0.5f : 1.0f;          // predictor: half of dt
-  float dts = dt * h;
-  double base = (A.pass == 0) ? A.pin[a] : Pn;     // p the cooling acts on
-  float basef = (A.pass == 0) ? d2f(base) : Pnf;
-  bool stiff = valid && !(dt <= 0.2f * Pnf / (g1 * fabsf(CooL)));
-  float dp_cool = 0.0f;
-  bool need_imc = stiff;
-  float nimc = H + pr + He + Hep + H2;
-  float nkbi = __fdividef(1.0f, kb * nimc);
-  float Tb = basef * nkbi;                         // temperature the implicit solve starts from
-  if (A.W) {
-    // surrogate: inputs log10 N, log10 T, log10(dts / t_cool) with
-    // t_cool = P/((gamma-1)|Lambda|) at the starting state
-    float Lb = fcool_ki(Tb, NN);
-    float r = dts * g1 * fabsf(Lb) / basef;
-    float x0 = log10f(NN), x1 = log10f(Tb), x2 = log10f(fmaxf(r, 1e-30f));
-    bool inbox = stiff && x0 >= -2.0f && x0 <= 5.0f && x1 >= -2.0f && x1 <= 1.30103f && x2 >= -3.0f && x2 <= 3.0f;
-    float conf;
-    float y = surrogate_warp(A.W, x0, x1, x2, inbox, &conf);
-    if (inbox) {
-      // the network's answer, polished by two Newton steps on
-      // f(P) = P + c Lambda(P) - P_start (c = dt (gamma-1)), then checked
-      float c = dts * g1;
-      float P = (Tb * exp10f(y)) / nkbi;
-      for (int it = 0; it < 2; it++) {
-        float L, dL;
-        fcool_ki_d(P * nkbi, NN, L, dL);
-        float fv = P + c * L - basef;
-        float fp = 1.0f + c * dL * nkbi;
-        if (fp > 0.0f) P = fmaxf(P - fv / fp, 0.1f * P);
-      }
-      // implicit residual |P + Lambda(P) dt (gamma-1) - P_old| / P_old
-      float res = fabsf(P + fcool_ki(P * nkbi, NN) * c - basef) / basef;
-      if (res <= A.tol) {
-        dp_cool = P - basef;
-        need_imc = false;
-        atomicAdd(A.sur_count, 1ull);
-      } else {
-        atomicAdd(A.fb_count, 1ull);
-      }
-    }
+  if constexpr (CHEM) {
+    c.cs = cell_species<float>(f, a, [](double v) { return d2f(v); });
+    c.CooL = fcool_species<float>(T0, c.cs);
+  } else {
+    c.CooL = fcool_ki(T0, c.NN);
   }
-  if (!valid) return;
-  if (!stiff) {
-    dp_cool = -(g1 * CooL * dts);
-  } else if (need_imc) {
-    float Pm = imc32(basef, nkbi, dts * g1, cool);
-    dp_cool = Pm - basef;
-    atomicAdd(A.imc_count, 1ull);
-  }
-  float tcd = g1 * Kc * sqrtf(T0);
-  tcd = __fdividef(0.49f * nimc * kb, tcd) * (dx0 * dx0);
-  float w = (tcd - dt >= 0.0f) ? 1.0f : 0.0f;      // (sign(0.5, tcd-dt) + 0.5)
-  float dp = dp_cool + w * g1 * dts * div;
-  double pnew = base + f2d(dp);
-  float pf = basef + dp;
+  const double Pn = A.pold[a];
+  const float Pnf = d2f(Pn);
+  c.dts = dt * ((A.pass == 0) ? 0.5f : 1.0f);      // predictor: half of dt
+  c.base = (A.pass == 0) ? A.pin[a] : Pn;          // p the cooling acts on
+  c.basef = (A.pass == 0) ? d2f(c.base) : Pnf;
+  c.stiff = !(dt <= 0.2f * Pnf / (c.g1 * fabsf(c.CooL)));
+  c.nimc = H + pr + He + Hep + H2;
+  c.nkbi = __fdividef(1.0f, kb * c.nimc);
+  c.T0 = T0;
+  c.dx0 = dx0;
+  return c;
+}
+
+template <bool CHEM>
+__device__ __forceinline__ void source32_finish(const Source32Args &A, const Cell32<CHEM> &c, float dp_cool) {
+  const float kb = d2f(A.ph.kb), Kc = d2f(A.ph.kcond), dt = d2f(A.dt);
+  float tcd = c.g1 * Kc * sqrtf(c.T0);
+  tcd = __fdividef(0.49f * c.nimc * kb, tcd) * (c.dx0 * c.dx0);
+  const float w = (tcd - dt >= 0.0f) ? 1.0f : 0.0f;      // (sign(0.5, tcd-dt) + 0.5)
+  const float dp = dp_cool + w * c.g1 * c.dts * c.div;
+  double pnew = c.base + f2d(dp);
+  const float pf = c.basef + dp;
   // floors max(pnew, pmin), min(pnew, pmax); a NaN passes and is reported
   if (pf < d2f(A.ph.pmin)) pnew = A.ph.pmin;
   if (pf > d2f(A.ph.pmax)) pnew = A.ph.pmax;
-  A.pout[a] = pnew;
+  A.pout[c.a] = pnew;
   if (!(pf == pf)) flag(A.err, ERRB_NONFINITE);
+}
+
+// The implicit solve of a stiff cell (IMC bisection), kept out of line: few
+// cells take it.
+template <bool CHEM>
+__device__ __noinline__ float imc32_cell(const Cell32<CHEM> &c) {
+  const float cc = c.dts * c.g1;
+  if constexpr (CHEM) return imc32(c.basef, c.nkbi, cc, [&](float T) { return fcool_species<float>(T, c.cs); });
+  else return imc32(c.basef, c.nkbi, cc, [&](float T) { return fcool_ki(T, c.NN); });
+}
+
+// The surrogate's answer for a stiff cell (warp-collective: every lane of
+// the warp calls it, `on` marks the lanes with a cell): its inputs log10 N,
+// log10 T, log10(dts / t_cool) with t_cool = P/((gamma-1)|Lambda|) at the
+// starting state, the network, two Newton steps on f(P) = P + c Lambda(P) -
+// P_start (c = dt (gamma-1)), and the implicit residual
+// |P + Lambda(P) dt (gamma-1) - P_old| / P_old as the acceptance test.
+// Returns true with dp when accepted.
+__device__ __forceinline__ bool surrogate_cell(const Source32Args &A, const SurNetSmem *net, bool on,
+                                               const Cell32<false> &c, float *dp) {
+  const float Tb = c.basef * c.nkbi;               // temperature the implicit solve starts from
+  const float Lb = fcool_ki(Tb, c.NN);
+  const float r = c.dts * c.g1 * fabsf(Lb) / c.basef;
+  const float x0 = log10f(c.NN), x1 = log10f(Tb), x2 = log10f(fmaxf(r, 1e-30f));
+  const bool inbox = on && x0 >= -2.0f && x0 <= 5.0f && x1 >= -2.0f && x1 <= 1.30103f && x2 >= -3.0f && x2 <= 3.0f;
+  float conf;
+  const float y = surrogate_warp_smem(net, x0, x1, x2, inbox, &conf);
+  if (!inbox) return false;
+  const float cc = c.dts * c.g1;
+  float P = (Tb * exp10f(y)) / c.nkbi;
+  for (int it = 0; it < 2; it++) {
+    float L, dL;
+    fcool_ki_d(P * c.nkbi, c.NN, L, dL);
+    const float fv = P + cc * L - c.basef;
+    const float fp = 1.0f + cc * dL * c.nkbi;
+    if (fp > 0.0f) P = fmaxf(P - fv / fp, 0.1f * P);
+  }
+  const float res = fabsf(P + fcool_ki(P * c.nkbi, c.NN) * cc - c.basef) / c.basef;
+  if (res <= A.tol) {
+    *dp = P - c.basef;
+    atomicAdd(A.sur_count, 1ull);
+    return true;
+  }
+  atomicAdd(A.fb_count, 1ull);
+  return false;
+}
+
+// Thread per cell.  CHEM: the species cooling function (ifchem = 2) instead
+// of the KI one.  DEFER (a surrogate is loaded): stiff cells are appended to
+// A.stiff_list and left to source32_stiff_kernel, so this kernel carries
+// only the registers of the explicit path (used with the KI cooling only);
+// otherwise they are solved here by the bisection.
+template <bool CHEM, bool DEFER>
+__global__ void __launch_bounds__(DEFER ? kSourceDeferThreads : 128) source32_kernel(Source32Args A) {
+  const Grid &g = A.g;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = t < (long long)g.n[0] * g.n[1] * g.n[2];
+  const Cell32<CHEM> c = source32_prep<CHEM>(A, valid ? t : 0);
+  const bool stiff = valid && c.stiff;
+  if constexpr (DEFER) {
+    // block-aggregated append of the stiff cells' indices: one atomic per
+    // block on the shared counter
+    __shared__ unsigned wcnt[kSourceDeferThreads / 32];
+    __shared__ unsigned long long bbase;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned m = __ballot_sync(0xffffffffu, stiff);
+    if (lane == 0) wcnt[w] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned tot = 0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) tot += wcnt[q];
+      bbase = tot ? atomicAdd(A.stiff_count, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    if (stiff) {
+      unsigned long long pos = bbase;
+      for (int q = 0; q < w; q++) pos += wcnt[q];
+      A.stiff_list[pos + __popc(m & ((1u << lane) - 1u))] = (int)t;
+    }
+    if (!valid || stiff) return;
+  }
+  if (!valid) return;
+  float dp_cool;
+  if (!stiff) {
+    dp_cool = -(c.g1 * c.CooL * c.dts);
+  } else {
+    dp_cool = imc32_cell<CHEM>(c) - c.basef;
+    atomicAdd(A.imc_count, 1ull);
+  }
+  source32_finish<CHEM>(A, c, dp_cool);
+}
+
+// The stiff cells listed by source32_kernel<false, true> (KI cooling): the
+// surrogate for whole warps of stiff cells, the bisection for the cells it
+// rejects.  Blocks stride over the list; every lane of a block runs the same
+// trips, so the warp-collective network sees full warps.
+__global__ void __launch_bounds__(128) source32_stiff_kernel(Source32Args A) {
+  constexpr bool CHEM = false;
+  const long long cnt = (long long)*A.stiff_count;
+  if ((long long)blockIdx.x * blockDim.x >= cnt) return;   // whole block: no stiff cell for it
+  __shared__ SurNetSmem net;
+  sur_stage(A.W, &net);
+  for (long long e0 = (long long)blockIdx.x * blockDim.x; e0 < cnt; e0 += (long long)gridDim.x * blockDim.x) {
+    const long long e = e0 + threadIdx.x;
+    const bool on = e < cnt;
+    const long long t = A.stiff_list[on ? e : e0];
+    const Cell32<CHEM> c = source32_prep<CHEM>(A, t);
+    float dp_cool = 0.0f;
+    const bool done = surrogate_cell(A, &net, on, c, &dp_cool);
+    if (!on) continue;
+    if (!done) {
+      dp_cool = imc32_cell<CHEM>(c) - c.basef;
+      atomicAdd(A.imc_count, 1ull);
+    }
+    source32_finish<CHEM>(A, c, dp_cool);
+  }
 }
 
 // dt for the chosen form: the Courant limit (:1912-1930) and the thermal

@@ -151,6 +151,127 @@ __device__ __forceinline__ void net_forward16(const SurNet *net, float n0, float
   o1 = (r < 8) ? v1 : v3;
 }
 
+// ---------------------------------------------------------------------
+// Inference inside the solver (source32_stiff_kernel): the weights of one
+// block in shared memory, staged once per block, instead of per-lane loads
+// from global memory for every tile; W2 and W3 rows padded from 64 to 72
+// BF16 so that the eight rows a B fragment load touches fall in distinct
+// banks.  The activation is SiLU(z) = s + s tanh(s), s = z/2, evaluated on
+// BF16 pairs with the hardware tanh approximation (one MUFU operation for
+// two activations instead of two for one); the activations are BF16
+// operands of the next layer in any case, and the solver checks every
+// answer by its implicit residual.
+constexpr int SUR_LD = 72;   // padded row length of W2 / W3 in shared memory
+
+struct SurNetSmem {
+  float4 w1[64];                      // (w0, w1, w2, b1) of hidden unit n
+  float b2[64], b3[8];
+  __nv_bfloat16 W2[64 * SUR_LD];      // [out][in]
+  __nv_bfloat16 W3[8 * SUR_LD];       // [out padded to 8][in]
+};
+
+// all threads of the block call; a barrier follows inside
+__device__ __forceinline__ void sur_stage(const SurNet *net, SurNetSmem *s) {
+  for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+    const __nv_bfloat16 *w = net->W1 + q * 16;
+    s->w1[q] = make_float4(__bfloat162float(w[0]), __bfloat162float(w[1]), __bfloat162float(w[2]), net->b1[q]);
+    s->b2[q] = net->b2[q];
+  }
+  for (int q = threadIdx.x; q < 8; q += blockDim.x) s->b3[q] = net->b3[q];
+  for (int q = threadIdx.x; q < 64 * 32; q += blockDim.x) {   // 32-bit words of W2
+    const int r = q >> 5, c = (q & 31) * 2;
+    *reinterpret_cast<uint32_t *>(&s->W2[r * SUR_LD + c]) = ld32(net->W2 + r * 64 + c);
+  }
+  for (int q = threadIdx.x; q < 8 * 32; q += blockDim.x) {
+    const int r = q >> 5, c = (q & 31) * 2;
+    *reinterpret_cast<uint32_t *>(&s->W3[r * SUR_LD + c]) = ld32(net->W3 + r * 64 + c);
+  }
+  __syncthreads();
+}
+
+// SiLU of two accumulator entries, packed as the BF16 pair of the next A
+// fragment: s = z/2 rounded to BF16, then s + s tanh(s) on the BF16 pair
+// (one tanh approximation for both entries).
+__device__ __forceinline__ uint32_t silu2_bf16(float z0, float z1) {
+  const uint32_t h = pack_bf16(0.5f * z0, 0.5f * z1);
+  uint32_t th, r;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(th) : "r"(h));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(r) : "r"(h), "r"(th));
+  return r;
+}
+
+__device__ __forceinline__ void act_frags_fast(const float (&z)[8][4], uint32_t (&a)[4][4]) {
+#pragma unroll
+  for (int kt = 0; kt < 4; kt++) {
+    a[kt][0] = silu2_bf16(z[2 * kt][0], z[2 * kt][1]);
+    a[kt][1] = silu2_bf16(z[2 * kt][2], z[2 * kt][3]);
+    a[kt][2] = silu2_bf16(z[2 * kt + 1][0], z[2 * kt + 1][1]);
+    a[kt][3] = silu2_bf16(z[2 * kt + 1][2], z[2 * kt + 1][3]);
+  }
+}
+
+__device__ __forceinline__ void net_forward16_smem(const SurNetSmem *s, float n0, float n1, float n2, int rowbase,
+                                                   float &o0, float &o1) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  // layer 1 on the CUDA cores in FP32 (accumulator layout, as layer1_fp32)
+  const float a0 = __shfl_sync(0xffffffffu, n0, rowbase + g), a1 = __shfl_sync(0xffffffffu, n1, rowbase + g),
+              a2 = __shfl_sync(0xffffffffu, n2, rowbase + g);
+  const float c0 = __shfl_sync(0xffffffffu, n0, rowbase + g + 8), c1 = __shfl_sync(0xffffffffu, n1, rowbase + g + 8),
+              c2 = __shfl_sync(0xffffffffu, n2, rowbase + g + 8);
+  float z[8][4];
+#pragma unroll
+  for (int nt = 0; nt < 8; nt++) {
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const float4 w = s->w1[nt * 8 + 2 * t + q];
+      z[nt][q] = w.w + w.x * a0 + w.y * a1 + w.z * a2;
+      z[nt][2 + q] = w.w + w.x * c0 + w.y * c1 + w.z * c2;
+    }
+  }
+  uint32_t a[4][4];
+  act_frags_fast(z, a);
+  // layer 2 on the tensor cores
+#pragma unroll
+  for (int nt = 0; nt < 8; nt++) {
+    const float b0 = s->b2[nt * 8 + 2 * t], b1 = s->b2[nt * 8 + 2 * t + 1];
+    z[nt][0] = b0; z[nt][1] = b1; z[nt][2] = b0; z[nt][3] = b1;
+    const __nv_bfloat16 *row = s->W2 + (nt * 8 + g) * SUR_LD;
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) mma_bf16(z[nt], a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
+  }
+  act_frags_fast(z, a);
+  // output layer
+  float y[4];
+  {
+    const float b0 = s->b3[2 * t], b1 = s->b3[2 * t + 1];
+    y[0] = b0; y[1] = b1; y[2] = b0; y[3] = b1;
+    const __nv_bfloat16 *row = s->W3 + g * SUR_LD;
+#pragma unroll
+    for (int kt = 0; kt < 4; kt++) mma_bf16(y, a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
+  }
+  const int r = lane - rowbase;
+  const int src = ((r & 7) << 2);
+  const float v0 = __shfl_sync(0xffffffffu, y[0], src), v1 = __shfl_sync(0xffffffffu, y[1], src);
+  const float v2 = __shfl_sync(0xffffffffu, y[2], src), v3 = __shfl_sync(0xffffffffu, y[3], src);
+  o0 = (r < 8) ? v0 : v2;
+  o1 = (r < 8) ? v1 : v3;
+}
+
+// whole-warp inference from the staged weights (all 32 lanes call)
+__device__ __forceinline__ float surrogate_warp_smem(const SurNetSmem *s, float x0, float x1, float x2, bool active,
+                                                     float *conf) {
+  const float n0 = active ? (x0 - SUR_C0) / SUR_S0 : 0.0f;
+  const float n1 = active ? (x1 - SUR_C1) / SUR_S1 : 0.0f;
+  const float n2 = active ? (x2 - SUR_C2) / SUR_S2 : 0.0f;
+  float o0a = 0.0f, o1a = 0.0f, o0b = 0.0f, o1b = 0.0f;
+  const unsigned any = __ballot_sync(0xffffffffu, active);
+  if (any & 0x0000ffffu) net_forward16_smem(s, n0, n1, n2, 0, o0a, o1a);
+  if (any & 0xffff0000u) net_forward16_smem(s, n0, n1, n2, 16, o0b, o1b);
+  const int lane = threadIdx.x & 31;
+  *conf = lane < 16 ? o1a : o1b;
+  return lane < 16 ? o0a : o0b;
+}
+
 // Whole-warp inference: every lane brings one sample (all 32 lanes must
 // call).  Returns log10(T_new/T) and writes the confidence estimate.
 __device__ __forceinline__ float surrogate_warp(const SurNet *net, float x0, float x1, float x2, bool active,
