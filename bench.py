@@ -14,8 +14,10 @@ steps.
 `plain_fp64` is the plain FP64 path timed the same way; `l1_error` compares
 the two at the same physical time after --l1-steps FP64 steps (each form
 takes its own dt).  `e2e` times the same step
-through the C ABI with the state uploaded from pinned host memory and
-downloaded again every step.  `roofline` is for the dominant kernel (the
+through the C ABI entry mhd_step_host: every step copies the whole state in
+from pinned host memory and the new state out, the finished arrays (rho and
+species after the sweeps, the face field after CT) while the step still
+runs.  `roofline` is for the dominant kernel (the
 fused sweep), with algorithmic bytes from the per-zone budget of the step.
 `cpu_baseline` is the CPU restatement (oracle, C++ with OpenMP) timed on a
 bounded sample on the host cores.  `stiff_cooling_source` times SOURCE alone
@@ -328,8 +330,8 @@ def main():
                                 "imc": d_acc["imc_cells"]}}
         del g64
 
-    # e2e through the C ABI with host buffers (pinned), one upload + step +
-    # download per step
+    # e2e through the C ABI with host buffers (pinned): every step copies the
+    # whole state in and the new state out (mhd_step_host)
     pin_U = torch.empty((8,) + tuple(st.U.shape[1:]), dtype=torch.float64, pin_memory=True).numpy()
     pin_S = torch.empty((8,) + tuple(st.U.shape[1:]), dtype=torch.float64, pin_memory=True).numpy()
     pin_U[...] = st.U
@@ -337,12 +339,11 @@ def main():
     out_U = torch.empty(pin_U.shape, dtype=torch.float64, pin_memory=True).numpy()
     out_S = torch.empty(pin_S.shape, dtype=torch.float64, pin_memory=True).numpy()
     g = g32
-    host_state = problems.MhdState(st.params, pin_U, pin_S, st.x, st.dx, st.y, st.dy, st.z, st.dz)
 
     def e2e_step():
-        g.upload(host_state)
-        g.step()
-        g.download(out=(out_U, out_S, None))
+        # mhd_step_host: the state in from pinned host memory, one step, the
+        # new state back (copies of finished arrays overlap the step's tail)
+        g.step_host(pin_U, pin_S, out_U, out_S)
 
     e2e_step()   # untimed: first touch of the pinned buffers
     barrier()

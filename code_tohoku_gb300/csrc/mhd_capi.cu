@@ -58,6 +58,10 @@ struct mhd_handle {
   long long launches = 0;
   long long imc_cells = 0;
   bool uploaded = false;
+  // mhd_step_host: copy-back stream and the events it waits on (created on
+  // first use)
+  cudaStream_t io_stream = nullptr;
+  cudaEvent_t ev_io[2] = {nullptr, nullptr};
   std::vector<double> rdx_host, rdxc_host;   // staging for the async coordinate copies
   std::vector<float> dxf_host;
   std::string msg;
@@ -256,6 +260,12 @@ int mhd_destroy(mhd_handle *h) {
   cudaFree(h->sur_master);
   cudaFree(h->sur_net);
   if (h->h_small) cudaFreeHost(h->h_small);
+  if (h->io_stream) {
+    cudaStreamSynchronize(h->io_stream);
+    cudaStreamDestroy(h->io_stream);
+  }
+  for (int e = 0; e < 2; e++)
+    if (h->ev_io[e]) cudaEventDestroy(h->ev_io[e]);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return MHD_OK;
@@ -366,12 +376,18 @@ int mhd_timestep(mhd_handle *h, double *dt, int *st) {
 }
 
 namespace {
-// the thermal branch of SOURCE (ifthrm = 2, :2477-2572)
-int source_thermal(mhd_handle *h, double dt) {
+// the thermal branch of SOURCE (ifthrm = 2, :2477-2572); rho_sp_filled:
+// the caller has already filled the ghosts of rho and the species with the
+// same values (mhd_step_host, which copies those arrays back meanwhile)
+int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
   // SOURCE :2481-2486 — rho, p and the species, one ghost layer, x y z
-  TRY(fill(h, {h->f.U[0], h->f.U[4]}, 7, 1, 0, {IN_RHO, IN_P}));
-  TRY(fill(h, {h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]}, 7, 1, 1,
-           {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4}));
+  if (rho_sp_filled) {
+    TRY(fill(h, {h->f.U[4]}, 7, 1, 0, {IN_P}));
+  } else {
+    TRY(fill(h, {h->f.U[0], h->f.U[4]}, 7, 1, 0, {IN_RHO, IN_P}));
+    TRY(fill(h, {h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]}, 7, 1, 1,
+             {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4}));
+  }
   if (h->p.precision == MHD_PREC_FP32) {
     if (h->p.cooling == MHD_COOL_SURROGATE && !h->sur_net)
       return fail(h, MHD_ERR_STATE, "surrogate cooling selected but no network loaded (mhd_surrogate_load)");
@@ -408,12 +424,13 @@ int source_thermal(mhd_handle *h, double dt) {
 }
 }  // namespace
 
-int mhd_source(mhd_handle *h, double dt) {
+namespace {
+int source_impl(mhd_handle *h, double dt, bool rho_sp_filled) {
   if (!h) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
   TRY(need_inflow(h));
-  if (h->p.ifthrm == 2) TRY(source_thermal(h, dt));
+  if (h->p.ifthrm == 2) TRY(source_thermal(h, dt, rho_sp_filled));
   // the chemistry network after the thermal update (ifchem = 2, :2576-2776)
   if (h->p.ifchem == 2) {
     if (h->p.precision == MHD_PREC_FP32) CK(chem_step_fp32(h->g, h->ph, h->f, dt, h->err, h->stream));
@@ -421,6 +438,9 @@ int mhd_source(mhd_handle *h, double dt) {
   }
   return MHD_OK;
 }
+}  // namespace
+
+int mhd_source(mhd_handle *h, double dt) { return source_impl(h, dt, false); }
 
 int mhd_sweep(mhd_handle *h, int dir, double dt) {
   if (!h || dir < 0 || dir > 2) return MHD_ERR_ARG;
@@ -434,7 +454,15 @@ int mhd_sweep(mhd_handle *h, int dir, double dt) {
   return MHD_OK;
 }
 
-int mhd_ct(mhd_handle *h, double dt) {
+namespace {
+int ct_impl(mhd_handle *h, double dt, bool rho_filled);
+}
+int mhd_ct(mhd_handle *h, double dt) { return ct_impl(h, dt, false); }
+
+namespace {
+// rho_filled: the caller has already filled rho's two ghost layers with the
+// values CC(2) needs (mhd_step_host)
+int ct_impl(mhd_handle *h, double dt, bool rho_filled) {
   if (!h) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
@@ -452,7 +480,7 @@ int mhd_ct(mhd_handle *h, double dt) {
   TRY(fill(h, {h->vf[0], h->vf[1]}, 4, 2));
   TRY(fill(h, {f.U[4]}, 7, 2, 0, {IN_P}));
   // CC(2) for Ez :2142
-  TRY(fill(h, {f.U[0]}, 7, 2, 0, {IN_RHO}));
+  if (!rho_filled) TRY(fill(h, {f.U[0]}, 7, 2, 0, {IN_RHO}));
   if (fp32) {
     CT32Args a{};
     a.g = h->g;
@@ -473,6 +501,7 @@ int mhd_ct(mhd_handle *h, double dt) {
   TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
   return MHD_OK;
 }
+}  // namespace
 
 int mhd_dissip(mhd_handle *h) {
   if (!h) return MHD_ERR_ARG;
@@ -513,6 +542,72 @@ int mhd_step(mhd_handle *h, double tsave, double *dt, int *st) {
   *dt = d;
   *st = s;
   return MHD_OK;
+}
+
+int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, double *U_out, double *species_out,
+                  double tsave, double *dt, int *st) {
+  if (!h || !U_in || !species_in || !U_out || !species_out || !dt || !st) return MHD_ERR_ARG;
+  if (!h->uploaded) return fail(h, MHD_ERR_STATE, "mhd_step_host needs a first mhd_upload (coordinates)");
+  CKR(cudaSetDevice(h->p.device));
+  TRY(need_inflow(h));
+  if (!h->io_stream) CKR(cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
+  for (int e = 0; e < 2; e++)
+    if (!h->ev_io[e]) CKR(cudaEventCreateWithFlags(&h->ev_io[e], cudaEventDisableTiming));
+  const Grid &g = h->g;
+  const size_t nc = (size_t)g.ncell, nb = nc * sizeof(double);
+  Fields &f = h->f;
+  // the state in (nde / ndtot of the chemistry stay on the device)
+  for (int q = 0; q < 8; q++) CKR(cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
+  for (int q = 0; q < 8; q++)
+    CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
+  CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
+  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
+  // dt (mhd_step)
+  double d;
+  int s;
+  TRY(mhd_timestep(h, &d, &s));
+  if (h->time + d > h->p.tfinal) d = h->p.tfinal - h->time;
+  if (h->time + d > tsave) d = tsave - h->time;
+  if (!(d > 0.0)) return fail(h, MHD_ERR_DT, "dt <= 0 after clipping (time %.17g)", h->time);
+  // the EVOLVE iteration of mhd_advance, copying arrays back as soon as
+  // they are final: without chemistry rho and the species are final after
+  // the sweeps (once their ghosts are filled), the face field after CC
+  static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
+  TRY(mhd_source(h, 0.5 * d));
+  for (int q = 0; q < 3; q++) TRY(mhd_sweep(h, orders[h->ifevo - 1][q], d));
+  h->ifevo = h->ifevo % 6 + 1;
+  const bool early = h->p.ifchem != 2;
+  if (early) {
+    // the ghost fills CC(2) and SOURCE would make, made now
+    TRY(fill(h, {f.U[0]}, 7, 2, 0, {IN_RHO}));
+    if (h->p.ifthrm == 2)
+      TRY(fill(h, {f.sp[0], f.sp[1], f.sp[2], f.sp[3], f.sp[4]}, 7, 1, 1,
+               {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4}));
+    CKR(cudaEventRecord(h->ev_io[0], h->stream));
+    CKR(cudaStreamWaitEvent(h->io_stream, h->ev_io[0], 0));
+    CKR(cudaMemcpyAsync(U_out, f.U[0], nb, cudaMemcpyDeviceToHost, h->io_stream));
+    for (int q = 0; q < 8; q++)
+      CKR(cudaMemcpyAsync(species_out + q * nc, f.sp[q], nb, cudaMemcpyDeviceToHost, h->io_stream));
+  }
+  TRY(ct_impl(h, d, early));
+  CKR(cudaEventRecord(h->ev_io[1], h->stream));
+  CKR(cudaStreamWaitEvent(h->io_stream, h->ev_io[1], 0));
+  for (int q = 5; q < 8; q++)
+    CKR(cudaMemcpyAsync(U_out + q * nc, f.U[q], nb, cudaMemcpyDeviceToHost, h->io_stream));
+  TRY(source_impl(h, 0.5 * d, early));
+  if (h->p.dissip) TRY(mhd_dissip(h));
+  h->time = h->time + d;
+  h->steps++;
+  for (int q = early ? 1 : 0; q < 5; q++)
+    CKR(cudaMemcpyAsync(U_out + q * nc, f.U[q], nb, cudaMemcpyDeviceToHost, h->stream));
+  if (!early)
+    for (int q = 0; q < 8; q++)
+      CKR(cudaMemcpyAsync(species_out + q * nc, f.sp[q], nb, cudaMemcpyDeviceToHost, h->stream));
+  CKR(cudaStreamSynchronize(h->io_stream));
+  CKR(cudaStreamSynchronize(h->stream));
+  *dt = d;
+  *st = s;
+  return check_err(h);
 }
 
 int mhd_evolve(mhd_handle *h, int nsteps, double tsave, int *steps_done) {

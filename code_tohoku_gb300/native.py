@@ -23,7 +23,7 @@ COOL_EXACT, COOL_SURROGATE = 0, 1
 
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_timestep", "mhd_source",
-           "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_evolve", "mhd_get_time",
+           "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_step_host", "mhd_evolve", "mhd_get_time",
            "mhd_set_time", "mhd_set_inflow", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
            "mhd_kernel_launches", "mhd_reset_counters", "mhd_surrogate_nparams", "mhd_surrogate_load",
            "mhd_surrogate_train", "mhd_surrogate_label", "mhd_surrogate_eval", "mhd_surrogate_grad",
@@ -95,6 +95,7 @@ def load(build_if_missing=True):
         "mhd_dissip": [H],
         "mhd_advance": [H, ctypes.c_double],
         "mhd_step": [H, ctypes.c_double, _P, ctypes.POINTER(ctypes.c_int)],
+        "mhd_step_host": [H, _P, _P, _P, _P, ctypes.c_double, _P, ctypes.POINTER(ctypes.c_int)],
         "mhd_evolve": [H, ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int)],
         "mhd_get_time": [H, _P, ctypes.POINTER(ctypes.c_int)],
         "mhd_set_time": [H, ctypes.c_double, ctypes.c_int],
@@ -278,6 +279,18 @@ class Mhd3D:
         dt = ctypes.c_double()
         st = ctypes.c_int()
         self._ck(self.L.mhd_step(self.h, tsave, ctypes.byref(dt), ctypes.byref(st)))
+        return dt.value, st.value
+
+    def step_host(self, U_in, species_in, U_out, species_out, tsave=1e30):
+        """mhd_step_host: one step from host arrays to host arrays (same
+        layout as upload/download; all four C-contiguous float64)."""
+        for a in (U_in, species_in, U_out, species_out):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != (8,) + self.shape:
+                raise ValueError("step_host: arrays must be C-contiguous float64 of shape (8,) + padded grid")
+        dt = ctypes.c_double()
+        st = ctypes.c_int()
+        self._ck(self.L.mhd_step_host(self.h, _ptr(U_in), _ptr(species_in), _ptr(U_out), _ptr(species_out),
+                                      tsave, ctypes.byref(dt), ctypes.byref(st)))
         return dt.value, st.value
 
     def evolve(self, nsteps, tsave=1e30):

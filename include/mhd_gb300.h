@@ -125,6 +125,21 @@ int mhd_advance(mhd_handle *h, double dt);
 /* Full iteration: dt from mhd_timestep clipped at tfinal and tsave
  * (:603-604), then mhd_advance.  Returns the dt used and the limiter. */
 int mhd_step(mhd_handle *h, double tsave, double *dt, int *st);
+/* One mhd_step from a host state to a host state, for a driver that keeps
+ * its module arrays on the host and calls the library once per EVOLVE
+ * iteration (the reference's loop body :569-656 with the arrays of
+ * INITIA / SAVEU on either side).  U_in / species_in are copied in (the
+ * layout of mhd_upload; the coordinates of the last mhd_upload are kept,
+ * and so are the chemistry's nde / ndtot, which are not host arrays), the
+ * step runs, and U_out / species_out receive the new state (the layout of
+ * mhd_download).  The arrays are copied back while the step still runs as
+ * soon as they are final: without chemistry rho and the species after the
+ * sweeps, the face field after CT.  The results equal mhd_upload's state
+ * copy + mhd_step + mhd_download bit for bit.  In and out may be the same
+ * buffers; pinned host memory gives full copy speed.  Needs one
+ * mhd_upload on the handle first. */
+int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, double *U_out,
+                  double *species_out, double tsave, double *dt, int *st);
 /* nsteps iterations of mhd_step; stops early at tfinal or tsave. */
 int mhd_evolve(mhd_handle *h, int nsteps, double tsave, int *steps_done);
 
