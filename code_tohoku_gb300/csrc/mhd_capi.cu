@@ -321,7 +321,7 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
     off += g.s[d];
   }
   // nde, ndtot (INITIA :471-474) and CC(4) as INITIA:470
-  CK(chem_totals(h->g, h->f, h->stream));
+  CK(chem_totals(h->g, h->f, 1, h->stream));
   CK(cell_b(h->g, h->f, h->stream));
   TRY(fill(h, {h->f.bcc[0], h->f.bcc[1], h->f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
   CKR(cudaStreamSynchronize(h->stream));
@@ -430,6 +430,9 @@ int source_impl(mhd_handle *h, double dt, bool rho_sp_filled) {
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
   TRY(need_inflow(h));
+  // nde, ndtot from the species of cells 1..n (:2460-2463); read only by
+  // the species cooling and the network
+  if (h->p.ifchem == 2) CK(chem_totals(h->g, h->f, 0, h->stream));
   if (h->p.ifthrm == 2) TRY(source_thermal(h, dt, rho_sp_filled));
   // the chemistry network after the thermal update (ifchem = 2, :2576-2776)
   if (h->p.ifchem == 2) {
@@ -556,7 +559,7 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   const Grid &g = h->g;
   const size_t nc = (size_t)g.ncell, nb = nc * sizeof(double);
   Fields &f = h->f;
-  // the state in (nde / ndtot of the chemistry stay on the device)
+  // the state in
   for (int q = 0; q < 8; q++) CKR(cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
   for (int q = 0; q < 8; q++)
     CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));

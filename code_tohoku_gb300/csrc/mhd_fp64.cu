@@ -63,9 +63,9 @@ cudaError_t chem_step(const Grid &g, const Phys &ph, const Fields &f, double dt,
   return cudaGetLastError();
 }
 
-cudaError_t chem_totals(const Grid &g, const Fields &f, cudaStream_t s) {
-  long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
-  chem_totals_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f);
+cudaError_t chem_totals(const Grid &g, const Fields &f, int plus, cudaStream_t s) {
+  long long n = (long long)(g.n[0] + plus) * (g.n[1] + plus) * (g.n[2] + plus);
+  chem_totals_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f, plus);
   return cudaGetLastError();
 }
 

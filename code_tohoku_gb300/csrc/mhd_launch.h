@@ -39,7 +39,7 @@ cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const doubl
 cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s);
 cudaError_t source_pass(const SourceArgs &a, cudaStream_t s);
 cudaError_t chem_step(const Grid &g, const Phys &ph, const Fields &f, double dt, int *err, cudaStream_t s);
-cudaError_t chem_totals(const Grid &g, const Fields &f, cudaStream_t s);
+cudaError_t chem_totals(const Grid &g, const Fields &f, int plus, cudaStream_t s);
 cudaError_t chem_step_fp32(const Grid &g, const Phys &ph, const Fields &f, double dt, int *err, cudaStream_t s);
 cudaError_t dt_reduce(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
                       cudaStream_t s);

@@ -129,8 +129,7 @@ int mhd_step(mhd_handle *h, double tsave, double *dt, int *st);
  * its module arrays on the host and calls the library once per EVOLVE
  * iteration (the reference's loop body :569-656 with the arrays of
  * INITIA / SAVEU on either side).  U_in / species_in are copied in (the
- * layout of mhd_upload; the coordinates of the last mhd_upload are kept,
- * and so are the chemistry's nde / ndtot, which are not host arrays), the
+ * layout of mhd_upload; the coordinates of the last mhd_upload are kept), the
  * step runs, and U_out / species_out receive the new state (the layout of
  * mhd_download).  The arrays are copied back while the step still runs as
  * soon as they are final: without chemistry rho and the species after the

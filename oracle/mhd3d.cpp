@@ -1139,6 +1139,16 @@ struct Mhd3D {
   }
 
   void SOURCE(double dt) {   // thermal branch ifthrm=2 (:2477-2572), then chemistry ifchem=2
+    // nde and ndtot from the species of cells 1..n (:2460-2463); only the
+    // species cooling and the network read them
+    if (P.ifchem == 2)
+      for (int k = 1; k <= Nz; k++)
+        for (int j = 1; j <= Ny; j++)
+          for (int i = 1; i <= Nx; i++) {
+            size_t c = id(i, j, k);
+            nde[c] = sp[SP][c] + sp[SHEP][c] + sp[SCP][c];
+            ndtot[c] = sp[SP][c] + sp[SH][c] + 2.0 * sp[SH2][c] + sp[SHE][c] + sp[SHEP][c];
+          }
     if (P.ifthrm == 2) SOURCE_thermal(dt);
     if (P.ifchem == 2) CHEM(dt);
   }
