@@ -9,10 +9,9 @@
 // restatement bit for bit; R = float (the chosen form) uses the fast FP32
 // intrinsics.  The operation order is the reference's in both.
 //
-// Column densities (Ntot, NH2, NnC, NCO, tCII) come from SHIELD, which runs
-// only with ifrad = 2; with ifrad = 0 (the shipped deck) they keep their
-// INITIA value 0 (:476-477), so the shielding factors below are those of
-// zero columns.
+// Column densities (Ntot, NH2, NnC, NCO, tCII from each x side) come from
+// SHIELD (:2924-3036), which runs only with ifrad = 2; with ifrad = 0 (the
+// shipped deck) they keep their INITIA value 0 (:476-477).
 #pragma once
 
 namespace mhd {
@@ -35,9 +34,13 @@ __device__ __forceinline__ double wmul(double w, double y) { return w * y; }
 __device__ __forceinline__ float wmul(float w, float y) { return w == 0.0f ? 0.0f : w * y; }
 
 // the species of one cell (number densities), and its nde / ndtot
+// slots of the columns in CellSpecies::col and Fields::col
+enum { COL_NTOT1 = 0, COL_NTOT2, COL_NH21, COL_NH22, COL_NNC1, COL_NNC2, COL_NCO1, COL_NCO2, COL_TC1, COL_TC2 };
+
 template <class R>
 struct CellSpecies {
   R H, p, H2, He, Hep, C, Cp, CO, ne, nt;
+  R col[10];
 };
 
 template <class R>
@@ -49,13 +52,37 @@ __device__ __forceinline__ R fesc_t(R tau) {
              (R(4) * tau * dsq(mlog(fmx(tau * R(0.56419), R(4)))) + R(1.e-8));
 }
 
+// LEVC2 (:2889-2895): the C+ level populations n1, n2
+template <class R>
+__device__ __forceinline__ void levc2(R T, R b21, R ndH, R ndH2, R nde, R ndCp, R &n1, R &n2) {
+  R c21 = R(8.854e-8) * nde / dsq(T) + R(9.399e-10) * mpow(T, R(0.07)) * (ndH + ndH2);
+  R c12 = R(2) * c21 * mexp(R(-0.092) / T);
+  R A21 = R(2.4e-6) * b21;
+  n2 = ndCp * c12 / (c12 + c21 + A21);
+  n1 = ndCp * (c21 + A21) / (c12 + c21 + A21);
+}
+
+// SHIELD's source term of the C+ optical depth at one cell (:2939-2944):
+// 11.5563 (n1 - n2) / dv with the level populations of LEVC2 at the escape
+// probabilities of the previous columns tCII
+template <class R>
+__device__ __forceinline__ R shield_tau_source(R pr, R kb, const CellSpecies<R> &c) {
+  const R dv = R(2);
+  R b21 = fesc_t(c.col[COL_TC1]) + fesc_t(c.col[COL_TC2]);
+  R T = pr / (kb * (c.p + c.H + c.H2 + c.He + c.Hep));
+  R n1, n2;
+  levc2(T, b21, c.H, c.H2, c.ne, c.Cp, n1, n2);
+  return R(1.15563e1) * (n1 - n2) * (R(1) / dv);
+}
+
 // Fcool of the species (:2825-2880): Ly-alpha, CII, OI, dust-recombination
 // and CO cooling minus photo-electric, cosmic-ray and photo-destruction
 // heating, T in 1e3 K
 template <class R>
 __device__ __forceinline__ R fcool_species(R T, const CellSpecies<R> &c) {
   const R G0 = R(1), xo = R(3.2e-4), dv = R(2);
-  const R Ntot1 = R(0), Ntot2 = R(0), NH21 = R(0), NH22 = R(0), NCO1 = R(0), NCO2 = R(0), tC1 = R(0), tC2 = R(0);
+  const R Ntot1 = c.col[COL_NTOT1], Ntot2 = c.col[COL_NTOT2], NH21 = c.col[COL_NH21], NH22 = c.col[COL_NH22];
+  const R NCO1 = c.col[COL_NCO1], NCO2 = c.col[COL_NCO2], tC1 = c.col[COL_TC1], tC2 = c.col[COL_TC2];
   R Av1 = R(1.63542e-3) * Ntot1, x1 = R(6.1714e3) * NH21;
   R Av2 = R(1.63542e-3) * Ntot2, x2 = R(6.1714e3) * NH22;
   R ATN1 = (mexp(R(-2.5) * Av1) + mexp(R(-2.5) * Av2)) * R(0.5);
@@ -65,11 +92,8 @@ __device__ __forceinline__ R fcool_species(R T, const CellSpecies<R> &c) {
   Laml = Laml + c.p * c.ne * R(1.48e6) * mexp(R(-8.e1) / T);
   R fesC1 = fesc_t(tC1), fesC2 = fesc_t(tC2);
   R b21 = fesC1 + fesC2;
-  // LEVC2 (:2889-2895)
-  R c21 = R(8.854e-8) * c.ne / dsq(T) + R(9.399e-10) * mpow(T, R(0.07)) * (c.H + c.H2);
-  R c12 = R(2) * c21 * mexp(R(-0.092) / T);
-  R A21 = R(2.4e-6) * b21;
-  R n2 = c.Cp * c12 / (c12 + c21 + A21);
+  R n1, n2;
+  levc2(T, b21, c.H, c.H2, c.ne, c.Cp, n1, n2);
   R Lamc = R(6.0157e7) * n2 * b21;
   R tO1 = R(3.40057e-6) * Ntot1 / xo, tO2 = R(3.40057e-6) * Ntot2 / xo;
   R fesO1 = fesc_t(tO1), fesO2 = fesc_t(tO2);
@@ -105,9 +129,11 @@ struct ChemRates {
 };
 
 template <class R>
-__device__ __forceinline__ ChemRates<R> chem_rates(R T, R ndH2, R nde) {
+__device__ __forceinline__ ChemRates<R> chem_rates(R T, const CellSpecies<R> &c) {
   const R G0 = R(1), xo = R(3.2e-4), dv = R(2), Tgr = R(5.e-3);
-  const R Ntot1 = R(0), Ntot2 = R(0), NH21 = R(0), NH22 = R(0), NCO1 = R(0), NCO2 = R(0), NnC1 = R(0), NnC2 = R(0);
+  const R ndH2 = c.H2, nde = c.ne;
+  const R Ntot1 = c.col[COL_NTOT1], Ntot2 = c.col[COL_NTOT2], NH21 = c.col[COL_NH21], NH22 = c.col[COL_NH22];
+  const R NCO1 = c.col[COL_NCO1], NCO2 = c.col[COL_NCO2], NnC1 = c.col[COL_NNC1], NnC2 = c.col[COL_NNC2];
   ChemRates<R> r;
   R Av1 = R(1.63542e-3) * Ntot1, x1 = R(6.1714e3) * NH21;
   R Av2 = R(1.63542e-3) * Ntot2, x2 = R(6.1714e3) * NH22;
@@ -170,7 +196,7 @@ template <class R>
 __device__ __forceinline__ void chem_network(CellSpecies<R> &c, R pr, R kb, R dt, const R (&ndmin)[8]) {
   R pold = c.p, Hold = c.H, H2old = c.H2, Heold = c.He, Hepold = c.Hep, Cold = c.C, Cpold = c.Cp, COold = c.CO;
   R T = pr / kb / (pold + Hold + H2old + Heold + Hepold);
-  const ChemRates<R> k = chem_rates(T, c.H2, c.ne);
+  const ChemRates<R> k = chem_rates(T, c);
   R t1, t2, t3, om;
   R &H = c.H, &p = c.p, &H2 = c.H2, &He = c.He, &Hep = c.Hep, &C = c.C, &Cp = c.Cp, &CO = c.CO, &ne = c.ne,
     &nt = c.nt;

@@ -133,6 +133,20 @@ cudaError_t chem_step_fp32(const Grid &g, const Phys &ph, const Fields &f, doubl
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(128) shield_tau32_kernel(Grid g, Phys ph, Fields f, double *tau) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)g.n[0] * g.n[1] * g.n[2]) return;
+  shield_tau_cell<float>(g, ph, f, tau, t, [](double v) { return d2f(v); }, [](float v) { return f2d(v); });
+}
+
+cudaError_t shield_fp32(const Grid &g, const Phys &ph, const Fields &f, double *tau, double dxh, cudaStream_t s) {
+  long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+  shield_tau32_kernel<<<blocks_for(n, 128), 128, 0, s>>>(g, ph, f, tau);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return shield_scan(g, f, tau, dxh, s);
+}
+
 cudaError_t source_fp32(const Source32Args &a, cudaStream_t s) {
   long long n = (long long)a.g.n[0] * a.g.n[1] * a.g.n[2];
   const unsigned nb = (unsigned)((n + 127) / 128);

@@ -63,6 +63,20 @@ cudaError_t chem_step(const Grid &g, const Phys &ph, const Fields &f, double dt,
   return cudaGetLastError();
 }
 
+cudaError_t shield(const Grid &g, const Phys &ph, const Fields &f, double *tau, double dxh, cudaStream_t s) {
+  long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+  shield_tau_kernel<<<nblk(n, 128), 128, 0, s>>>(g, ph, f, tau);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return shield_scan(g, f, tau, dxh, s);
+}
+
+cudaError_t shield_scan(const Grid &g, const Fields &f, const double *tau, double dxh, cudaStream_t s) {
+  long long n = (long long)g.n[1] * g.n[2];
+  shield_scan_kernel<<<nblk(n, 128), 128, 0, s>>>(g, f, tau, dxh);
+  return cudaGetLastError();
+}
+
 cudaError_t chem_totals(const Grid &g, const Fields &f, int plus, cudaStream_t s) {
   long long n = (long long)(g.n[0] + plus) * (g.n[1] + plus) * (g.n[2] + plus);
   chem_totals_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f, plus);

@@ -40,6 +40,11 @@ cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s);
 cudaError_t source_pass(const SourceArgs &a, cudaStream_t s);
 cudaError_t chem_step(const Grid &g, const Phys &ph, const Fields &f, double dt, int *err, cudaStream_t s);
 cudaError_t chem_totals(const Grid &g, const Fields &f, int plus, cudaStream_t s);
+// SHIELD: the optical-depth source term (FP64 / chosen form) into tau, then
+// the columns from both x sides (FP64 sums)
+cudaError_t shield(const Grid &g, const Phys &ph, const Fields &f, double *tau, double dxh, cudaStream_t s);
+cudaError_t shield_fp32(const Grid &g, const Phys &ph, const Fields &f, double *tau, double dxh, cudaStream_t s);
+cudaError_t shield_scan(const Grid &g, const Fields &f, const double *tau, double dxh, cudaStream_t s);
 cudaError_t chem_step_fp32(const Grid &g, const Phys &ph, const Fields &f, double dt, int *err, cudaStream_t s);
 cudaError_t dt_reduce(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
                       cudaStream_t s);

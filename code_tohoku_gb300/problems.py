@@ -57,6 +57,7 @@ class MhdParams:
     ifthrm: int = 2
     dissip: int = 1
     ifchem: int = 0     # 2: chemistry network + species cooling (the shipped deck's); 0: KI cooling
+    ifrad: int = 0      # 2: SHIELD column densities (x sides); 0: columns 0 (the shipped deck's)
 
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)

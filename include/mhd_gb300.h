@@ -73,6 +73,9 @@ typedef struct mhd_params {
   int ifchem;                  /* 2: the reference's chemistry network and
                                   species cooling (:2576-2776, :2825-2880);
                                   0: the KI cooling function                */
+  int ifrad;                   /* 2: SHIELD column densities from both x
+                                  sides (:2924-3036) for the species cooling
+                                  and the rates; 0: columns 0 (the deck's) */
 } mhd_params;
 
 /* Inflow boundary data (BC code 4 on an x side): the values a ghost cell on
@@ -111,6 +114,11 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species,
                const double *dy, const double *z, const double *dz);
 /* SAVEU: copies U and species back (bcc may be NULL; else 3 blocks). */
 int mhd_download(mhd_handle *h, double *U, double *species, double *bcc);
+/* SHIELD's column densities (ifrad = 2): ten blocks in the layout of U,
+ * Ntot(:,:,:,1), Ntot(:,:,:,2), NH2(1), NH2(2), NnC(1), NnC(2), NCO(1),
+ * NCO(2), tCII(1), tCII(2) (the module arrays of :30, side 1 = column from
+ * x = 0, side 2 = from the far end). */
+int mhd_download_columns(mhd_handle *h, double *columns);
 
 /* Couran + Stblty + min (EVOLVE:569-599 for the whole grid).  *dt is
  * min(tfinal, CFL*tCFL, tLMT); *st is 1 (FastSpd) or 2 (Conduct). */

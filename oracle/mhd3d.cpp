@@ -72,6 +72,7 @@ struct Params {
   int ifchem;         // 2: chemistry network and the species cooling function
                       //    (SOURCE :2576-2776, Fcool :2825-2880); 0: KI cooling
   int dissip;         // 1: DISSIP edge damping (MCF3DSGincfca3.f90:3143-3173)
+  int ifrad;          // 2: SHIELD column densities (:2924-3036); 0: columns stay 0
   int nspecies;       // 8 (all species carried)
 };
 
@@ -92,6 +93,9 @@ struct Mhd3D {
   // and by the chemistry network only, never advected (Fcool and RATES read
   // them as they were after the last chemistry update)
   std::vector<double> nde, ndtot;
+  // SHIELD's columns from the two x sides: Ntot(1,2), NH2(1,2), NnC(1,2),
+  // NCO(1,2), tCII(1,2) (:30, :89-90), 0 unless ifrad = 2
+  std::vector<double> col[10];
   std::vector<float> dtf;   // DTF(-1..nx+2, -1..ny+2, -1..nz+2), REAL*4 like the reference
 
   size_t id(int i, int j, int k) const {
@@ -108,6 +112,7 @@ struct Mhd3D {
     ncell = (size_t)sx * sy * sz;
     for (int f = 1; f <= 8; f++) U[f].assign(ncell, 0.0);
     nde.assign(ncell, 0.0); ndtot.assign(ncell, 0.0);
+    for (auto &v : col) v.assign(ncell, 0.0);
     for (int s = 0; s < 8; s++) sp[s].assign(ncell, 0.0);
     for (int c = 1; c <= 3; c++) { Bcc[c].assign(ncell, 0.0); Vfc[c].assign(ncell, 0.0); EMF[c].assign(ncell, 0.0); }
     for (int c = 1; c <= 2; c++) Blg[c].assign(ncell, 0.0);
@@ -829,7 +834,7 @@ struct Mhd3D {
   // ----------------------------------------- chemistry (ifchem = 2)
   // Column densities (Ntot, NH2, NnC, NCO, tCII) come from SHIELD, which
   // runs only with ifrad = 2; with ifrad = 0 (the shipped deck) they keep
-  // their INITIA value 0 (:476-477), and so they are 0 here.
+  // their INITIA value 0 (:476-477).
   static constexpr double G0 = 1.0, xo = 3.2e-4, dv = 2.0, Tgr = 5.e-3;   // :28
   static double pw(double x, double y) { return detmath::pow(x, y); }
   static double fesc(double tau) {   // :2882-2887
@@ -850,7 +855,8 @@ struct Mhd3D {
   // Fcool (:2825-2880): Ly-alpha, CII, OI, dust recombination and CO
   // cooling minus photo-electric, cosmic-ray and photo-destruction heating
   double FcoolSpecies(double T, size_t c) {
-    const double Ntot1 = 0.0, Ntot2 = 0.0, NH21 = 0.0, NH22 = 0.0, NCO1 = 0.0, NCO2 = 0.0, tC1 = 0.0, tC2 = 0.0;
+    const double Ntot1 = col[0][c], Ntot2 = col[1][c], NH21 = col[2][c], NH22 = col[3][c];
+    const double NCO1 = col[6][c], NCO2 = col[7][c], tC1 = col[8][c], tC2 = col[9][c];
     const double H = sp[SH][c], p = sp[SP][c], H2 = sp[SH2][c], He = sp[SHE][c], Hep = sp[SHEP][c];
     const double Cp = sp[SCP][c], CO = sp[SCO][c], ne = nde[c], nt = ndtot[c];
     double Av1 = 1.63542e-3 * Ntot1, x1 = 6.1714e3 * NH21;
@@ -896,7 +902,8 @@ struct Mhd3D {
   };
   // RATES (:3037-3131) at temperature T of cell c
   Rates RATES(double T, size_t c) {
-    const double Ntot1 = 0.0, Ntot2 = 0.0, NH21 = 0.0, NH22 = 0.0, NCO1 = 0.0, NCO2 = 0.0, NnC1 = 0.0, NnC2 = 0.0;
+    const double Ntot1 = col[0][c], Ntot2 = col[1][c], NH21 = col[2][c], NH22 = col[3][c];
+    const double NCO1 = col[6][c], NCO2 = col[7][c], NnC1 = col[4][c], NnC2 = col[5][c];
     Rates r;
     double Av1 = 1.63542e-3 * Ntot1, x1 = 6.1714e3 * NH21;
     double Av2 = 1.63542e-3 * Ntot2, x2 = 6.1714e3 * NH22;
@@ -1093,7 +1100,44 @@ struct Mhd3D {
       for (int j = 1; j <= Ny; j++)
         for (int i = 1; i <= Nx; i++) CHEM_cell(id(i, j, k), dt);
   }
-  // nde, ndtot from the species (INITIA :471-474), cells 1..n+1
+  // SHIELD (:2924-3036) on one block: the C+ optical-depth source term of
+  // every cell from the previous tCII, then the columns of ndtot, H2, C, CO
+  // and that term from each x side of every (j, k) line, each cell adding
+  // half its width before and half after its own value is stored
+  void SHIELD() {
+    std::vector<double> temp(ncell, 0.0);
+    const double dxh = 0.5 * DX(0, 1);
+    const double dvin = 1.0 / dv;
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny; j++)
+        for (int i = 1; i <= Nx; i++) {
+          size_t c = id(i, j, k);
+          double b21 = fesc(col[8][c]) + fesc(col[9][c]);
+          double T = U[5][c] / (P.kb * (sp[SP][c] + sp[SH][c] + sp[SH2][c] + sp[SHE][c] + sp[SHEP][c]));
+          double n1, n2;
+          LEVC2(T, b21, sp[SH][c], sp[SH2][c], nde[c], sp[SCP][c], n1, n2);
+          temp[c] = 1.15563e1 * (n1 - n2) * dvin;
+        }
+    const std::vector<double> *src[5] = {&ndtot, &sp[SH2], &sp[SC], &sp[SCO], &temp};
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny; j++)
+        for (int side = 0; side < 2; side++) {
+          double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+          for (int s = 1; s <= Nx; s++) {
+            int i = side == 0 ? s : Nx + 1 - s;
+            size_t c = id(i, j, k);
+            for (int q = 0; q < 5; q++) {
+              double v = (*src[q])[c];
+              acc[q] = acc[q] + dxh * v;
+              col[2 * q + side][c] = acc[q];
+              acc[q] = acc[q] + dxh * v;
+            }
+          }
+        }
+  }
+
+  // nde, ndtot from the species (INITIA :471-474), cells 1..n+1, and the
+  // columns set to 0 (:475-476)
   void init_chem_totals() {
     for (int k = 1; k <= Nz + 1; k++)
       for (int j = 1; j <= Ny + 1; j++)
@@ -1101,6 +1145,7 @@ struct Mhd3D {
           size_t c = id(i, j, k);
           nde[c] = sp[SP][c] + sp[SHEP][c] + sp[SCP][c];
           ndtot[c] = sp[SP][c] + sp[SH][c] + 2.0 * sp[SH2][c] + sp[SHE][c] + sp[SHEP][c];
+          for (auto &v : col) v[c] = 0.0;
         }
   }
   static double FcoolN(double T, double NN) {   // KI form, KIcool/1DMHDwCC3.f90:1166-1173
@@ -1141,7 +1186,7 @@ struct Mhd3D {
   void SOURCE(double dt) {   // thermal branch ifthrm=2 (:2477-2572), then chemistry ifchem=2
     // nde and ndtot from the species of cells 1..n (:2460-2463); only the
     // species cooling and the network read them
-    if (P.ifchem == 2)
+    if (P.ifchem == 2 || P.ifrad == 2)
       for (int k = 1; k <= Nz; k++)
         for (int j = 1; j <= Ny; j++)
           for (int i = 1; i <= Nx; i++) {
@@ -1149,6 +1194,7 @@ struct Mhd3D {
             nde[c] = sp[SP][c] + sp[SHEP][c] + sp[SCP][c];
             ndtot[c] = sp[SP][c] + sp[SH][c] + 2.0 * sp[SH2][c] + sp[SHE][c] + sp[SHEP][c];
           }
+    if (P.ifrad == 2) SHIELD();   // :2466-2468
     if (P.ifthrm == 2) SOURCE_thermal(dt);
     if (P.ifchem == 2) CHEM(dt);
   }
@@ -1308,7 +1354,7 @@ struct Mhd3D {
 
 extern "C" {
 
-// params (doubles): nx,ny,nz, CFL,facdep,tfinal, bc[6], pmin,pmax,rmin, kb,Kcond, ifthrm, dissip, ifchem
+// params (doubles): nx,ny,nz, CFL,facdep,tfinal, bc[6], pmin,pmax,rmin, kb,Kcond, ifthrm, dissip, ifchem, ifrad
 void *o3d_create(const double *p) {
   Params P{};
   P.nx = (int)p[0]; P.ny = (int)p[1]; P.nz = (int)p[2];
@@ -1318,6 +1364,7 @@ void *o3d_create(const double *p) {
   P.kb = p[15]; P.Kcond = p[16];
   P.ifthrm = (int)p[17]; P.dissip = (int)p[18];
   P.ifchem = (int)p[19];
+  P.ifrad = (int)p[20];
   P.nspecies = 8;
   Mhd3D *m = new Mhd3D();
   m->init(P);
@@ -1337,8 +1384,15 @@ void o3d_upload(void *h, const double *U, const double *sp, const double *coords
     memcpy(m->xc[d].data(), coords + off, n * sizeof(double)); off += n;
     memcpy(m->dxc[d].data(), coords + off, n * sizeof(double)); off += n;
   }
-  m->init_chem_totals();
   m->CC4();
+  m->init_chem_totals();   // nde, ndtot and the columns (:471-477)
+  if (m->P.ifrad == 2)
+    for (int l = 0; l < 20; l++) m->SHIELD();   // :479
+}
+
+void o3d_columns(void *h, double *out) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  for (int q = 0; q < 10; q++) memcpy(out + q * m->ncell, m->col[q].data(), m->ncell * sizeof(double));
 }
 
 void o3d_download(void *h, double *U, double *sp, double *bcc) {

@@ -60,6 +60,7 @@ def lib():
         L.o3d_step.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
         L.o3d_destroy.argtypes = [ctypes.c_void_p]
         L.o3d_set_inflow.argtypes = [ctypes.c_void_p, _P, ctypes.c_void_p, ctypes.c_double]
+        L.o3d_columns.argtypes = [ctypes.c_void_p, _P]
         L.o3d_ki_label.restype = ctypes.c_double
         L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
@@ -107,7 +108,7 @@ class Oracle3D:
     def __init__(self, params):
         p = params
         v = [p.nx, p.ny, p.nz, p.cfl, p.facdep, p.tfinal, *p.bc, p.pmin, p.pmax, p.rmin,
-             p.kb, p.kcond, p.ifthrm, p.dissip, getattr(p, "ifchem", 0)]
+             p.kb, p.kcond, p.ifthrm, p.dissip, getattr(p, "ifchem", 0), getattr(p, "ifrad", 0)]
         self.params = p
         self.shape = (p.nz + 4, p.ny + 4, p.nx + 4)
         self.h = lib().o3d_create(_ptr(np.array(v, dtype=np.float64)))
@@ -132,6 +133,13 @@ class Oracle3D:
 
     def source(self, dt):
         lib().o3d_source(self.h, dt)
+
+    def columns(self):
+        """SHIELD's ten column arrays (Ntot, NH2, NnC, NCO, tCII; each from
+        the left and the right), padded layout."""
+        out = np.zeros((10,) + self.shape)
+        lib().o3d_columns(self.h, _ptr(out))
+        return out
 
     def sweep(self, d, dt):
         lib().o3d_sweep(self.h, d, dt)

@@ -90,3 +90,51 @@ def test_chem_steps_stay_finite():
     # periodic box: the nuclei totals are conserved by advection and network
     for a, b in zip(nuclei(sp0), nuclei(sp)):
         np.testing.assert_allclose(b[C].sum(), a[C].sum(), rtol=1e-10)
+
+
+def shield_state(n=12, seed=5):
+    st = chem_state(n, seed)
+    st.params = st.params.replace(ifrad=2)
+    return st
+
+
+def column_totals(o, st):
+    """Σ dx ndtot along x of every (j, k) line, from the species of the state
+    the oracle holds (ndtot of INITIA, :473)."""
+    _, sp, _ = o.download()
+    ndtot = sp[1] + sp[0] + 2.0 * sp[2] + sp[3] + sp[4]
+    return (ndtot[C] * st.dx[2]).sum(axis=2)
+
+
+def test_shield_columns_split_the_line_total():
+    """SHIELD (:2924-3036): the column from the left plus the column from the
+    right of every cell is the whole line's column Σ dx ndtot."""
+    st = shield_state()
+    o = Oracle3D(st.params)
+    o.upload(st)
+    cols = o.columns()
+    tot = column_totals(o, st)
+    np.testing.assert_allclose((cols[0] + cols[1])[C], np.repeat(tot[:, :, None], st.params.nx, axis=2),
+                               rtol=1e-12)
+    # the left columns grow along x, the right ones shrink
+    assert np.all(np.diff(cols[0][C], axis=2) > 0) and np.all(np.diff(cols[1][C], axis=2) < 0)
+    # H2, C and CO columns likewise split their line totals
+    _, sp, _ = o.download()
+    for q, s in ((1, 2), (2, 5), (3, 7)):
+        line = (sp[s][C] * st.dx[2]).sum(axis=2)
+        np.testing.assert_allclose((cols[2 * q] + cols[2 * q + 1])[C],
+                                   np.repeat(line[:, :, None], st.params.nx, axis=2), rtol=1e-12)
+
+
+def test_shield_changes_the_microphysics():
+    """With columns the species cooling and the rates see shielding: the
+    same source step gives a different state than with ifrad = 0."""
+    st = shield_state()
+    outs = []
+    for ifrad in (0, 2):
+        o = Oracle3D(st.params.replace(ifrad=ifrad))
+        o.upload(st)
+        o.source(0.05)
+        outs.append(o.download())
+    assert not np.array_equal(outs[0][0][4], outs[1][0][4])
+    assert not np.array_equal(outs[0][1][2], outs[1][1][2])
