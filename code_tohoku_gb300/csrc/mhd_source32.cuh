@@ -225,23 +225,26 @@ __global__ void __launch_bounds__(DEFER ? kSourceDeferThreads : 128) source32_ke
   const bool stiff = valid && c.stiff;
   if constexpr (DEFER) {
     // block-aggregated append of the stiff cells' indices: one atomic per
-    // block on the shared counter
-    __shared__ unsigned wcnt[kSourceDeferThreads / 32];
-    __shared__ unsigned long long bbase;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned m = __ballot_sync(0xffffffffu, stiff);
-    if (lane == 0) wcnt[w] = __popc(m);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned tot = 0;
-      for (int q = 0; q < (int)(blockDim.x >> 5); q++) tot += wcnt[q];
-      bbase = tot ? atomicAdd(A.stiff_count, (unsigned long long)tot) : 0ull;
-    }
-    __syncthreads();
-    if (stiff) {
-      unsigned long long pos = bbase;
-      for (int q = 0; q < w; q++) pos += wcnt[q];
-      A.stiff_list[pos + __popc(m & ((1u << lane) - 1u))] = (int)t;
+    // block on the shared counter; a block without stiff cells passes one
+    // barrier only
+    if (__syncthreads_or(stiff)) {
+      __shared__ unsigned wcnt[kSourceDeferThreads / 32];
+      __shared__ unsigned long long bbase;
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      const unsigned m = __ballot_sync(0xffffffffu, stiff);
+      if (lane == 0) wcnt[w] = __popc(m);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) tot += wcnt[q];
+        bbase = atomicAdd(A.stiff_count, (unsigned long long)tot);
+      }
+      __syncthreads();
+      if (stiff) {
+        unsigned long long pos = bbase;
+        for (int q = 0; q < w; q++) pos += wcnt[q];
+        A.stiff_list[pos + __popc(m & ((1u << lane) - 1u))] = (int)t;
+      }
     }
     if (!valid || stiff) return;
   }
