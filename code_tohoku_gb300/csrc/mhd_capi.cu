@@ -146,6 +146,8 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   if (!p || !out) return MHD_ERR_ARG;
   *out = nullptr;
   if (p->nx < 4 || p->ny < 4 || p->nz < 4) return MHD_ERR_ARG;
+  // linear cell indices are split in 32-bit arithmetic (split3)
+  if ((long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4) >= (1LL << 31)) return MHD_ERR_ARG;
   for (int q = 0; q < 6; q++)   // codes 1 (free), 3 (periodic), 4 (inflow, x sides only)
     if (!(valid_bc(p->bc[q]) || (q < 2 && p->bc[q] == 4))) return MHD_ERR_ARG;
   if (p->precision != MHD_PREC_FP64 && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;

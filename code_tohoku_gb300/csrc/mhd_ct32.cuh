@@ -40,9 +40,9 @@ __global__ void __launch_bounds__(256) face_velocity32_kernel(Grid g, Fields f, 
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
   if (t >= (long long)nx1 * ny1 * nz1) return;
-  int i = 1 + (int)(t % nx1);
-  int j = 1 + (int)((t / nx1) % ny1);
-  int k = 1 + (int)(t / ((long long)nx1 * ny1));
+  int i, j, k;
+  split3(t, nx1, ny1, i, j, k);
+  i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
   const float *dx = g.dxf[0], *dy = g.dxf[1], *dz = g.dxf[2];
   if (j <= g.n[1] && k <= g.n[2])
@@ -83,9 +83,8 @@ __global__ void __launch_bounds__(128) emf32_kernel(CT32Args A) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long long)ext[0] * ext[1] * ext[2]) return;
   int c3[3];
-  c3[0] = 1 + (int)(t % ext[0]);
-  c3[1] = 1 + (int)((t / ext[0]) % ext[1]);
-  c3[2] = 1 + (int)(t / ((long long)ext[0] * ext[1]));
+  split3(t, ext[0], ext[1], c3[0], c3[1], c3[2]);
+  c3[0] += 1; c3[1] += 1; c3[2] += 1;
   const int aa = c3[da], bb = c3[db];
   long long p0 = gidx(g, c3[0], c3[1], c3[2]);
   const long long sa = g.st[da], sb = g.st[db];
@@ -180,9 +179,9 @@ __global__ void __launch_bounds__(256) face_b32_kernel(Grid g, Fields f, const f
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
   if (t >= (long long)nx1 * ny1 * nz1) return;
-  int i = 1 + (int)(t % nx1);
-  int j = 1 + (int)((t / nx1) % ny1);
-  int k = 1 + (int)(t / ((long long)nx1 * ny1));
+  int i, j, k;
+  split3(t, nx1, ny1, i, j, k);
+  i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
   long long sx = 1, sy = g.st[1], sz = g.st[2];
   const double cx = dt * g.rdxc[0][i + 1], cy = dt * g.rdxc[1][j + 1], cz = dt * g.rdxc[2][k + 1];

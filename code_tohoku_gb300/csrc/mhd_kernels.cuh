@@ -96,6 +96,23 @@ __host__ __device__ inline long long gidx(const Grid &g, int i, int j, int k) {
   return (long long)(i + 1) + g.st[1] * (long long)(j + 1) + g.st[2] * (long long)(k + 1);
 }
 
+// The 0-based (i, j, k) of a linear index t over an nx x ny box of
+// positions, in 32-bit unsigned arithmetic: every linear index here is
+// below 2^31 (mhd_create refuses larger grids), and the 32-bit division is
+// a short multiply sequence where a 64-bit one is a long library routine.
+__host__ __device__ __forceinline__ void split3(long long t, int nx, int ny, int &i, int &j, int &k) {
+  const unsigned u = (unsigned)t, q = u / (unsigned)nx, r = q / (unsigned)ny;
+  i = (int)(u - q * (unsigned)nx);
+  j = (int)(q - r * (unsigned)ny);
+  k = (int)r;
+}
+// the padded index of interior cell t of the n[0] x n[1] x n[2] block
+__host__ __device__ __forceinline__ long long gidx_lin(const Grid &g, long long t, int nx, int ny) {
+  int i, j, k;
+  split3(t, nx, ny, i, j, k);
+  return gidx(g, 1 + i, 1 + j, 1 + k);
+}
+
 // density of inflow ghost cell gi of row (j,k): DTF at the upstream position
 // x - time vx_in, wrapped into the box (BC_MPI :821-825, :857-861).  The
 // operation order is the reference's; the index is clamped into the padded
@@ -308,7 +325,7 @@ template <class R, class Load, class Store>
 __device__ __forceinline__ void shield_tau_cell(const Grid &g, const Phys &ph, const Fields &f, double *tau,
                                                 long long t, Load &&ld, Store &&st) {
   const int nx = g.n[0], ny = g.n[1];
-  const long long a = gidx(g, 1 + (int)(t % nx), 1 + (int)((t / nx) % ny), 1 + (int)(t / ((long long)nx * ny)));
+  const long long a = gidx_lin(g, t, nx, ny);
   const CellSpecies<R> c = cell_species<R>(f, a, ld);
   tau[a] = st(shield_tau_source<R>(ld(f.U[4][a]), ld(ph.kb), c));
 }
@@ -332,9 +349,9 @@ __global__ void ghost_fill_kernel(Grid g, FillArgs a, int d, int nol, int specie
   long long nl = (long long)g.s[o1] * g.s[o2];
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nl * a.nf) return;
-  int fi = (int)(t / nl);
-  long long r = t - (long long)fi * nl;
-  int q1 = (int)(r % g.s[o1]) - 1, q2 = (int)(r / g.s[o1]) - 1;
+  int q1, q2, fi;
+  split3(t, g.s[o1], g.s[o2], q1, q2, fi);
+  q1 -= 1; q2 -= 1;
   int c[3];
   c[o1] = q1;
   c[o2] = q2;
@@ -791,9 +808,9 @@ __global__ void face_velocity_kernel(Grid g, Fields f, double *vf0, double *vf1,
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
   if (t >= (long long)nx1 * ny1 * nz1) return;
-  int i = 1 + (int)(t % nx1);
-  int j = 1 + (int)((t / nx1) % ny1);
-  int k = 1 + (int)(t / ((long long)nx1 * ny1));
+  int i, j, k;
+  split3(t, nx1, ny1, i, j, k);
+  i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
   const double *dx = g.dx[0], *dy = g.dx[1], *dz = g.dx[2];
   if (j <= g.n[1] && k <= g.n[2])
@@ -936,9 +953,9 @@ __global__ void face_b_kernel(Grid g, Fields f, const double *Ez, const double *
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
   if (t >= (long long)nx1 * ny1 * nz1) return;
-  int i = 1 + (int)(t % nx1);
-  int j = 1 + (int)((t / nx1) % ny1);
-  int k = 1 + (int)(t / ((long long)nx1 * ny1));
+  int i, j, k;
+  split3(t, nx1, ny1, i, j, k);
+  i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
   long long sx = 1, sy = g.st[1], sz = g.st[2];
   const double *dx = g.dx[0], *dy = g.dx[1], *dz = g.dx[2];
@@ -955,9 +972,9 @@ __global__ void cell_b_kernel(Grid g, Fields f) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   if (t >= (long long)nx * ny * nz) return;
-  int i = 1 + (int)(t % nx);
-  int j = 1 + (int)((t / nx) % ny);
-  int k = 1 + (int)(t / ((long long)nx * ny));
+  int i, j, k;
+  split3(t, nx, ny, i, j, k);
+  i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
   f.bcc[0][a] = 0.5 * (f.U[5][a] + f.U[5][a + 1]);
   f.bcc[1][a] = 0.5 * (f.U[6][a] + f.U[6][a + g.st[1]]);
@@ -1042,9 +1059,9 @@ __device__ __forceinline__ double ntot_imc(const Fields &f, long long a) {
 __device__ __forceinline__ void cell_dt_limits(const Grid &g, const Phys &ph, const Fields &f, long long t,
                                                double &c_min, double &s_min) {
   int nx = g.n[0], ny = g.n[1];
-  int i = 1 + (int)(t % nx);
-  int j = 1 + (int)((t / nx) % ny);
-  int k = 1 + (int)(t / ((long long)nx * ny));
+  int i, j, k;
+  split3(t, nx, ny, i, j, k);
+  i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
   double H = f.sp[0][a], pr = f.sp[1][a], H2 = f.sp[2][a], He = f.sp[3][a], Hep = f.sp[4][a];
   double gam = gam_of(H, pr, He, Hep, H2);
@@ -1081,9 +1098,9 @@ __global__ void source_kernel(SourceArgs A) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   if (t >= (long long)nx * ny * nz) return;
-  int i = 1 + (int)(t % nx);
-  int j = 1 + (int)((t / nx) % ny);
-  int k = 1 + (int)(t / ((long long)nx * ny));
+  int i, j, k;
+  split3(t, nx, ny, i, j, k);
+  i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
   const double kb = A.ph.kb, Kc = A.ph.kcond, dt = A.dt;
   const double *pin = A.pin;
@@ -1142,7 +1159,7 @@ __global__ void chem_kernel(Grid g, Phys ph, Fields f, double dt, int *err) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   if (t >= (long long)nx * ny * nz) return;
-  long long a = gidx(g, 1 + (int)(t % nx), 1 + (int)((t / nx) % ny), 1 + (int)(t / ((long long)nx * ny)));
+  long long a = gidx_lin(g, t, nx, ny);
   CellSpecies<double> c = cell_species<double>(f, a, [](double v) { return v; });
   const double (&mn)[8] = ph.ndmin;
   chem_network<double>(c, f.U[4][a], ph.kb, dt, mn);
@@ -1193,7 +1210,7 @@ __global__ void chem_totals_kernel(Grid g, Fields f, int plus) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx = g.n[0] + plus, ny = g.n[1] + plus, nz = g.n[2] + plus;
   if (t >= (long long)nx * ny * nz) return;
-  long long a = gidx(g, 1 + (int)(t % nx), 1 + (int)((t / nx) % ny), 1 + (int)(t / ((long long)nx * ny)));
+  long long a = gidx_lin(g, t, nx, ny);
   f.nde[a] = f.sp[1][a] + f.sp[4][a] + f.sp[6][a];
   f.ndtot[a] = f.sp[1][a] + f.sp[0][a] + 2.0 * f.sp[2][a] + f.sp[3][a] + f.sp[4][a];
 }
@@ -1210,9 +1227,9 @@ __global__ void dt_kernel(Grid g, Phys ph, Fields f, unsigned long long *out /* 
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   double c_min = ph.tfinal, s_min = ph.tfinal;
   if (t < (long long)nx * ny * nz) {
-    int i = 1 + (int)(t % nx);
-    int j = 1 + (int)((t / nx) % ny);
-    int k = 1 + (int)(t / ((long long)nx * ny));
+    int i, j, k;
+    split3(t, nx, ny, i, j, k);
+    i += 1; j += 1; k += 1;
     long long a = gidx(g, i, j, k);
     double H = f.sp[0][a], pr = f.sp[1][a], H2 = f.sp[2][a], He = f.sp[3][a], Hep = f.sp[4][a];
     double gam = gam_of(H, pr, He, Hep, H2);
@@ -1308,9 +1325,9 @@ __global__ void diag_kernel(Grid g, Phys ph, Fields f, double *part /* 6 per blo
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   double v[6] = {0, 0, 0, 0, 0, 0};
   if (t < (long long)nx * ny * nz) {
-    int i = 1 + (int)(t % nx);
-    int j = 1 + (int)((t / nx) % ny);
-    int k = 1 + (int)(t / ((long long)nx * ny));
+    int i, j, k;
+    split3(t, nx, ny, i, j, k);
+    i += 1; j += 1; k += 1;
     long long a = gidx(g, i, j, k);
     double dV = g.dx[0][i + 1] * g.dx[1][j + 1] * g.dx[2][k + 1];
     double rho = f.U[0][a];

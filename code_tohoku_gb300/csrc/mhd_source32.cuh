@@ -102,9 +102,9 @@ template <bool CHEM>
 __device__ __forceinline__ Cell32<CHEM> source32_prep(const Source32Args &A, long long t) {
   const Grid &g = A.g;
   const int nx = g.n[0], ny = g.n[1];
-  const int i = 1 + (int)(t % nx);
-  const int j = 1 + (int)((t / nx) % ny);
-  const int k = 1 + (int)(t / ((long long)nx * ny));
+  int i, j, k;
+  split3(t, nx, ny, i, j, k);
+  i += 1; j += 1; k += 1;
   Cell32<CHEM> c;
   const long long a = gidx(g, i, j, k);
   c.a = a;
@@ -293,9 +293,9 @@ __global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, un
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   float c_min = d2f(ph.tfinal), s_min = c_min;
   if (t < (long long)nx * ny * nz) {
-    int i = 1 + (int)(t % nx);
-    int j = 1 + (int)((t / nx) % ny);
-    int k = 1 + (int)(t / ((long long)nx * ny));
+    int i, j, k;
+    split3(t, nx, ny, i, j, k);
+    i += 1; j += 1; k += 1;
     long long a = gidx(g, i, j, k);
     float H = d2f(f.sp[0][a]), pr = d2f(f.sp[1][a]), H2 = d2f(f.sp[2][a]), He = d2f(f.sp[3][a]),
           Hep = d2f(f.sp[4][a]);
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(128) chem32_kernel(Grid g, Phys ph, Fields f, 
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   if (t >= (long long)nx * ny * nz) return;
-  long long a = gidx(g, 1 + (int)(t % nx), 1 + (int)((t / nx) % ny), 1 + (int)(t / ((long long)nx * ny)));
+  long long a = gidx_lin(g, t, nx, ny);
   CellSpecies<float> c = cell_species<float>(f, a, [](double v) { return d2f(v); });
   float mn[8];
   for (int q = 0; q < 8; q++) mn[q] = d2f(ph.ndmin[q]);

@@ -58,7 +58,8 @@ extern "C" {
 #define MHD_COOL_SURROGATE 1   /* MLP surrogate with exact fallback          */
 
 typedef struct mhd_params {
-  int nx, ny, nz;              /* interior cells (Ncellx, Ncelly, Ncellz)   */
+  int nx, ny, nz;              /* interior cells (Ncellx, Ncelly, Ncellz);
+                                  (nx+4)(ny+4)(nz+4) must be below 2^31  */
   double cfl, facdep, tfinal;  /* INPUT3D.DAT rows 13-14                    */
   int bc[6];                   /* BCx1,BCx2,BCy1,BCy2,BCz1,BCz2: 1 = free
                                   (zero-gradient), 3 = periodic, 4 = inflow
