@@ -37,6 +37,7 @@ struct mhd_handle {
   double *colblock = nullptr;     // SHIELD's ten column arrays (ifrad = 2)
   double dxh = 0.0;               // SHIELD's half width 0.5 dx(1)
   float *temp32 = nullptr;
+  float *nsum32 = nullptr;               // SOURCE's FP32 species sum (predictor -> corrector)
   int *stiff_list = nullptr;             // SOURCE's stiff cells (FP32 form with a surrogate)
   float *vf32[3] = {nullptr, nullptr, nullptr};
   float *bf32[3] = {nullptr, nullptr, nullptr};
@@ -226,7 +227,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     for (int q = 0; q < 10; q++) h->f.col[q] = h->colblock + (size_t)q * g.ncell;
   }
   if (p->precision == MHD_PREC_FP32) {
-    const size_t nf = 13;   // 12 FP32 arrays + the stiff-cell list of SOURCE
+    const size_t nf = 14;   // 13 FP32 arrays + the stiff-cell list of SOURCE
     size_t fbytes = nf * (size_t)g.ncell * sizeof(float);
     if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess) {
       cudaGetLastError();
@@ -235,6 +236,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     }
     float *fq = h->fblock;
     h->temp32 = fq; fq += g.ncell;
+    h->nsum32 = fq; fq += g.ncell;
     for (int c = 0; c < 3; c++) { h->vf32[c] = fq; fq += g.ncell; }
     for (int c = 0; c < 3; c++) { h->bf32[c] = fq; fq += g.ncell; }
     h->rn32 = fq; fq += g.ncell;
@@ -446,12 +448,12 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
     // with a surrogate, source_fp32 launches a second (stiff-cell) kernel
     const int extra = (a.W && h->ph.ifchem != 2) ? 1 : 0;
-    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
+    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->nsum32, true, h->stream));
     CK(source_fp32(a, h->stream));
     h->launches += extra;
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
-    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->stream));
+    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->nsum32, false, h->stream));
     CK(source_fp32(a, h->stream));
     h->launches += extra;
     return MHD_OK;

@@ -20,7 +20,10 @@ cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s);
 // chosen form (FP32 reconstruction / Riemann / characteristics / EMF)
 cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s);
 cudaError_t source_fp32(const Source32Args &a, cudaStream_t s);
-cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, cudaStream_t s);
+// FP32 temperatures of every padded cell; from_species: from the species
+// (and store their sum in nsum), else from the sum stored by the last call
+cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *nsum,
+                      bool from_species, cudaStream_t s);
 cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
                            cudaStream_t s);
 cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
