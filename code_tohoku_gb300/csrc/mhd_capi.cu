@@ -107,17 +107,29 @@ const double kNdMinH = 0.91, kNdMinHe = 0.09;
 
 // ghost exchange of a list of arrays in the directions of mask (x,y,z order);
 // rules: the BC=4 rule of each array on an inflow side of x
-int fill(mhd_handle *h, std::initializer_list<double *> arrays, int dirs, int nol, int species = 0,
-         std::initializer_list<int> rules = {}) {
+// BC_MPI-style exchange of up to 8 arrays along the directions in dirs (bit
+// d), nol ghost layers; spmask bit q: array q is a species array, whose
+// free-boundary copy covers interior transverse lines only
+int fill_mask(mhd_handle *h, const double *const *arrays, int n, int dirs, int nol, unsigned spmask,
+              const int *rules, int nrules) {
   FillArgs a{};
-  a.nf = 0;
-  for (double *p : arrays) a.f[a.nf++] = p;
-  int q = 0;
-  for (int r : rules) a.rule[q++] = r;
+  a.nf = n;
+  for (int q = 0; q < n; q++) a.f[q] = const_cast<double *>(arrays[q]);
+  for (int q = 0; q < nrules; q++) a.rule[q] = rules[q];
+  a.spmask = spmask;
   a.in = h->ph.in;
   for (int d = 0; d < 3; d++)
-    if (dirs & (1 << d)) CK(ghost_fill(h->g, a, d, nol, species, h->stream));
+    if (dirs & (1 << d)) CK(ghost_fill(h->g, a, d, nol, h->stream));
   return MHD_OK;
+}
+
+int fill(mhd_handle *h, std::initializer_list<double *> arrays, int dirs, int nol, int species = 0,
+         std::initializer_list<int> rules = {}) {
+  const double *arr[8];
+  int n = 0, nr = 0, r[8];
+  for (double *p : arrays) arr[n++] = p;
+  for (int x : rules) r[nr++] = x;
+  return fill_mask(h, arr, n, dirs, nol, species ? (1u << n) - 1u : 0u, r, nr);
 }
 
 int check_err(mhd_handle *h) {
@@ -430,9 +442,10 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
   if (rho_sp_filled) {
     TRY(fill(h, {h->f.U[4]}, 7, 1, 0, {IN_P}));
   } else {
-    TRY(fill(h, {h->f.U[0], h->f.U[4]}, 7, 1, 0, {IN_RHO, IN_P}));
-    TRY(fill(h, {h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]}, 7, 1, 1,
-             {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4}));
+    // rho and p, and the species (interior transverse lines), in one exchange
+    const double *arr[7] = {h->f.U[0], h->f.U[4], h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]};
+    const int rules[7] = {IN_RHO, IN_P, IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4};
+    TRY(fill_mask(h, arr, 7, 7, 1, 0x7cu, rules, 7));
   }
   if (h->p.precision == MHD_PREC_FP32) {
     if (h->p.cooling == MHD_COOL_SURROGATE && !h->sur_net)
@@ -519,18 +532,25 @@ int ct_impl(mhd_handle *h, double dt, bool rho_filled) {
   Fields &f = h->f;
   // CC(1) :2122-2137
   TRY(need_inflow(h));
-  TRY(fill(h, {f.U[1], f.U[6], f.U[7]}, 1, 2, 0, {IN_V1, IN_B2, IN_B3}));
-  TRY(fill(h, {f.U[2], f.U[5], f.U[7]}, 2, 2));
-  TRY(fill(h, {f.U[3], f.U[5], f.U[6]}, 4, 2));
+  // with them, the x, y and z exchanges of p and rho that CC(2) needs
+  // (:2142; nothing in between changes either)
+  {
+    const int n = rho_filled ? 4 : 5;
+    const double *ax[5] = {f.U[1], f.U[6], f.U[7], f.U[4], f.U[0]};
+    const double *ay[5] = {f.U[2], f.U[5], f.U[7], f.U[4], f.U[0]};
+    const double *az[5] = {f.U[3], f.U[5], f.U[6], f.U[4], f.U[0]};
+    const int rx[5] = {IN_V1, IN_B2, IN_B3, IN_P, IN_RHO};
+    TRY(fill_mask(h, ax, n, 1, 2, 0u, rx, n));
+    TRY(fill_mask(h, ay, n, 2, 2, 0u, nullptr, 0));
+    TRY(fill_mask(h, az, n, 4, 2, 0u, nullptr, 0));
+  }
   const bool fp32 = h->p.precision == MHD_PREC_FP32;
   if (fp32) CK(face_velocity_fp32(h->g, f, h->vf[0], h->vf[1], h->vf[2], h->stream));
   else CK(face_velocity(h->g, f, h->vf[0], h->vf[1], h->vf[2], h->stream));
   TRY(fill(h, {h->vf[1], h->vf[2]}, 1, 2, 0, {IN_VFC, IN_VFC}));
   TRY(fill(h, {h->vf[0], h->vf[2]}, 2, 2));
   TRY(fill(h, {h->vf[0], h->vf[1]}, 4, 2));
-  TRY(fill(h, {f.U[4]}, 7, 2, 0, {IN_P}));
-  // CC(2) for Ez :2142
-  if (!rho_filled) TRY(fill(h, {f.U[0]}, 7, 2, 0, {IN_RHO}));
+  // CC(2) for Ez :2142 (p and rho exchanged above)
   if (fp32) {
     CT32Args a{};
     a.g = h->g;

@@ -26,9 +26,9 @@ cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s) { return launch_emf
 
 static unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-cudaError_t ghost_fill(const Grid &g, const FillArgs &f, int d, int nol, int species, cudaStream_t s) {
+cudaError_t ghost_fill(const Grid &g, const FillArgs &f, int d, int nol, cudaStream_t s) {
   long long n = (long long)g.s[(d + 1) % 3] * g.s[(d + 2) % 3] * f.nf;
-  ghost_fill_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f, d, nol, species);
+  ghost_fill_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f, d, nol);
   return cudaGetLastError();
 }
 

@@ -340,11 +340,12 @@ struct FillArgs {
   double *f[8];
   int nf;
   int rule[8];          // BC=4 rule per array (IN_KEEP where x has no inflow rule)
+  unsigned spmask;      // bit q: array q is a species array (interior transverse lines only)
   InflowDev in;
 };
 
 #ifdef MHD_COMMON_KERNELS
-__global__ void ghost_fill_kernel(Grid g, FillArgs a, int d, int nol, int species) {
+__global__ void ghost_fill_kernel(Grid g, FillArgs a, int d, int nol) {
   int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
   long long nl = (long long)g.s[o1] * g.s[o2];
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -359,6 +360,7 @@ __global__ void ghost_fill_kernel(Grid g, FillArgs a, int d, int nol, int specie
   long long base = gidx(g, c[0], c[1], c[2]);
   long long sd = g.st[d];
   double *F = a.f[fi];
+  const bool species = (a.spmask >> fi) & 1u;
   int N = g.n[d];
   bool tr_in = q1 >= 1 && q1 <= g.n[o1] && q2 >= 1 && q2 <= g.n[o2];
   bool fl = g.bcl[d] == 1 && (!species || tr_in);
