@@ -68,7 +68,7 @@ def test_colliding_flows_steps_bit_exact():
     compare(g, o)
 
 
-@pytest.mark.parametrize("shape", [(12, 10, 8), (9, 7, 11)])
+@pytest.mark.parametrize("shape", [(12, 10, 8), (9, 7, 11), (264, 8, 4)])
 def test_non_cubic_grids_bit_exact(shape):
     nx, ny, nz = shape
     st = problems.turbulence(1, kmax=2)   # placeholder for the physics values
