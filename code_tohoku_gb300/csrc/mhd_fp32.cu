@@ -43,11 +43,25 @@ constexpr size_t kSweepSmemPerCta = (227 * 1024) / MHD_SWEEP_MIN_BLOCKS - 1024;
 #endif
 constexpr int kSweepFixedStride = MHD_SWEEP_FIXED_STRIDE;
 
-template <int DIR, int P, int LS = 0>
+// Pencils of 257..512 cells (the 512^3 grid): a second compile-time stride
+// (516), with the shape measured best per direction at 512^3 (ms per sweep
+// x / y / z): the x sweep two pencils per CTA and two CTAs per SM (17.0 /
+// 34.3 / 43.2 for all three that way), the y and z sweeps four pencils per
+// CTA -- full 32-byte rows -- and one 768-thread CTA per SM (19.0 / 22.1 /
+// 30.5); the run-time stride with two pencils gave 18.5 / 34.5 / 43.4.
+#ifndef MHD_SWEEP_LONG_STRIDE
+#define MHD_SWEEP_LONG_STRIDE 516
+#endif
+#ifndef MHD_SWEEP_LONG_THREADS
+#define MHD_SWEEP_LONG_THREADS 768
+#endif
+constexpr int kSweepLongStride = MHD_SWEEP_LONG_STRIDE;
+
+template <int DIR, int P, int LS, int NT, int MINB>
 static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
   const Grid &g = a.g;
   size_t smem = sweep32_smem_bytes(g.n[DIR], P, LS);
-  auto k = sweep32_kernel<DIR, P, sweep_threads<DIR>(), kSweepMinBlocks, LS>;
+  auto k = sweep32_kernel<DIR, P, NT, MINB, LS>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // x sweep: P adjacent y rows per CTA; y and z sweeps: P adjacent x columns
@@ -57,22 +71,33 @@ static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
   if (DIR == 0) grid = dim3(g.n[1] / P, g.n[2]);
   else if (DIR == 1) grid = dim3(xgroups, g.n[2]);
   else grid = dim3(xgroups, g.n[1]);
-  k<<<grid, sweep_threads<DIR>(), smem, s>>>(a);
+  k<<<grid, NT, smem, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int DIR>
 static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
+  constexpr int NT = sweep_threads<DIR>(), MB = kSweepMinBlocks;
   // the x sweep needs P to divide ny; the y and z sweeps pad their groups
   const int nb = (DIR == 0) ? a.g.n[1] : 4;
-  if (MHD_SWEEP_MAX_PENCILS >= 4 && nb % 4 == 0 && a.g.n[DIR] + 4 <= kSweepFixedStride &&
+  const int L = a.g.n[DIR] + 4;
+  if (MHD_SWEEP_MAX_PENCILS >= 4 && nb % 4 == 0 && L <= kSweepFixedStride &&
       sweep32_smem_bytes(a.g.n[DIR], 4, kSweepFixedStride) <= kSweepSmemPerCta)
-    return launch32<DIR, 4, kSweepFixedStride>(a, s);
+    return launch32<DIR, 4, kSweepFixedStride, NT, MB>(a, s);
+  if (L > kSweepFixedStride && L <= kSweepLongStride) {
+    if constexpr (DIR != 0) {
+      if (sweep32_smem_bytes(a.g.n[DIR], 4, kSweepLongStride) <= 226 * 1024)
+        return launch32<DIR, 4, kSweepLongStride, MHD_SWEEP_LONG_THREADS, 1>(a, s);
+    } else {
+      if (nb % 2 == 0 && sweep32_smem_bytes(a.g.n[DIR], 2, kSweepLongStride) <= kSweepSmemPerCta)
+        return launch32<DIR, 2, kSweepLongStride, NT, MB>(a, s);
+    }
+  }
   if (MHD_SWEEP_MAX_PENCILS >= 4 && nb % 4 == 0 && sweep32_smem_bytes(a.g.n[DIR], 4) <= kSweepSmemPerCta)
-    return launch32<DIR, 4>(a, s);
-  if (nb % 2 == 0 && sweep32_smem_bytes(a.g.n[DIR], 2) <= kSweepSmemPerCta) return launch32<DIR, 2>(a, s);
+    return launch32<DIR, 4, 0, NT, MB>(a, s);
+  if (nb % 2 == 0 && sweep32_smem_bytes(a.g.n[DIR], 2) <= kSweepSmemPerCta) return launch32<DIR, 2, 0, NT, MB>(a, s);
   if (sweep32_smem_bytes(a.g.n[DIR], 1) > 227 * 1024) return cudaErrorInvalidValue;
-  return launch32<DIR, 1>(a, s);
+  return launch32<DIR, 1, 0, NT, MB>(a, s);
 }
 
 cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s) {
