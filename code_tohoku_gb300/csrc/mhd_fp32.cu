@@ -89,7 +89,8 @@ static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
   // pencils cross a 2 MB page every four cells, and wider groups spread the
   // CTAs running at once over fewer pages: 2.68 ms at 256^3 against 2.99
   // with four columns and two CTAs per SM (the y sweep, whose pencils stay
-  // within a page or two, is faster with four: 2.41 against 2.52)
+  // within a page or two, is faster with four: 2.41 against 2.52, and the x
+  // sweep with four rows and two CTAs: 2.16 against 2.58)
   if constexpr (DIR == 2) {
     if (L <= kSweepFixedStride && sweep32_smem_bytes(a.g.n[DIR], 8, kSweepFixedStride) <= 226 * 1024)
       return launch32<DIR, 8, kSweepFixedStride, kSweepZThreads, 1>(a, s);
