@@ -112,11 +112,12 @@ constexpr int kGlobalUnroll = MHD_SWEEP_GLOBAL_UNROLL;
 constexpr int kMergeLoads = MHD_SWEEP_MERGE_LOADS;
 // Bit d set: the finishing phases of the direction-d sweep load every FP64
 // value of a position before using any; clear: each value where it is used.
-// Measured at 256^3 (ms, x / y / z): hoisted 2.16 / 2.41 / 3.21, in place
-// 2.23 / 2.47 / 3.01 -- the z sweep, whose pencils cross a page every few
-// cells, is slower with more loads in flight.
+// Measured at 256^3 (ms, x / y / z): hoisted 2.16 / 2.41 / 2.61, in place
+// 2.23 / 2.47 / 2.68 (the z sweep with eight columns per CTA; with four and
+// two CTAs per SM it was the other way round, 3.21 hoisted against 3.01).
+// Merging the load pass (kMergeLoads) helps the x sweep only (z: 2.69).
 #ifndef MHD_SWEEP_HOIST_LOADS
-#define MHD_SWEEP_HOIST_LOADS 3
+#define MHD_SWEEP_HOIST_LOADS 7
 #endif
 constexpr int kHoistLoads = MHD_SWEEP_HOIST_LOADS;
 
@@ -124,8 +125,8 @@ constexpr int kHoistLoads = MHD_SWEEP_HOIST_LOADS;
 // starts p transverse strides after pencil 0 (adjacent y rows for the x
 // sweep, adjacent x columns for the y and z sweeps).  For the y and z
 // sweeps a group starts at padded x index P*blockIdx.x, so the P words a
-// row of the group reads sit in one 32-byte sector (the padded row length
-// n+4 is a multiple of 4 for n divisible by 4); the group may then contain
+// row of the group reads fill whole 32-byte sectors for P = 4 or 8 (the
+// padded row length n+4 is a multiple of 4 for n divisible by 4); the group may then contain
 // ghost columns (x < 1 or x > n), which are computed along but never
 // stored.  Columns beyond the padded grid read the last column.
 template <int DIR, int P>
