@@ -53,19 +53,36 @@ __global__ void __launch_bounds__(256) face_velocity32_kernel(Grid g, Fields f, 
     vf2[a] = f2d(__fdividef(dz[k] * d2f(f.U[3][a]) + dz[k + 1] * d2f(f.U[3][a - g.st[2]]), dz[k] + dz[k + 1]));
 }
 
+// Two cells per thread (block-strided, so every warp access stays
+// coalesced), all 16 loads issued before the first store: a copy-like
+// kernel needs many loads in flight per SM to approach HBM bandwidth.
 __global__ void __launch_bounds__(256) ct_prep32_kernel(long long ncell, Fields f, const double *vf0,
                                                         const double *vf1, const double *vf2, float kb,
                                                         CT32Args A) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncell) return;
-  const_cast<float *>(A.vf[0])[t] = d2f(vf0[t]);
-  const_cast<float *>(A.vf[1])[t] = d2f(vf1[t]);
-  const_cast<float *>(A.vf[2])[t] = d2f(vf2[t]);
-  for (int c = 0; c < 3; c++) const_cast<float *>(A.bf[c])[t] = d2f(f.U[5 + c][t]);
-  float r = d2f(f.U[0][t]);
-  const_cast<float *>(A.rn)[t] = r;
-  // T = 1.27 p/(kb rho); sign(0.5, T-3)
-  const_cast<float *>(A.sw)[t] = (1.27f * d2f(f.U[4][t]) >= 3.0f * kb * r) ? 0.5f : -0.5f;
+  const long long t0 = (long long)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+  double v[2][8];
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const long long t = t0 + u * blockDim.x;
+    if (t < ncell) {
+      v[u][0] = __ldg(vf0 + t); v[u][1] = __ldg(vf1 + t); v[u][2] = __ldg(vf2 + t);
+      v[u][3] = __ldg(f.U[5] + t); v[u][4] = __ldg(f.U[6] + t); v[u][5] = __ldg(f.U[7] + t);
+      v[u][6] = __ldg(f.U[0] + t); v[u][7] = __ldg(f.U[4] + t);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const long long t = t0 + u * blockDim.x;
+    if (t >= ncell) continue;
+    const_cast<float *>(A.vf[0])[t] = d2f(v[u][0]);
+    const_cast<float *>(A.vf[1])[t] = d2f(v[u][1]);
+    const_cast<float *>(A.vf[2])[t] = d2f(v[u][2]);
+    for (int c = 0; c < 3; c++) const_cast<float *>(A.bf[c])[t] = d2f(v[u][3 + c]);
+    float r = d2f(v[u][6]);
+    const_cast<float *>(A.rn)[t] = r;
+    // T = 1.27 p/(kb rho); sign(0.5, T-3)
+    const_cast<float *>(A.sw)[t] = (1.27f * d2f(v[u][7]) >= 3.0f * kb * r) ? 0.5f : -0.5f;
+  }
 }
 
 // CC(2) + CCT for the edge direction E (0: Ez on x/y, 1: Ex on y/z,

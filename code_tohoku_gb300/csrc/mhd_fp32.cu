@@ -1,6 +1,7 @@
 // mhd_fp32.cu — chosen form: reconstruction, Riemann solver, characteristic
 // and EMF arithmetic in FP32; accumulation into the FP64 state.  Built with
 // the default contraction (FMA) enabled.
+#include <algorithm>
 #define MHD_FP32_KERNELS
 #include "mhd_sweep32.cuh"
 #include "mhd_ct32.cuh"
@@ -124,7 +125,9 @@ cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s) {
 cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
                            cudaStream_t s) {
   long long n = (long long)g.n[0] * g.n[1] * g.n[2];
-  dt32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, out, err);
+  // 4864 blocks of 256 threads (32 per SM): about 13 cells per thread at 256^3
+  const unsigned nb = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 8 * 4);
+  dt32_kernel<<<nb, 256, 0, s>>>(g, ph, f, out, err);
   return cudaGetLastError();
 }
 
@@ -132,7 +135,7 @@ static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1)
 
 cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *nsum,
                       bool from_species, cudaStream_t s) {
-  if (from_species) temp32_kernel<true><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T, nsum);
+  if (from_species) temp32_kernel<true><<<blocks_for(g.ncell, 512), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T, nsum);
   else temp32_kernel<false><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T, nsum);
   return cudaGetLastError();
 }
@@ -145,7 +148,7 @@ cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, doubl
 
 cudaError_t ct_prep_fp32(const Grid &g, const Fields &f, double *const vf[3], double kb, const CT32Args &a,
                          cudaStream_t s) {
-  ct_prep32_kernel<<<blocks_for(g.ncell, 256), 256, 0, s>>>(g.ncell, f, vf[0], vf[1], vf[2], d2f(kb), a);
+  ct_prep32_kernel<<<blocks_for(g.ncell, 512), 256, 0, s>>>(g.ncell, f, vf[0], vf[1], vf[2], d2f(kb), a);
   return cudaGetLastError();
 }
 

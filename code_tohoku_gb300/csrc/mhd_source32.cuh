@@ -76,19 +76,36 @@ namespace mhd {
 // so they are formed once per pass instead of once per neighbour.  The
 // predictor pass also stores the species sum n, which the corrector pass
 // reads instead of the five species (they do not change between passes).
+// The species pass handles two cells per thread (block-strided, loads of
+// both issued first) to keep more loads in flight.
 template <bool FROM_SPECIES>
 __global__ void __launch_bounds__(256) temp32_kernel(long long ncell, Fields f, const double *pin, float kb,
                                                      float *T, float *nsum) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncell) return;
-  float n;
   if constexpr (FROM_SPECIES) {
-    n = d2f(f.sp[1][t]) + d2f(f.sp[0][t]) + d2f(f.sp[2][t]) + d2f(f.sp[3][t]) + d2f(f.sp[4][t]);
-    nsum[t] = n;
+    const long long t0 = (long long)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+    double v[2][6];
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const long long t = t0 + u * blockDim.x;
+      if (t < ncell) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) v[u][q] = __ldg(f.sp[q] + t);
+        v[u][5] = __ldg(pin + t);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const long long t = t0 + u * blockDim.x;
+      if (t >= ncell) continue;
+      const float n = d2f(v[u][1]) + d2f(v[u][0]) + d2f(v[u][2]) + d2f(v[u][3]) + d2f(v[u][4]);
+      nsum[t] = n;
+      T[t] = __fdividef(d2f(v[u][5]), kb * n);
+    }
   } else {
-    n = nsum[t];
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) return;
+    T[t] = __fdividef(d2f(pin[t]), kb * nsum[t]);
   }
-  T[t] = __fdividef(d2f(pin[t]), kb * n);
 }
 
 // block size of the pass that defers stiff cells (one list append per block)
@@ -297,11 +314,14 @@ __global__ void __launch_bounds__(128) source32_stiff_kernel(Source32Args A) {
 // dt for the chosen form: the Courant limit (:1912-1930) and the thermal
 // limit of Stblty (:2784-2822) in FP32; the per-cell minima are widened to
 // FP64 bit patterns for the same order-independent atomicMin reduction.
+// Grid-stride: each thread folds several cells into its minima, so the
+// block results that end in the two global atomicMin are ~50x fewer than
+// with a thread per cell (they all hit the same two words).
 __global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, unsigned long long *out, int *err) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   float c_min = d2f(ph.tfinal), s_min = c_min;
-  if (t < (long long)nx * ny * nz) {
+  const long long ncells = (long long)nx * ny * nz, stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ncells; t += stride) {
     int i, j, k;
     split3(t, nx, ny, i, j, k);
     i += 1; j += 1; k += 1;
