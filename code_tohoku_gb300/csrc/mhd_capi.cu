@@ -35,6 +35,7 @@ struct mhd_handle {
   // velocities, face B, rho, T switch and EMFs for CT) and FP32 widths
   float *fblock = nullptr;
   double *colblock = nullptr;     // SHIELD's ten column arrays (ifrad = 2)
+  double *ctcoef = nullptr;       // chosen form's CC(3): dt/dx of every coordinate
   double dxh = 0.0;               // SHIELD's half width 0.5 dx(1)
   float *temp32 = nullptr;
   float *nsum32 = nullptr;               // SOURCE's FP32 species sum (predictor -> corrector)
@@ -246,6 +247,11 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
       mhd_destroy(h);
       return MHD_ERR_CUDA;
     }
+    if (cudaMalloc(&h->ctcoef, (size_t)(g.s[0] + g.s[1] + g.s[2]) * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      mhd_destroy(h);
+      return MHD_ERR_CUDA;
+    }
     float *fq = h->fblock;
     h->temp32 = fq; fq += g.ncell;
     h->nsum32 = fq; fq += g.ncell;
@@ -283,6 +289,7 @@ int mhd_destroy(mhd_handle *h) {
   cudaFree(h->dtf);
   cudaFree(h->fblock);
   cudaFree(h->colblock);
+  cudaFree(h->ctcoef);
   cudaFree(h->divv);
   cudaFree(h->diag_part);
   cudaFree(h->dtred);
@@ -559,7 +566,8 @@ int ct_impl(mhd_handle *h, double dt, bool rho_filled) {
     a.dt = (float)dt; a.facm = (float)(h->ph.facdep * 0.5);
     CK(ct_prep_fp32(h->g, f, h->vf, h->ph.kb, a, h->stream));
     for (int e = 0; e < 3; e++) CK(emf32(e, a, h->stream));
-    CK(face_b_fp32(h->g, f, h->emf32, dt, h->stream));
+    CK(face_b_fp32(h->g, f, h->emf32, dt, h->ctcoef, h->stream));
+    h->launches++;   // the coefficient kernel
   } else {
     CTArgs a{};
     a.g = h->g; a.ph = h->ph; a.f = f; a.dt = dt;

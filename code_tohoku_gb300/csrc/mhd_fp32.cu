@@ -167,9 +167,14 @@ cudaError_t emf32(int e, const CT32Args &a, cudaStream_t s) {
   return emf32_e<2>(a, s);
 }
 
-cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], double dt, cudaStream_t s) {
+cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], double dt, double *coef,
+                        cudaStream_t s) {
+  const int nc = g.s[0] + g.s[1] + g.s[2];
+  ct_coef32_kernel<<<(nc + 255) / 256, 256, 0, s>>>(g, dt, coef);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
   long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
-  face_b32_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, f, emf[0], emf[1], emf[2], dt);
+  face_b32_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, f, emf[0], emf[1], emf[2], coef);
   return cudaGetLastError();
 }
 

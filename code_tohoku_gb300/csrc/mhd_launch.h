@@ -30,7 +30,9 @@ cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, doubl
 cudaError_t ct_prep_fp32(const Grid &g, const Fields &f, double *const vf[3], double kb, const CT32Args &a,
                          cudaStream_t s);
 cudaError_t emf32(int e, const CT32Args &a, cudaStream_t s);
-cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], double dt, cudaStream_t s);
+// CC(3) of the chosen form; coef: scratch of s[0]+s[1]+s[2] doubles for dt/dx
+cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], double dt, double *coef,
+                        cudaStream_t s);
 // pack FP32 master surrogate parameters into the BF16 device network
 cudaError_t surrogate_pack(const float *master, SurNet *net, cudaStream_t s);
 
