@@ -3,7 +3,7 @@
 // GPU.  The handle owns the resident state (U, species, Bcc) and the step's
 // scratch (face velocities, EMFs, the predictor pressure, DISSIP's divv);
 // every ghost exchange the reference performs between its subroutines is
-// issued here as a ghost_fill on the same fields and directions.
+// issued here as a ghost exchange (ghost_fill_all) on the same fields and directions.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -119,8 +119,7 @@ int fill_mask(mhd_handle *h, const double *const *arrays, int n, int dirs, int n
   for (int q = 0; q < nrules; q++) a.rule[q] = rules[q];
   a.spmask = spmask;
   a.in = h->ph.in;
-  for (int d = 0; d < 3; d++)
-    if (dirs & (1 << d)) CK(ghost_fill(h->g, a, d, nol, h->stream));
+  CK(ghost_fill_all(h->g, a, dirs, nol, h->stream));
   return MHD_OK;
 }
 

@@ -26,11 +26,22 @@ cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s) { return launch_emf
 
 static unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-cudaError_t ghost_fill(const Grid &g, const FillArgs &f, int d, int nol, cudaStream_t s) {
-  long long n = (long long)g.s[(d + 1) % 3] * g.s[(d + 2) % 3] * f.nf;
-  ghost_fill_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f, d, nol);
+cudaError_t ghost_fill_all(const Grid &g, const FillArgs &f, int dirs, int nol, cudaStream_t s) {
+  FillAll r{};
+  const bool mk[3] = {(dirs & 1) != 0, (dirs & 2) != 0, (dirs & 4) != 0};
+  for (int reg = 0; reg < 3; reg++) {
+    if (!mk[reg]) continue;
+    long long n = 1;
+    for (int d = 0; d < 3; d++)
+      n *= d < reg ? (g.s[d] - (mk[d] ? 2 * nol : 0)) : (d == reg ? 2 * nol : g.s[d]);
+    r.nreg[reg] = n;
+  }
+  const long long n = (r.nreg[0] + r.nreg[1] + r.nreg[2]) * f.nf;
+  if (n == 0) return cudaSuccess;
+  ghost_fill_all_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f, dirs, nol, r);
   return cudaGetLastError();
 }
+
 
 cudaError_t face_velocity(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s) {
   long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);

@@ -11,7 +11,7 @@
 // U(-1:ndx,-1:ndy,-1:ndz,k) column.  The whole grid is resident in HBM; the
 // reference's MPI halo exchanges become the ghost copies below (periodic
 // wrap or the free-boundary copy), done either in global memory
-// (ghost_fill_kernel) or inside the fused sweep kernel on its pencils.
+// (ghost_fill_all_kernel) or inside the fused sweep kernel on its pencils.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -345,44 +345,82 @@ struct FillArgs {
 };
 
 #ifdef MHD_COMMON_KERNELS
-__global__ void ghost_fill_kernel(Grid g, FillArgs a, int d, int nol) {
-  int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
-  long long nl = (long long)g.s[o1] * g.s[o2];
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nl * a.nf) return;
-  int q1, q2, fi;
-  split3(t, g.s[o1], g.s[o2], q1, q2, fi);
-  q1 -= 1; q2 -= 1;
+// One BC_MPI / BC_MPI_OT exchange of up to 8 arrays, all its directions in
+// one launch.  The exchange is a pass per direction x, y, z (those in
+// dirs), each over every line along its direction with all transverse
+// indices, ghosts included (like the MPI vector types): the periodic wrap,
+// then the free-boundary copy on a free side (species arrays: on lines with
+// interior transverse indices only, ...-feedback.f90:1057), or on an x side
+// with inflow (BC=4) the inflow value of the array's rule.  Those passes are
+// pure gathers except the inflow rule, so the value a ghost cell holds after
+// them is the pre-exchange value of one source cell, found here by walking
+// the passes backwards from the cell: at each pass whose ghost layers hold
+// the current coordinate, move it to where that pass copied from, with the
+// rule the pass applies to the current line (its transverse coordinates
+// decide the species restriction), or end at the inflow value it computes.
+// Sources are never written (every pass reads interior cells only, and a
+// cell the passes leave alone maps to itself and is skipped), so the launch
+// is free of races and equals the passes run one after another (checked
+// against them on the CPU for every direction set, 1 and 2 layers, species
+// and free / periodic sides).
+struct FillAll {
+  long long nreg[3];   // threads per array in the x, y and z shells
+};
+__device__ __forceinline__ int fill_layer(int f, int nol, int N) {   // f-th filled ghost index
+  return f < nol ? 1 - nol + f : N + 1 + (f - nol);
+}
+__device__ __forceinline__ int fill_other(int u, bool masked, int nol, int N) {   // u-th index outside them
+  if (!masked) return u - 1;
+  if (nol == 2) return u + 1;
+  return u == 0 ? -1 : (u <= N ? u : N + 2);
+}
+__global__ void ghost_fill_all_kernel(Grid g, FillArgs a, int dirs, int nol, FillAll r) {
+  const long long per = r.nreg[0] + r.nreg[1] + r.nreg[2];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= per * a.nf) return;
+  const int fi = (int)(t / per);
+  long long u = t - (long long)fi * per;
+  const bool mk[3] = {(dirs & 1) != 0, (dirs & 2) != 0, (dirs & 4) != 0};
+  const int N[3] = {g.n[0], g.n[1], g.n[2]};
   int c[3];
-  c[o1] = q1;
-  c[o2] = q2;
-  c[d] = -1;
-  long long base = gidx(g, c[0], c[1], c[2]);
-  long long sd = g.st[d];
+  // the shell: x ghosts; else y ghosts; else z ghosts (disjoint)
+  int reg = 0;
+  while (u >= r.nreg[reg]) u -= r.nreg[reg++];
+  {
+    int ext[3];
+    for (int d = 0; d < 3; d++) ext[d] = d < reg ? (g.s[d] - (mk[d] ? 2 * nol : 0)) : (d == reg ? 2 * nol : g.s[d]);
+    int e0, e1, e2;
+    split3(u, ext[0], ext[1], e0, e1, e2);
+    const int e[3] = {e0, e1, e2};
+    for (int d = 0; d < 3; d++)
+      c[d] = d == reg ? fill_layer(e[d], nol, N[d]) : (d < reg ? fill_other(e[d], mk[d], nol, N[d]) : e[d] - 1);
+  }
   double *F = a.f[fi];
   const bool species = (a.spmask >> fi) & 1u;
-  int N = g.n[d];
-  bool tr_in = q1 >= 1 && q1 <= g.n[o1] && q2 >= 1 && q2 <= g.n[o2];
-  bool fl = g.bcl[d] == 1 && (!species || tr_in);
-  bool fr = g.bcr[d] == 1 && (!species || tr_in);
-  // position i lives at base + (i+1)*sd
-  const bool inL = d == 0 && a.in.on[0], inR = d == 0 && a.in.on[1];
   const int rule = a.rule[fi];
-  if (!inL) {
-    for (int q = 1 - nol; q <= 0; q++) F[base + (q + 1) * sd] = F[base + (q + N + 1) * sd];
-    if (fl) for (int q = 1 - nol; q <= 0; q++) F[base + (q + 1) * sd] = F[base + 2 * sd];
-  } else if (rule != IN_KEEP && (!species || tr_in)) {
-    // BC=4: no neighbour on this side; the inflow value of the field
-    for (int q = 1 - nol; q <= 0; q++)
-      F[base + (q + 1) * sd] = inflow_value(g, a.in, rule, 0, q, q1, q2, 0.0, F[base + 2 * sd], F[base + (N + 1) * sd]);
+  int cur[3] = {c[0], c[1], c[2]};
+  for (int d = 2; d >= 0; d--) {
+    if (!mk[d]) continue;
+    const int q = cur[d];
+    const bool left = q <= 0 && q >= 1 - nol, right = q >= N[d] + 1 && q <= N[d] + nol;
+    if (!left && !right) continue;
+    const int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+    const bool tr_in = cur[o1] >= 1 && cur[o1] <= N[o1] && cur[o2] >= 1 && cur[o2] <= N[o2];
+    const bool infl = d == 0 && a.in.on[left ? 0 : 1];
+    if (infl) {
+      if (rule != IN_KEEP && (!species || tr_in)) {
+        // the inflow value (x is the first pass: it reads the pre-exchange state)
+        const double f1 = F[gidx(g, 1, cur[1], cur[2])], fN = F[gidx(g, N[0], cur[1], cur[2])];
+        F[gidx(g, c[0], c[1], c[2])] = inflow_value(g, a.in, rule, left ? 0 : 1, q, cur[1], cur[2], 0.0, f1, fN);
+        return;
+      }
+      continue;   // kept: this pass leaves the cell alone
+    }
+    const bool freeb = (left ? g.bcl[d] : g.bcr[d]) == 1 && (!species || tr_in);
+    cur[d] = freeb ? (left ? 1 : N[d]) : (left ? q + N[d] : q - N[d]);
   }
-  if (!inR) {
-    for (int q = N + 1; q <= N + nol; q++) F[base + (q + 1) * sd] = F[base + (q - N + 1) * sd];
-    if (fr) for (int q = N + 1; q <= N + nol; q++) F[base + (q + 1) * sd] = F[base + (N + 1) * sd];
-  } else if (rule != IN_KEEP && (!species || tr_in)) {
-    for (int q = N + 1; q <= N + nol; q++)
-      F[base + (q + 1) * sd] = inflow_value(g, a.in, rule, 1, q, q1, q2, 0.0, F[base + 2 * sd], F[base + (N + 1) * sd]);
-  }
+  if (cur[0] == c[0] && cur[1] == c[1] && cur[2] == c[2]) return;
+  F[gidx(g, c[0], c[1], c[2])] = F[gidx(g, cur[0], cur[1], cur[2])];
 }
 
 #endif  // MHD_COMMON_KERNELS

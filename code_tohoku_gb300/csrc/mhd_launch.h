@@ -37,7 +37,8 @@ cudaError_t face_b_fp32(const Grid &g, const Fields &f, float *const emf[3], dou
 cudaError_t surrogate_pack(const float *master, SurNet *net, cudaStream_t s);
 
 // precision-independent FP64 kernels (built in the FP64 unit)
-cudaError_t ghost_fill(const Grid &g, const FillArgs &f, int dir, int nol, cudaStream_t s);
+// one ghost exchange over every direction in dirs, one launch
+cudaError_t ghost_fill_all(const Grid &g, const FillArgs &f, int dirs, int nol, cudaStream_t s);
 cudaError_t face_velocity(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
 cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const double *ex, const double *ey, double dt,
                    cudaStream_t s);
