@@ -38,7 +38,7 @@ struct mhd_handle {
   double *ctcoef = nullptr;       // chosen form's CC(3): dt/dx of every coordinate
   double dxh = 0.0;               // SHIELD's half width 0.5 dx(1)
   float *temp32 = nullptr;
-  float *nsum32 = nullptr;               // SOURCE's FP32 species sum (predictor -> corrector)
+  float *sh2_32 = nullptr;               // SOURCE's FP32 S = H+p+He+He+ and H2 (2 ncell floats)
   int *stiff_list = nullptr;             // SOURCE's stiff cells (FP32 form with a surrogate)
   float *vf32[3] = {nullptr, nullptr, nullptr};
   float *bf32[3] = {nullptr, nullptr, nullptr};
@@ -239,7 +239,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     for (int q = 0; q < 10; q++) h->f.col[q] = h->colblock + (size_t)q * g.ncell;
   }
   if (p->precision == MHD_PREC_FP32) {
-    const size_t nf = 14;   // 13 FP32 arrays + the stiff-cell list of SOURCE
+    const size_t nf = 15;   // 14 FP32 arrays + the stiff-cell list of SOURCE
     size_t fbytes = nf * (size_t)g.ncell * sizeof(float);
     if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess) {
       cudaGetLastError();
@@ -253,7 +253,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     }
     float *fq = h->fblock;
     h->temp32 = fq; fq += g.ncell;
-    h->nsum32 = fq; fq += g.ncell;
+    h->sh2_32 = fq; fq += 2 * g.ncell;
     for (int c = 0; c < 3; c++) { h->vf32[c] = fq; fq += g.ncell; }
     for (int c = 0; c < 3; c++) { h->bf32[c] = fq; fq += g.ncell; }
     h->rn32 = fq; fq += g.ncell;
@@ -464,15 +464,16 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     a.tol = h->sur_tol;
     a.T = h->temp32;
     a.stiff_list = h->stiff_list; a.stiff_count = h->dtred + 5;
+    a.sh2 = h->sh2_32;
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
     // with a surrogate, source_fp32 launches a second (stiff-cell) kernel
     const int extra = (a.W && h->ph.ifchem != 2) ? 1 : 0;
-    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->nsum32, true, h->stream));
+    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, true, h->stream));
     CK(source_fp32(a, h->stream));
     h->launches += extra;
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
-    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->nsum32, false, h->stream));
+    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, false, h->stream));
     CK(source_fp32(a, h->stream));
     h->launches += extra;
     return MHD_OK;

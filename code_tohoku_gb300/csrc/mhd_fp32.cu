@@ -133,10 +133,10 @@ cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsig
 
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *nsum,
+cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *sh2,
                       bool from_species, cudaStream_t s) {
-  if (from_species) temp32_kernel<true><<<blocks_for(g.ncell, 512), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T, nsum);
-  else temp32_kernel<false><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T, nsum);
+  if (from_species) temp32_kernel<true><<<blocks_for(g.ncell, 512), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T, sh2);
+  else temp32_kernel<false><<<blocks_for(g.ncell, 256), 256, 0, s>>>(g.ncell, f, pin, d2f(kb), T, sh2);
   return cudaGetLastError();
 }
 

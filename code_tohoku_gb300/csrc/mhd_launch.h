@@ -21,8 +21,8 @@ cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s);
 cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s);
 cudaError_t source_fp32(const Source32Args &a, cudaStream_t s);
 // FP32 temperatures of every padded cell; from_species: from the species
-// (and store their sum in nsum), else from the sum stored by the last call
-cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *nsum,
+// (and store S = H+p+He+He+ and H2 in sh2, 2 ncell floats), else from them
+cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *sh2,
                       bool from_species, cudaStream_t s);
 cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
                            cudaStream_t s);
