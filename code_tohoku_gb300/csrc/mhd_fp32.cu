@@ -125,9 +125,9 @@ cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s) {
 cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
                            cudaStream_t s) {
   long long n = (long long)g.n[0] * g.n[1] * g.n[2];
-  // 4864 blocks of 256 threads (32 per SM): about 13 cells per thread at 256^3
-  const unsigned nb = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 8 * 4);
-  dt32_kernel<<<nb, 256, 0, s>>>(g, ph, f, out, err);
+  // a thread per cell: with a capped grid of 4864 blocks (~13 cells per
+  // thread, 50x fewer atomics) the 256^3 kernel took 385 us against 333-358
+  dt32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, out, err);
   return cudaGetLastError();
 }
 

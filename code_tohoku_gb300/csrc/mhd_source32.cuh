@@ -323,9 +323,7 @@ __global__ void __launch_bounds__(128) source32_stiff_kernel(Source32Args A) {
 // dt for the chosen form: the Courant limit (:1912-1930) and the thermal
 // limit of Stblty (:2784-2822) in FP32; the per-cell minima are widened to
 // FP64 bit patterns for the same order-independent atomicMin reduction.
-// Grid-stride: each thread folds several cells into its minima, so the
-// block results that end in the two global atomicMin are ~50x fewer than
-// with a thread per cell (they all hit the same two words).
+// Grid-stride loop over the cells (the launch uses a thread per cell).
 __global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, unsigned long long *out, int *err) {
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   float c_min = d2f(ph.tfinal), s_min = c_min;
