@@ -106,10 +106,9 @@ int fail(mhd_handle *h, int code, const char *fmt, ...) {
 
 const double kNdMinH = 0.91, kNdMinHe = 0.09;
 
-// ghost exchange of a list of arrays in the directions of mask (x,y,z order);
-// rules: the BC=4 rule of each array on an inflow side of x
 // BC_MPI-style exchange of up to 8 arrays along the directions in dirs (bit
-// d), nol ghost layers; spmask bit q: array q is a species array, whose
+// d), nol ghost layers; rules: the BC=4 rule of each array on an inflow side
+// of x (IN_KEEP past nrules); spmask bit q: array q is a species array, whose
 // free-boundary copy covers interior transverse lines only
 int fill_mask(mhd_handle *h, const double *const *arrays, int n, int dirs, int nol, unsigned spmask,
               const int *rules, int nrules) {
@@ -126,7 +125,7 @@ int fill_mask(mhd_handle *h, const double *const *arrays, int n, int dirs, int n
 int fill(mhd_handle *h, std::initializer_list<double *> arrays, int dirs, int nol, int species = 0,
          std::initializer_list<int> rules = {}) {
   const double *arr[8];
-  int n = 0, nr = 0, r[8];
+  int n = 0, nr = 0, r[8] = {IN_KEEP, IN_KEEP, IN_KEEP, IN_KEEP, IN_KEEP, IN_KEEP, IN_KEEP, IN_KEEP};
   for (double *p : arrays) arr[n++] = p;
   for (int x : rules) r[nr++] = x;
   return fill_mask(h, arr, n, dirs, nol, species ? (1u << n) - 1u : 0u, r, nr);
@@ -622,34 +621,14 @@ int mhd_step(mhd_handle *h, double tsave, double *dt, int *st) {
   return MHD_OK;
 }
 
-int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, double *U_out, double *species_out,
-                  double tsave, double *dt, int *st) {
-  if (!h || !U_in || !species_in || !U_out || !species_out || !dt || !st) return MHD_ERR_ARG;
-  if (!h->uploaded) return fail(h, MHD_ERR_STATE, "mhd_step_host needs a first mhd_upload (coordinates)");
-  CKR(cudaSetDevice(h->p.device));
-  TRY(need_inflow(h));
-  if (!h->io_stream) CKR(cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
-  for (int e = 0; e < 2; e++)
-    if (!h->ev_io[e]) CKR(cudaEventCreateWithFlags(&h->ev_io[e], cudaEventDisableTiming));
-  const Grid &g = h->g;
-  const size_t nc = (size_t)g.ncell, nb = nc * sizeof(double);
+namespace {
+// the EVOLVE iteration of mhd_advance for mhd_step_host, copying arrays
+// back as soon as they are final: without chemistry rho and the species are
+// final after the sweeps (once their ghosts are filled), the face field
+// after CC
+int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out) {
+  const size_t nc = (size_t)h->g.ncell, nb = nc * sizeof(double);
   Fields &f = h->f;
-  // the state in
-  for (int q = 0; q < 8; q++) CKR(cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
-  for (int q = 0; q < 8; q++)
-    CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
-  CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
-  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
-  // dt (mhd_step)
-  double d;
-  int s;
-  TRY(mhd_timestep(h, &d, &s));
-  if (h->time + d > h->p.tfinal) d = h->p.tfinal - h->time;
-  if (h->time + d > tsave) d = tsave - h->time;
-  if (!(d > 0.0)) return fail(h, MHD_ERR_DT, "dt <= 0 after clipping (time %.17g)", h->time);
-  // the EVOLVE iteration of mhd_advance, copying arrays back as soon as
-  // they are final: without chemistry rho and the species are final after
-  // the sweeps (once their ghosts are filled), the face field after CC
   static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
   TRY(mhd_source(h, 0.5 * d));
   for (int q = 0; q < 3; q++) TRY(mhd_sweep(h, orders[h->ifevo - 1][q], d));
@@ -681,7 +660,44 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   if (!early)
     for (int q = 0; q < 8; q++)
       CKR(cudaMemcpyAsync(species_out + q * nc, f.sp[q], nb, cudaMemcpyDeviceToHost, h->stream));
-  CKR(cudaStreamSynchronize(h->io_stream));
+  return MHD_OK;
+}
+}  // namespace
+
+int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, double *U_out, double *species_out,
+                  double tsave, double *dt, int *st) {
+  if (!h || !U_in || !species_in || !U_out || !species_out || !dt || !st) return MHD_ERR_ARG;
+  if (!h->uploaded) return fail(h, MHD_ERR_STATE, "mhd_step_host needs a first mhd_upload (coordinates)");
+  CKR(cudaSetDevice(h->p.device));
+  TRY(need_inflow(h));
+  if (!h->io_stream) CKR(cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
+  for (int e = 0; e < 2; e++)
+    if (!h->ev_io[e]) CKR(cudaEventCreateWithFlags(&h->ev_io[e], cudaEventDisableTiming));
+  const Grid &g = h->g;
+  const size_t nc = (size_t)g.ncell, nb = nc * sizeof(double);
+  Fields &f = h->f;
+  // the state in
+  for (int q = 0; q < 8; q++) CKR(cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
+  for (int q = 0; q < 8; q++)
+    CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
+  CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
+  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
+  // dt (mhd_step)
+  double d;
+  int s;
+  TRY(mhd_timestep(h, &d, &s));
+  if (h->time + d > h->p.tfinal) d = h->p.tfinal - h->time;
+  if (h->time + d > tsave) d = tsave - h->time;
+  if (!(d > 0.0)) return fail(h, MHD_ERR_DT, "dt <= 0 after clipping (time %.17g)", h->time);
+  // the copy-back stream may hold copies into the caller's buffers: every
+  // exit below waits for it, so the buffers are never written after return
+  const int r = step_host_body(h, d, U_out, species_out);
+  const cudaError_t es = cudaStreamSynchronize(h->io_stream);
+  if (r != MHD_OK) {
+    cudaStreamSynchronize(h->stream);   // its copies into U_out too
+    return r;
+  }
+  if (es != cudaSuccess) return fail(h, MHD_ERR_CUDA, "copy-back: %s", cudaGetErrorString(es));
   CKR(cudaStreamSynchronize(h->stream));
   *dt = d;
   *st = s;

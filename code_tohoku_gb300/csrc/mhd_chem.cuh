@@ -32,6 +32,9 @@ __device__ __forceinline__ float mpow(float x, float y) {
 // zero weight selects 0 explicitly instead of forming 0 * inf.
 __device__ __forceinline__ double wmul(double w, double y) { return w * y; }
 __device__ __forceinline__ float wmul(float w, float y) { return w == 0.0f ? 0.0f : w * y; }
+// the reference's 1e-100 guard: below FP32's range, so 0 in the float form
+__device__ __forceinline__ double guard100(double) { return 1.e-100; }
+__device__ __forceinline__ float guard100(float) { return 0.0f; }
 
 // the species of one cell (number densities), and its nde / ndtot
 // slots of the columns in CellSpecies::col and Fields::col
@@ -145,10 +148,10 @@ __device__ __forceinline__ ChemRates<R> chem_rates(R T, const CellSpecies<R> &c)
   const R e06 = R(0.6f);   // the literal 0.6 is REAL*4 in the reference (:3068)
   R ATN5 = (R(0.5) - fsgn(R(0.5), NCO1 - R(1.40995e-3))) * mexp(R(-1) * mpow(R(1.02857e3) * NCO1, e06)) +
            wmul(R(0.5) + fsgn(R(0.5), NCO1 - R(1.40995e-3)),
-                fmn(mpow(R(3.75439e3) * NCO1 + R(1.e-100), R(-0.75)), mpow(R(7.3469e1) * NCO1 + R(1.e-100), R(-1.3))));
+                fmn(mpow(R(3.75439e3) * NCO1 + guard100(R(0)), R(-0.75)), mpow(R(7.3469e1) * NCO1 + guard100(R(0)), R(-1.3))));
   ATN5 = ATN5 + (R(0.5) - fsgn(R(0.5), NCO2 - R(1.40995e-3))) * mexp(R(-1) * mpow(R(1.02857e3) * NCO2, e06)) +
          wmul(R(0.5) + fsgn(R(0.5), NCO2 - R(1.40995e-3)),
-              fmn(mpow(R(3.75439e3) * NCO2 + R(1.e-100), R(-0.75)), mpow(R(7.3469e1) * NCO2 + R(1.e-100), R(-1.3))));
+              fmn(mpow(R(3.75439e3) * NCO2 + guard100(R(0)), R(-0.75)), mpow(R(7.3469e1) * NCO2 + guard100(R(0)), R(-1.3))));
   ATN5 = ATN5 * R(0.5);
   r.zeta = R(9.4671e-4);
   R kh = (R(0.5) + fsgn(R(0.5), R(15.78) - T)) * R(0.45) * mlog(R(1.578e2) / T) +

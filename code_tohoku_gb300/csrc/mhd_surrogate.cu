@@ -358,7 +358,7 @@ int mhd_surrogate_label(const float *x, float *y, long long n, double kb, int de
   SCK(cudaMalloc(&dx.p, n * 3 * sizeof(float)));
   SCK(cudaMalloc(&dy.p, n * sizeof(float)));
   SCK(cudaMemcpy(dx.p, x, n * 3 * sizeof(float), cudaMemcpyHostToDevice));
-  sur_label_kernel<<<nb(n, 128), 128>>>(dx.as<float>(), dy.as<float>(), n, 8.63359);
+  sur_label_kernel<<<nb(n, 128), 128>>>(dx.as<float>(), dy.as<float>(), n, kb);
   SCK(cudaGetLastError());
   SCK(cudaMemcpy(y, dy.p, n * sizeof(float), cudaMemcpyDeviceToHost));
   return MHD_OK;

@@ -31,10 +31,11 @@ def trained():
     return p, hist
 
 
-def test_labels_bit_exact_vs_oracle():
+@pytest.mark.parametrize("kb", [8.63359, 6.0])
+def test_labels_bit_exact_vs_oracle(kb):
     x = sample(3000, 1)
-    gpu = native.surrogate_label(x)
-    cpu = pyoracle.ki_labels(x).astype(np.float32)
+    gpu = native.surrogate_label(x, kb=kb)
+    cpu = pyoracle.ki_labels(x, kb=kb).astype(np.float32)
     assert np.array_equal(gpu, cpu)
 
 
