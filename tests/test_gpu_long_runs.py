@@ -4,7 +4,6 @@ interior value identical after 100 steps of the decaying turbulence and of
 the KI colliding flows, and after 50 steps of the shipped deck's setup
 (inflow boundaries, chemistry network and species cooling), at sizes the
 oracle runs in seconds."""
-import numpy as np
 import pytest
 
 from code_tohoku_gb300 import native, problems
