@@ -44,7 +44,7 @@ enum {
   F_P,       // p -> Bnap (MOC) -> flux m2 -> species flux 3 / 7
   F_B1,      // Bcc_t1 -> Blg1 -> q_B1 -> B1,new
   F_B2,      // Bcc_t2 -> Blg2 -> q_B2 -> B2,new
-  F_BN,      // face-normal B
+  F_BN,      // face-normal B -> cell-centred normal B (from the MOC update on)
   F_DXL,     // Lagrangian width
   F_VA,      // Va at interface i+1/2
   F_PA,      // Pa -> Bay -> flux E -> species q 7
@@ -58,7 +58,7 @@ enum {
   F_G4,      // slope; then flux m1 -> species flux 2 / 6
   F_T,       // T-switch variable (p ghosts, e inside) -> q_E -> E_new
   F_IMN,     // momentum increment along the sweep -> species q 2 / 6
-  F_SW,      // remap T switch (+-0.5) of cells 0..n+1
+  F_SW,      // cell-centred normal B -> remap T switch (+-0.5) of cells 0..n+1
   F_COUNT
 };
 enum { C_DX = 0, C_RDX, C_X2, C_COUNT };
@@ -217,9 +217,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
       Fb(b, 0, p) = v;
     }
   };
-  auto put = [&](int b, int i, int p, float v, int rule) {
-    Fb(b, i, p) = v;
-    put_ghosts(b, i, p, v, rule);
+  // Only cells 1, 2, n-1 and n feed ghosts.  A phase stores its interior
+  // values first and copies them into the ghosts in one block for those
+  // cells (copy_ghosts: the ghosts of buffer b take its entry i), so the
+  // other items skip the ghost tests with one branch.
+  auto edge = [&](int i) { return i <= 2 || i >= N - 1; };
+  auto copy_ghosts = [&](int b, int i, int p) {
+    const float v = Fb(b, i, p);
+    for_ghosts(i, [&](int gi) { Fb(b, gi, p) = v; });
   };
   // the inflow ghosts of listed buffers (values that depend on no interior
   // cell); run by the phase that writes those buffers, before its barrier
@@ -235,12 +240,31 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     return vlim_sel(Fb(b, i - 1, p), Fb(b, i, p), Fb(b, i + 1, p), dm, d0, dp, s);
   };
   auto tsw = [&](float e5, float rho) { return (1.27f * e5 >= 3.0f * kb * rho) ? 0.5f : -0.5f; };
-  // upwind MUSCL flux of reconstruction buffer qb through interface i
-  auto flux = [&](int qb, int i, int p, float vadt) {
-    const int c = (vadt <= 0.0f) ? i + 1 : i;
-    float gs = vl(qb, c, p, Fb(F_DXL, c - 1, p), Fb(F_DXL, c, p), Fb(F_DXL, c + 1, p), Fb(F_SW, c, p));
-    if (vadt <= 0.0f) return -vadt * (Fb(qb, c, p) - (0.5f * (Fb(F_DXL, c, p) + vadt) * facdep) * gs);
-    return -vadt * (Fb(qb, c, p) + (0.5f * (Fb(F_DXL, c, p) - vadt) * facdep) * gs);
+  // Upwind MUSCL fluxes through interface i: the upwind cell c, its
+  // Lagrangian widths and switch are read once per interface (upwind) and
+  // shared by the fields (flux), whose values a phase stores only after all
+  // are formed, so no store separates the shared loads from their uses.
+  struct Upwind {
+    int c;
+    bool left;   // vadt <= 0: the upwind cell is i+1
+    float vadt, dm, d0, dp, s, w;
+  };
+  auto upwind = [&](int i, int p, float vadt) {
+    Upwind u;
+    u.vadt = vadt;
+    u.left = vadt <= 0.0f;
+    u.c = u.left ? i + 1 : i;
+    u.dm = Fb(F_DXL, u.c - 1, p);
+    u.d0 = Fb(F_DXL, u.c, p);
+    u.dp = Fb(F_DXL, u.c + 1, p);
+    u.s = Fb(F_SW, u.c, p);
+    u.w = u.left ? (0.5f * (u.d0 + vadt) * facdep) : (0.5f * (u.d0 - vadt) * facdep);
+    return u;
+  };
+  auto flux = [&](int qb, const Upwind &u, int p) {
+    const float gs = vl(qb, u.c, p, u.dm, u.d0, u.dp, u.s);
+    const float q = Fb(qb, u.c, p);
+    return u.left ? -u.vadt * (q - u.w * gs) : -u.vadt * (q + u.w * gs);
   };
 
   // ------------------------------------------------ A: load (+ ghosts)
@@ -252,21 +276,36 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   }
   // the interior state of position i: flow variables ...
   auto load_flow = [&](int i, int p, double u0, double un, double u1, double u2, double u4) {
-    put(F_R, i, p, d2f(u0), IN_RHO);
-    put(F_VN, i, p, d2f(un), IN_V1);
-    put(F_VT1, i, p, d2f(u1), IN_V2);
-    put(F_VT2, i, p, d2f(u2), IN_V3);
-    const float pr = d2f(u4);
-    put(F_P, i, p, pr, IN_P);
-    put_ghosts(F_T, i, p, pr, IN_P);
+    Fb(F_R, i, p) = d2f(u0);
+    Fb(F_VN, i, p) = d2f(un);
+    Fb(F_VT1, i, p) = d2f(u1);
+    Fb(F_VT2, i, p) = d2f(u2);
+    Fb(F_P, i, p) = d2f(u4);
   };
-  // ... and species sums and the face-normal field (the face-field exchange
-  // rewrites the ghost faces, incl. face n+1; an inflow side copies face 1
-  // into faces -1, 0 and face n+1 into n+2)
-  auto load_species_face = [&](int i, int p, double s0, double s1, double s2, double s3, double s4, double bn) {
-    put(F_S, i, p, d2f(s0) + d2f(s1) + d2f(s3) + d2f(s4), IN_SSUM);
-    put(F_H2, i, p, d2f(s2), IN_SPEC + 2);
-    put(F_BN, i, p, d2f(bn), IN_BXF);
+  // ... species sums, the face-normal field and the cell-centred normal
+  // field (held in F_SW until the MOC update moves it to F_BN, for the
+  // Lagrangian step and the pressure at the end) ...
+  auto load_species_face = [&](int i, int p, double s0, double s1, double s2, double s3, double s4, double bn,
+                               double bnc) {
+    Fb(F_S, i, p) = d2f(s0) + d2f(s1) + d2f(s3) + d2f(s4);
+    Fb(F_H2, i, p) = d2f(s2);
+    Fb(F_BN, i, p) = d2f(bn);
+    Fb(F_SW, i, p) = d2f(bnc);
+  };
+  // ... and the ghosts they feed (the face-field exchange rewrites the ghost
+  // faces, incl. face n+1; an inflow side copies face 1 into faces -1, 0
+  // and face n+1 into n+2)
+  auto load_ghosts = [&](int i, int p, double bn) {
+    copy_ghosts(F_R, i, p);
+    copy_ghosts(F_VN, i, p);
+    copy_ghosts(F_VT1, i, p);
+    copy_ghosts(F_VT2, i, p);
+    copy_ghosts(F_P, i, p);
+    const float pr = Fb(F_P, i, p);
+    for_ghosts(i, [&](int gi) { Fb(F_T, gi, p) = pr; });
+    copy_ghosts(F_S, i, p);
+    copy_ghosts(F_H2, i, p);
+    put_ghosts(F_BN, i, p, Fb(F_BN, i, p), IN_BXF);
     if (pc.active(p)) for_ghosts(i, [&](int gi) { A.f.U[5 + DIR][pc.at(p, gi)] = bn; });
     if (inL && i == 1)
       for (int gi = -1; gi <= 0; gi++) A.f.U[5 + DIR][pc.at(p, gi)] = bn;
@@ -288,18 +327,20 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
       const double c1 = __ldg(A.f.bcc[C1] + a), c2 = __ldg(A.f.bcc[C2] + a);
       const bool inside = i >= 1 && i <= N;
       double u0 = 0.0, un = 0.0, u1 = 0.0, u2 = 0.0, u4 = 0.0;
-      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0, bn = 0.0;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, s4 = 0.0, bn = 0.0, bnc = 0.0;
       if (inside) {
         u0 = __ldg(A.f.U[0] + a); un = __ldg(A.f.U[1 + DIR] + a); u1 = __ldg(A.f.U[1 + C1] + a);
         u2 = __ldg(A.f.U[1 + C2] + a); u4 = __ldg(A.f.U[4] + a);
         s0 = __ldg(A.f.sp[0] + a); s1 = __ldg(A.f.sp[1] + a); s2 = __ldg(A.f.sp[2] + a);
         s3 = __ldg(A.f.sp[3] + a); s4 = __ldg(A.f.sp[4] + a); bn = __ldg(A.f.U[5 + DIR] + a);
+        bnc = __ldg(A.f.bcc[DIR] + a);
       }
       Fb(F_B1, i, p) = d2f(c1);
       Fb(F_B2, i, p) = d2f(c2);
       if (!inside) return;
       load_flow(i, p, u0, un, u1, u2, u4);
-      load_species_face(i, p, s0, s1, s2, s3, s4, bn);
+      load_species_face(i, p, s0, s1, s2, s3, s4, bn, bnc);
+      if (edge(i)) load_ghosts(i, p, bn);
     });
   } else {
     // three passes: transverse field (-1..n+2), flow state, species + face field
@@ -320,8 +361,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
       const int i = 1 + t / P, p = t % P;
       const long long a = pc.at(p, i);
       const double s0 = __ldg(A.f.sp[0] + a), s1 = __ldg(A.f.sp[1] + a), s2 = __ldg(A.f.sp[2] + a),
-                   s3 = __ldg(A.f.sp[3] + a), s4 = __ldg(A.f.sp[4] + a), bn = __ldg(A.f.U[5 + DIR] + a);
-      load_species_face(i, p, s0, s1, s2, s3, s4, bn);
+                   s3 = __ldg(A.f.sp[3] + a), s4 = __ldg(A.f.sp[4] + a), bn = __ldg(A.f.U[5 + DIR] + a),
+                   bnc = __ldg(A.f.bcc[DIR] + a);
+      load_species_face(i, p, s0, s1, s2, s3, s4, bn, bnc);
+      if (edge(i)) load_ghosts(i, p, bn);
     });
   }
   if (inL || inR) {
@@ -371,9 +414,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   });
   __syncthreads();
   // ------------------------------------------------ D: Lagrangian step
-  unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
+  unrolled<NT, kSmemUnroll>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
-    long long a = pc.at(p, i);
     float dx0 = cx(C_DX, i);
     float Va1 = Fb(F_VA, i, p), Va0 = Fb(F_VA, i - 1, p), Pa1 = Fb(F_PA, i, p), Pa0 = Fb(F_PA, i - 1, p);
     float dxl = (dx0 + Va1 * dt) - Va0 * dt;
@@ -382,17 +424,23 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     float S = Fb(F_S, i, p), H2 = Fb(F_H2, i, p);
     float g1 = fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
     float vn = Fb(F_VN, i, p), v1 = Fb(F_VT1, i, p), v2 = Fb(F_VT2, i, p);
-    float bn = d2f(__ldg(A.f.bcc[DIR] + a)), b1 = Fb(F_B1, i, p), b2 = Fb(F_B2, i, p);
+    float bn = Fb(F_SW, i, p), b1 = Fb(F_B1, i, p), b2 = Fb(F_B2, i, p);
     float e = fdiv(Fb(F_P, i, p), rho * g1) + 0.5f * (vn * vn + v1 * v1 + v2 * v2) +
               fdiv(0.5f * (bn * bn + b1 * b1 + b2 * b2), rho);
     float EL = e * dm - dt * (Pa1 * Va1 - Pa0 * Va0);
     Fb(F_IMN, i, p) = -dt * (Pa1 - Pa0);
     float inv = fdiv(1.0f, dxl);
     Fb(F_T, i, p) = fdiv(EL, dm);   // e after RHS: MOC's T switch inside
-    put(F_DXL, i, p, dxl, IN_DXLAG);
-    put(F_R, i, p, dm * inv, IN_RHO);
-    put(F_B1, i, p, b1 * dx0 * inv, IN_B2);
-    put(F_B2, i, p, b2 * dx0 * inv, IN_B3);
+    Fb(F_DXL, i, p) = dxl;
+    Fb(F_R, i, p) = dm * inv;
+    Fb(F_B1, i, p) = b1 * dx0 * inv;
+    Fb(F_B2, i, p) = b2 * dx0 * inv;
+    if (edge(i)) {
+      copy_ghosts(F_DXL, i, p);
+      copy_ghosts(F_R, i, p);
+      copy_ghosts(F_B1, i, p);
+      copy_ghosts(F_B2, i, p);
+    }
   });
   if (inL || inR) {
     const int bl[4] = {F_DXL, F_R, F_B1, F_B2};
@@ -464,13 +512,23 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     float EL = Fb(F_T, i, p) * dm + dt * ((0.5f * Bnap * Vnap + Bay1 * Vay1 + Baz1 * Vaz1) * Bnap -
                                           (0.5f * Bnam * Vnam + Bay0 * Vay0 + Baz0 * Vaz0) * Bnam);
     const float qE = EL * inv;
-    put(F_T, i, p, qE, IN_E);
-    put(F_SW, i, p, tsw(qE, rl), IN_SW);   // the remap's T switch, from E and rho
-    put(F_B1, i, p, Fb(F_B1, i, p) + dt * (Bnap * Vay1 - Bnam * Vay0) * inv, IN_B2);
-    put(F_B2, i, p, Fb(F_B2, i, p) + dt * (Bnap * Vaz1 - Bnam * Vaz0) * inv, IN_B3);
-    put(F_VN, i, p, Fb(F_VN, i, p) * rl + imn * inv, IN_M1);
-    put(F_VT1, i, p, Fb(F_VT1, i, p) * rl + im1 * inv, IN_M2);
-    put(F_VT2, i, p, Fb(F_VT2, i, p) * rl + im2 * inv, IN_M3);
+    Fb(F_BN, i, p) = Fb(F_SW, i, p);   // cell-centred normal field, kept for the pressure
+    Fb(F_T, i, p) = qE;
+    Fb(F_SW, i, p) = tsw(qE, rl);   // the remap's T switch, from E and rho
+    Fb(F_B1, i, p) = Fb(F_B1, i, p) + dt * (Bnap * Vay1 - Bnam * Vay0) * inv;
+    Fb(F_B2, i, p) = Fb(F_B2, i, p) + dt * (Bnap * Vaz1 - Bnam * Vaz0) * inv;
+    Fb(F_VN, i, p) = Fb(F_VN, i, p) * rl + imn * inv;
+    Fb(F_VT1, i, p) = Fb(F_VT1, i, p) * rl + im1 * inv;
+    Fb(F_VT2, i, p) = Fb(F_VT2, i, p) * rl + im2 * inv;
+    if (edge(i)) {
+      copy_ghosts(F_T, i, p);
+      copy_ghosts(F_SW, i, p);
+      copy_ghosts(F_B1, i, p);
+      copy_ghosts(F_B2, i, p);
+      copy_ghosts(F_VN, i, p);
+      copy_ghosts(F_VT1, i, p);
+      copy_ghosts(F_VT2, i, p);
+    }
   });
   if (inL || inR) {
     const int bl[7] = {F_T, F_SW, F_B1, F_B2, F_VN, F_VT1, F_VT2};
@@ -481,14 +539,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   // ------------------------------------------------ H: field fluxes
   unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
-    float vadt = Fb(F_VA, i, p) * dt;
-    Fb(F_G2, i, p) = flux(F_R, i, p, vadt);
-    Fb(F_G3, i, p) = flux(F_VN, i, p, vadt);
-    Fb(F_G4, i, p) = flux(F_VT1, i, p, vadt);
-    Fb(F_P, i, p) = flux(F_VT2, i, p, vadt);
-    Fb(F_PA, i, p) = flux(F_T, i, p, vadt);
-    Fb(F_GAM, i, p) = flux(F_B1, i, p, vadt);
-    Fb(F_S, i, p) = flux(F_B2, i, p, vadt);
+    const Upwind u = upwind(i, p, Fb(F_VA, i, p) * dt);
+    const float fr = flux(F_R, u, p), fn = flux(F_VN, u, p), f1 = flux(F_VT1, u, p), f2 = flux(F_VT2, u, p),
+                fe = flux(F_T, u, p), fb1 = flux(F_B1, u, p), fb2 = flux(F_B2, u, p);
+    Fb(F_G2, i, p) = fr;
+    Fb(F_G3, i, p) = fn;
+    Fb(F_G4, i, p) = f1;
+    Fb(F_P, i, p) = f2;
+    Fb(F_PA, i, p) = fe;
+    Fb(F_GAM, i, p) = fb1;
+    Fb(F_S, i, p) = fb2;
   });
   __syncthreads();
   // ------------------------- I: field finish, species 0-3 reconstruction
@@ -543,10 +603,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     if (act && (!(vn == vn) || !(v1 == v1) || !(v2 == v2) || !(rf < 3e38f))) flag(A.err, ERRB_NONFINITE);
     // species 0..3: content n dx is unchanged by the Lagrangian step
     const float w = cx(C_DX, i) * fdiv(1.0f, dxl);
-    put(F_G0, i, p, d2f(get(4)) * w, IN_SPEC + 0);
-    put(F_G1, i, p, d2f(get(5)) * w, IN_SPEC + 1);
-    put(F_IMN, i, p, d2f(get(6)) * w, IN_SPEC + 2);
-    put(F_H2, i, p, d2f(get(7)) * w, IN_SPEC + 3);
+    Fb(F_G0, i, p) = d2f(get(4)) * w;
+    Fb(F_G1, i, p) = d2f(get(5)) * w;
+    Fb(F_IMN, i, p) = d2f(get(6)) * w;
+    Fb(F_H2, i, p) = d2f(get(7)) * w;
+    if (edge(i)) {
+      copy_ghosts(F_G0, i, p);
+      copy_ghosts(F_G1, i, p);
+      copy_ghosts(F_IMN, i, p);
+      copy_ghosts(F_H2, i, p);
+    }
   });
   if (inL || inR) {
     const int bl[4] = {F_G0, F_G1, F_IMN, F_H2};
@@ -557,11 +623,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   // ------------------------------------------------ J: species 0-3 fluxes
   unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
-    float vadt = Fb(F_VA, i, p) * dt;
-    Fb(F_G2, i, p) = flux(F_G0, i, p, vadt);
-    Fb(F_G3, i, p) = flux(F_G1, i, p, vadt);
-    Fb(F_G4, i, p) = flux(F_IMN, i, p, vadt);
-    Fb(F_P, i, p) = flux(F_H2, i, p, vadt);
+    const Upwind u = upwind(i, p, Fb(F_VA, i, p) * dt);
+    const float f0 = flux(F_G0, u, p), f1 = flux(F_G1, u, p), f2 = flux(F_IMN, u, p), f3 = flux(F_H2, u, p);
+    Fb(F_G2, i, p) = f0;
+    Fb(F_G3, i, p) = f1;
+    Fb(F_G4, i, p) = f2;
+    Fb(F_P, i, p) = f3;
   });
   __syncthreads();
   // ------------------------- K: species 0-3 finish, 4-7 reconstruction
@@ -591,11 +658,17 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     float H2 = species_new(2, get(2), a, i, p, F_G4, act);
     Fb(F_S, i, p) = S;
     const float w = cx(C_DX, i) * fdiv(1.0f, Fb(F_DXL, i, p));
-    put(F_G0, i, p, d2f(get(4)) * w, IN_SPEC + 4);
-    put(F_G1, i, p, d2f(get(5)) * w, IN_SPEC + 5);
-    put(F_IMN, i, p, d2f(get(6)) * w, IN_SPEC + 6);
-    put(F_PA, i, p, d2f(get(7)) * w, IN_SPEC + 7);
+    Fb(F_G0, i, p) = d2f(get(4)) * w;
+    Fb(F_G1, i, p) = d2f(get(5)) * w;
+    Fb(F_IMN, i, p) = d2f(get(6)) * w;
+    Fb(F_PA, i, p) = d2f(get(7)) * w;
     Fb(F_H2, i, p) = H2;
+    if (edge(i)) {
+      copy_ghosts(F_G0, i, p);
+      copy_ghosts(F_G1, i, p);
+      copy_ghosts(F_IMN, i, p);
+      copy_ghosts(F_PA, i, p);
+    }
   });
   if (inL || inR) {
     const int bl[4] = {F_G0, F_G1, F_IMN, F_PA};
@@ -606,11 +679,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   // ------------------------------------------------ L: species 4-7 fluxes
   unrolled<NT, kSmemUnroll>((N + 1) * P, [&](int t) {
     int i = t / P, p = t % P;
-    float vadt = Fb(F_VA, i, p) * dt;
-    Fb(F_G2, i, p) = flux(F_G0, i, p, vadt);
-    Fb(F_G3, i, p) = flux(F_G1, i, p, vadt);
-    Fb(F_G4, i, p) = flux(F_IMN, i, p, vadt);
-    Fb(F_P, i, p) = flux(F_PA, i, p, vadt);
+    const Upwind u = upwind(i, p, Fb(F_VA, i, p) * dt);
+    const float f0 = flux(F_G0, u, p), f1 = flux(F_G1, u, p), f2 = flux(F_IMN, u, p), f3 = flux(F_PA, u, p);
+    Fb(F_G2, i, p) = f0;
+    Fb(F_G3, i, p) = f1;
+    Fb(F_G4, i, p) = f2;
+    Fb(F_P, i, p) = f3;
   });
   __syncthreads();
   // ---------------------------- M: species 4-7 finish, pressure + floors
@@ -619,11 +693,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     int i = 1 + t / P, p = t % P;
     const bool act = pc.active(p);
     long long a = pc.at(p, i);
-    const double *src[5] = {A.f.sp[4], A.f.sp[5], A.f.sp[6], A.f.sp[7], A.f.bcc[DIR]};
-    double pre[5];
+    const double *src[4] = {A.f.sp[4], A.f.sp[5], A.f.sp[6], A.f.sp[7]};
+    double pre[4];
     if constexpr (((kHoistLoads >> DIR) & 1) != 0) {
 #pragma unroll
-      for (int q = 0; q < 5; q++) pre[q] = __ldg(src[q] + a);
+      for (int q = 0; q < 4; q++) pre[q] = __ldg(src[q] + a);
     }
     auto get = [&](int q) -> double {
       if constexpr (((kHoistLoads >> DIR) & 1) != 0) return pre[q];
@@ -637,7 +711,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     float g1 = fdiv(2.0f * S + 2.0f * H2, 3.0f * S + 5.0f * H2);
     float rf = Fb(F_R, i, p), vn = Fb(F_VN, i, p), v1 = Fb(F_VT1, i, p), v2 = Fb(F_VT2, i, p);
     float ekin = 0.5f * (vn * vn + v1 * v1 + v2 * v2) * rf;
-    float bn = d2f(get(4)), l1 = Fb(F_B1, i, p), l2 = Fb(F_B2, i, p);
+    float bn = Fb(F_BN, i, p), l1 = Fb(F_B1, i, p), l2 = Fb(F_B2, i, p);
     float emag = 0.5f * (bn * bn + l1 * l1 + l2 * l2);
     float pr = (Fb(F_T, i, p) - ekin - emag) * g1;
     pr = fminf(pmax, fmaxf(pmin, pr));
