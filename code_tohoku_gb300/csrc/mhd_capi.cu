@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/mhd_gb300.h"
+#include "mhd_conv.cuh"
 #include "mhd_launch.h"
 
 using namespace mhd;
@@ -189,7 +190,10 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   ph.ifrad = p->ifrad;
   // species floors, MCF3DSGincfca3.f90:178-179 (slots H,p,H2,He,Hep,C,Cp,CO)
   double mins[8] = {p->rmin * kNdMinH, 1e-20, 1e-20, p->rmin * kNdMinHe, 1e-20, 1e-20, 1e-20, 1e-20};
-  for (int s = 0; s < 8; s++) ph.ndmin[s] = mins[s];
+  for (int s = 0; s < 8; s++) {
+    ph.ndmin[s] = mins[s];
+    ph.ndminf[s] = d2f(mins[s]);
+  }
   ph.in.on[0] = p->bc[0] == 4;
   ph.in.on[1] = p->bc[1] == 4;
 

@@ -61,6 +61,7 @@ struct Phys {
   int ifchem;              // 2: species cooling + chemistry network; 0: KI cooling
   int ifrad;               // 2: SHIELD column densities; 0: columns stay 0
   double ndmin[8];
+  float ndminf[8];         // the floors rounded to FP32 (chosen form)
   InflowDev in;
 };
 
