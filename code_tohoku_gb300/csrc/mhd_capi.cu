@@ -66,7 +66,7 @@ struct mhd_handle {
   // mhd_step_host: copy-back stream and the events it waits on (created on
   // first use)
   cudaStream_t io_stream = nullptr;
-  cudaEvent_t ev_io[2] = {nullptr, nullptr};
+  cudaEvent_t ev_io[3] = {nullptr, nullptr, nullptr};
   std::vector<double> rdx_host, rdxc_host;   // staging for the async coordinate copies
   std::vector<float> dxf_host;
   std::string msg;
@@ -303,7 +303,7 @@ int mhd_destroy(mhd_handle *h) {
     cudaStreamSynchronize(h->io_stream);
     cudaStreamDestroy(h->io_stream);
   }
-  for (int e = 0; e < 2; e++)
+  for (int e = 0; e < 3; e++)
     if (h->ev_io[e]) cudaEventDestroy(h->ev_io[e]);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -630,11 +630,14 @@ namespace {
 // back as soon as they are final: without chemistry rho and the species are
 // final after the sweeps (once their ghosts are filled), the face field
 // after CC
-int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out) {
+// late_species: species 5-7 are still coming in on the copy stream (event
+// ev_io[2]); the first sweep, their first reader, waits for them
+int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, bool late_species) {
   const size_t nc = (size_t)h->g.ncell, nb = nc * sizeof(double);
   Fields &f = h->f;
   static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
   TRY(mhd_source(h, 0.5 * d));
+  if (late_species) CKR(cudaStreamWaitEvent(h->stream, h->ev_io[2], 0));
   for (int q = 0; q < 3; q++) TRY(mhd_sweep(h, orders[h->ifevo - 1][q], d));
   h->ifevo = h->ifevo % 6 + 1;
   const bool early = h->p.ifchem != 2;
@@ -668,6 +671,26 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out) 
 }
 }  // namespace
 
+namespace {
+// mhd_step_host after the copies in: CC(4), the time step (mhd_step's
+// clipping), then the step with its copies back
+int step_host_run(mhd_handle *h, double tsave, double *dt, int *st, double *U_out, double *species_out,
+                  bool late_species) {
+  Fields &f = h->f;
+  CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
+  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
+  double d;
+  int s;
+  TRY(mhd_timestep(h, &d, &s));
+  if (h->time + d > h->p.tfinal) d = h->p.tfinal - h->time;
+  if (h->time + d > tsave) d = tsave - h->time;
+  if (!(d > 0.0)) return fail(h, MHD_ERR_DT, "dt <= 0 after clipping (time %.17g)", h->time);
+  *dt = d;
+  *st = s;
+  return step_host_body(h, d, U_out, species_out, late_species);
+}
+}  // namespace
+
 int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, double *U_out, double *species_out,
                   double tsave, double *dt, int *st) {
   if (!h || !U_in || !species_in || !U_out || !species_out || !dt || !st) return MHD_ERR_ARG;
@@ -675,27 +698,32 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   CKR(cudaSetDevice(h->p.device));
   TRY(need_inflow(h));
   if (!h->io_stream) CKR(cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
-  for (int e = 0; e < 2; e++)
+  for (int e = 0; e < 3; e++)
     if (!h->ev_io[e]) CKR(cudaEventCreateWithFlags(&h->ev_io[e], cudaEventDisableTiming));
   const Grid &g = h->g;
   const size_t nc = (size_t)g.ncell, nb = nc * sizeof(double);
   Fields &f = h->f;
-  // the state in
+  // The state in.  Without chemistry or SHIELD neither the time step nor
+  // the first SOURCE reads species 5-7 (C, C+, CO), so those three arrays
+  // come in on the copy stream, after the other copies, while those kernels
+  // run; the first sweep waits for them.
+  const bool late = h->p.ifchem != 2 && h->p.ifrad != 2;
   for (int q = 0; q < 8; q++) CKR(cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
-  for (int q = 0; q < 8; q++)
+  for (int q = 0; q < (late ? 5 : 8); q++)
     CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
-  CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
-  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
-  // dt (mhd_step)
-  double d;
-  int s;
-  TRY(mhd_timestep(h, &d, &s));
-  if (h->time + d > h->p.tfinal) d = h->p.tfinal - h->time;
-  if (h->time + d > tsave) d = tsave - h->time;
-  if (!(d > 0.0)) return fail(h, MHD_ERR_DT, "dt <= 0 after clipping (time %.17g)", h->time);
-  // the copy-back stream may hold copies into the caller's buffers: every
-  // exit below waits for it, so the buffers are never written after return
-  const int r = step_host_body(h, d, U_out, species_out);
+  if (late) {
+    CKR(cudaEventRecord(h->ev_io[2], h->stream));   // after everything queued before (readers included)
+    CKR(cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0));
+    for (int q = 5; q < 8; q++)
+      CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->io_stream));
+    CKR(cudaEventRecord(h->ev_io[2], h->io_stream));
+  }
+  // the copy stream may hold copies from the caller's input buffers and into
+  // its output buffers: every exit below waits for it, so the buffers are
+  // never touched after return
+  double d = 0.0;
+  int s = 0;
+  const int r = step_host_run(h, tsave, &d, &s, U_out, species_out, late);
   const cudaError_t es = cudaStreamSynchronize(h->io_stream);
   if (r != MHD_OK) {
     cudaStreamSynchronize(h->stream);   // its copies into U_out too

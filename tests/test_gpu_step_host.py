@@ -1,8 +1,9 @@
 """mhd_step_host (one step from host arrays to host arrays, copying arrays
 back while the step still runs) against the device-resident path:
 mhd_upload + mhd_step + mhd_download must give the same state bit for bit,
-with and without the chemistry network, in both forms, and over several
-calls that feed each step's output back in."""
+with and without the chemistry network or SHIELD, in both forms, from
+pageable and page-locked buffers, and over several calls that feed each
+step's output back in."""
 import numpy as np
 import pytest
 
@@ -45,6 +46,39 @@ def test_step_host_inflow_chemistry():
     st.params = st.params.replace(ifchem=2)
     inflow, dinit = problems.shock_tube_inflow()
     Ur, Sr, U, S = run_both(st, native.PREC_FP64, 3, inflow=(inflow, None, dinit))
+    assert np.array_equal(Ur.view(np.int64), U.view(np.int64))
+    assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
+
+
+def test_step_host_shield_without_chemistry():
+    """SHIELD reads C, C+ and CO before the sweeps, so they come in with the
+    other arrays (not on the copy stream as without chemistry or SHIELD)."""
+    st = problems.colliding_flows(16)
+    st.params = st.params.replace(ifrad=2)
+    Ur, Sr, U, S = run_both(st, native.PREC_FP32, 3)
+    assert np.array_equal(Ur.view(np.int64), U.view(np.int64))
+    assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
+
+
+def test_step_host_pinned_buffers():
+    """With page-locked host buffers every copy is asynchronous: species 5-7
+    arrive on the copy stream while the time step and the first SOURCE run,
+    and the arrays copied back overlap the rest of the step."""
+    torch = pytest.importorskip("torch")
+    st = problems.colliding_flows(32)
+    ref = native.Mhd3D(st.params, precision=native.PREC_FP32)
+    host = native.Mhd3D(st.params, precision=native.PREC_FP32)
+    for g in (ref, host):
+        g.upload(st)
+    shape = (8,) + tuple(st.U.shape[1:])
+    U, S, Uo, So = (torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4))
+    U[...] = st.U
+    S[...] = st.species
+    for _ in range(3):
+        assert ref.step() == host.step_host(U, S, Uo, So)
+        U[...] = Uo
+        S[...] = So
+    Ur, Sr, _ = ref.download()
     assert np.array_equal(Ur.view(np.int64), U.view(np.int64))
     assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
 
