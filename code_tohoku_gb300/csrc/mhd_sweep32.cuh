@@ -24,7 +24,8 @@
 // each (L = n+4), plus FP32 copies of the coordinate widths.  Ghost entries
 // of a buffer are written by the thread that computes their source cell
 // (periodic wrap or free copy), so the in-pencil halo exchanges cost no
-// extra barrier: the sweep has 11 barriers.
+// extra barrier: the sweep has 12 barriers, one after each of its 13
+// phases but the last.
 //
 // VLIMIT's T switch keeps the reference's meaning at every stage: p for
 // RHS, e inside and p in the ghosts for MOC, E for the remap.
@@ -99,7 +100,7 @@ constexpr int kSmemUnroll = MHD_SWEEP_SMEM_UNROLL;
 // more threads, a phase over 4 pencils of 256 cells (1024 items) never
 // fills a group of 4 trips, yet the group's code sets the kernel's
 // register count: depth 4 needs 96 registers, depth 1 fits in 56 at 576
-// threads without spills.
+// threads (with a 72-byte spill) and depth 2 measured no faster.
 #ifndef MHD_SWEEP_GLOBAL_UNROLL
 #define MHD_SWEEP_GLOBAL_UNROLL 1
 #endif
