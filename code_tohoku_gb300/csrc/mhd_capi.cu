@@ -40,6 +40,10 @@ struct mhd_handle {
   double dxh = 0.0;               // SHIELD's half width 0.5 dx(1)
   float *temp32 = nullptr;
   float *sh2_32 = nullptr;               // SOURCE's FP32 S = H+p+He+He+ and H2 (2 ncell floats)
+  // sh2_32 holds S and H2 of the current species: set by SOURCE's first
+  // pass, cleared by every writer of the species (upload, mhd_step_host,
+  // the sweeps, the chemistry network)
+  bool sh2_valid = false;
   int *stiff_list = nullptr;             // SOURCE's stiff cells (FP32 form with a surrogate)
   float *vf32[3] = {nullptr, nullptr, nullptr};
   float *bf32[3] = {nullptr, nullptr, nullptr};
@@ -342,6 +346,7 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
   CKR(cudaSetDevice(h->p.device));
   const Grid &g = h->g;
   size_t nb = (size_t)g.ncell * sizeof(double);
+  h->sh2_valid = false;
   for (int f = 0; f < 8; f++) CKR(cudaMemcpyAsync(h->f.U[f], U + (size_t)f * g.ncell, nb, cudaMemcpyHostToDevice, h->stream));
   for (int s = 0; s < 8; s++)
     CKR(cudaMemcpyAsync(h->f.sp[s], species + (size_t)s * g.ncell, nb, cudaMemcpyHostToDevice, h->stream));
@@ -418,7 +423,10 @@ int mhd_timestep(mhd_handle *h, double *dt, int *st) {
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
   CKR(cudaMemsetAsync(h->dtred, 0xff, 2 * sizeof(unsigned long long), h->stream));
-  if (h->p.precision == MHD_PREC_FP32) CK(dt_reduce_fp32(h->g, h->ph, h->f, h->dtred, h->err, h->stream));
+  // the time step reads S and H2 of the interior cells from SOURCE's
+  // arrays while the species are unchanged since (the same floats)
+  if (h->p.precision == MHD_PREC_FP32)
+    CK(dt_reduce_fp32(h->g, h->ph, h->f, h->sh2_valid ? h->sh2_32 : nullptr, h->dtred, h->err, h->stream));
   else CK(dt_reduce(h->g, h->ph, h->f, h->dtred, h->err, h->stream));
   CKR(cudaMemcpyAsync(h->h_small, h->dtred, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
   TRY(check_err(h));
@@ -471,7 +479,12 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
     // with a surrogate, source_fp32 launches a second (stiff-cell) kernel
     const int extra = (a.W && h->ph.ifchem != 2) ? 1 : 0;
-    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, true, h->stream));
+    // S and H2 from the species, unless SOURCE formed them from the same
+    // species before (the previous step's second SOURCE); an inflow side
+    // refills the ghost species from the advected reservoir every time
+    const bool inflow = h->ph.in.on[0] || h->ph.in.on[1];
+    CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, !(h->sh2_valid && !inflow), h->stream));
+    h->sh2_valid = true;
     CK(source_fp32(a, h->stream));
     h->launches += extra;
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
@@ -508,6 +521,7 @@ int source_impl(mhd_handle *h, double dt, bool rho_sp_filled) {
   if (h->p.ifchem == 2) {
     if (h->p.precision == MHD_PREC_FP32) CK(chem_step_fp32(h->g, h->ph, h->f, dt, h->err, h->stream));
     else CK(chem_step(h->g, h->ph, h->f, dt, h->err, h->stream));
+    h->sh2_valid = false;
   }
   return MHD_OK;
 }
@@ -520,6 +534,7 @@ int mhd_sweep(mhd_handle *h, int dir, double dt) {
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   TRY(need_inflow(h));
   CKR(cudaSetDevice(h->p.device));
+  h->sh2_valid = false;   // the sweeps move the species
   SweepArgs a{};
   a.g = h->g; a.ph = h->ph; a.f = h->f; a.dt = dt; a.err = h->err;
   if (h->p.precision == MHD_PREC_FP32) CK(sweep_fp32(dir, a, h->stream));
@@ -708,6 +723,7 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   // come in on the copy stream, after the other copies, while those kernels
   // run; the first sweep waits for them.
   const bool late = h->p.ifchem != 2 && h->p.ifrad != 2;
+  h->sh2_valid = false;
   for (int q = 0; q < 8; q++) CKR(cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
   for (int q = 0; q < (late ? 5 : 8); q++)
     CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));

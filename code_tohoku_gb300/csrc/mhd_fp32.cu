@@ -122,12 +122,12 @@ cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s) {
   if (dir == 1) return launch32_d<1>(a, s);
   return launch32_d<2>(a, s);
 }
-cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
-                           cudaStream_t s) {
+cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, unsigned long long *out,
+                           int *err, cudaStream_t s) {
   long long n = (long long)g.n[0] * g.n[1] * g.n[2];
   // a thread per cell: with a capped grid of 4864 blocks (~13 cells per
   // thread, 50x fewer atomics) the 256^3 kernel took 385 us against 333-358
-  dt32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, out, err);
+  dt32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, sh2, out, err);
   return cudaGetLastError();
 }
 

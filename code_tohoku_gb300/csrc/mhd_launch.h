@@ -24,8 +24,10 @@ cudaError_t source_fp32(const Source32Args &a, cudaStream_t s);
 // (and store S = H+p+He+He+ and H2 in sh2, 2 ncell floats), else from them
 cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *sh2,
                       bool from_species, cudaStream_t s);
-cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
-                           cudaStream_t s);
+// sh2: S and H2 of every cell (SOURCE's arrays) when they are current, or
+// null to form them from the species
+cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, unsigned long long *out,
+                           int *err, cudaStream_t s);
 cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
 cudaError_t ct_prep_fp32(const Grid &g, const Fields &f, double *const vf[3], double kb, const CT32Args &a,
                          cudaStream_t s);

@@ -77,7 +77,9 @@ namespace mhd {
 // so they are formed once per pass instead of once per neighbour.  The
 // predictor pass also stores S = H + p + He + He+ and H2 (sh2[t], sh2[ncell
 // + t]), which both passes of the KI source read instead of the five
-// species (they do not change within a SOURCE call).
+// species (they do not change within a SOURCE call); the host keeps them
+// while the species stay unchanged, for the next time step and the next
+// SOURCE, whose predictor pass then takes the <false> form too.
 // The species pass handles two cells per thread (block-strided, loads of
 // both issued first) to keep more loads in flight.
 template <bool FROM_SPECIES>
@@ -324,7 +326,8 @@ __global__ void __launch_bounds__(128) source32_stiff_kernel(Source32Args A) {
 // limit of Stblty (:2784-2822) in FP32; the per-cell minima are widened to
 // FP64 bit patterns for the same order-independent atomicMin reduction.
 // Grid-stride loop over the cells (the launch uses a thread per cell).
-__global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, unsigned long long *out, int *err) {
+__global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, const float *sh2, unsigned long long *out,
+                                                   int *err) {
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   float c_min = d2f(ph.tfinal), s_min = c_min;
   const long long ncells = (long long)nx * ny * nz, stride = (long long)gridDim.x * blockDim.x;
@@ -333,9 +336,15 @@ __global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, un
     split3(t, nx, ny, i, j, k);
     i += 1; j += 1; k += 1;
     long long a = gidx(g, i, j, k);
-    float H = d2f(f.sp[0][a]), pr = d2f(f.sp[1][a]), H2 = d2f(f.sp[2][a]), He = d2f(f.sp[3][a]),
-          Hep = d2f(f.sp[4][a]);
-    float S = H + pr + He + Hep;
+    // S = H+p+He+He+ and H2: SOURCE's floats when current (the same sums)
+    float S, H2;
+    if (sh2) {
+      S = sh2[a];
+      H2 = sh2[g.ncell + a];
+    } else {
+      S = d2f(f.sp[0][a]) + d2f(f.sp[1][a]) + d2f(f.sp[3][a]) + d2f(f.sp[4][a]);
+      H2 = d2f(f.sp[2][a]);
+    }
     float rg = __fdividef(1.0f, 3.0f * S + 5.0f * H2);
     float gam = (5.0f * S + 7.0f * H2) * rg;
     float bx = d2f(f.bcc[0][a]), by = d2f(f.bcc[1][a]), bz = d2f(f.bcc[2][a]);
