@@ -100,7 +100,7 @@ constexpr int kSmemUnroll = MHD_SWEEP_SMEM_UNROLL;
 // more threads, a phase over 4 pencils of 256 cells (1024 items) never
 // fills a group of 4 trips, yet the group's code sets the kernel's
 // register count: depth 4 needs 96 registers, depth 1 fits in 56 at 576
-// threads (with a 72-byte spill) and depth 2 measured no faster.
+// threads without spills and depth 2 measured no faster.
 #ifndef MHD_SWEEP_GLOBAL_UNROLL
 #define MHD_SWEEP_GLOBAL_UNROLL 1
 #endif
@@ -132,19 +132,19 @@ constexpr int kHoistLoads = MHD_SWEEP_HOIST_LOADS;
 // stored.  Columns beyond the padded grid read the last column.
 template <int DIR, int P>
 struct PencilRun {
-  long long b0, sp, sd;
+  int b0, sp, sd;   // 32-bit cell offsets: the padded grid has fewer than 2^31 cells
   unsigned act;   // bit p: pencil p is an interior pencil
   int plast;      // last pencil inside the padded grid
   __device__ PencilRun(const Grid &g) {
-    sd = g.st[DIR];
+    sd = (int)g.st[DIR];
     act = (1u << P) - 1;
     plast = P - 1;
     if (DIR == 0) {
-      b0 = gidx(g, -1, blockIdx.x * P + 1, blockIdx.y + 1);
-      sp = g.st[1];
+      b0 = (int)gidx(g, -1, blockIdx.x * P + 1, blockIdx.y + 1);
+      sp = (int)g.st[1];
     } else {
       const int x0 = (int)blockIdx.x * P - 1;
-      b0 = (DIR == 1) ? gidx(g, x0, -1, blockIdx.y + 1) : gidx(g, x0, blockIdx.y + 1, -1);
+      b0 = (int)((DIR == 1) ? gidx(g, x0, -1, blockIdx.y + 1) : gidx(g, x0, blockIdx.y + 1, -1));
       sp = 1;
       act = 0;
       for (int p = 0; p < P; p++)
@@ -154,8 +154,8 @@ struct PencilRun {
   }
   __device__ __forceinline__ bool active(int p) const { return (act >> p) & 1u; }
   // global offset of sweep position i (-1..n+2) on pencil p
-  __device__ __forceinline__ long long at(int p, int i) const {
-    return b0 + min(p, plast) * sp + (long long)(i + 1) * sd;
+  __device__ __forceinline__ int at(int p, int i) const {
+    return b0 + min(p, plast) * sp + (i + 1) * sd;
   }
 };
 
@@ -323,16 +323,16 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   // four ghost positions: x sweep at 256^3 1.87 -> 1.83 ms); the y and z
   // sweeps keep a separate pass over all n+4 positions (2.34 / 2.42 ms
   // folded against 2.32 / 2.42).
-  auto load_transverse = [&](int i, int p, long long a) {
+  auto load_transverse = [&](int i, int p, int a) {
     const double c1 = __ldg(A.f.bcc[C1] + a), c2 = __ldg(A.f.bcc[C2] + a);
     double l1a = 0.0, l1b = 0.0, l2a = 0.0, l2b = 0.0, r1a = 0.0, r1b = 0.0, r2a = 0.0, r2b = 0.0;
     if (i == 1) {
-      const long long g0 = pc.at(p, -1), g1 = pc.at(p, 0);
+      const int g0 = pc.at(p, -1), g1 = pc.at(p, 0);
       l1a = __ldg(A.f.bcc[C1] + g0); l1b = __ldg(A.f.bcc[C1] + g1);
       l2a = __ldg(A.f.bcc[C2] + g0); l2b = __ldg(A.f.bcc[C2] + g1);
     }
     if (i == N) {
-      const long long g0 = pc.at(p, N + 1), g1 = pc.at(p, N + 2);
+      const int g0 = pc.at(p, N + 1), g1 = pc.at(p, N + 2);
       r1a = __ldg(A.f.bcc[C1] + g0); r1b = __ldg(A.f.bcc[C1] + g1);
       r2a = __ldg(A.f.bcc[C2] + g0); r2b = __ldg(A.f.bcc[C2] + g1);
     }
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     // memory once per position rather than once per field group
     unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
       const int i = 1 + t / P, p = t % P;
-      const long long a = pc.at(p, i);
+      const int a = pc.at(p, i);
       const double u0 = __ldg(A.f.U[0] + a), un = __ldg(A.f.U[1 + DIR] + a), u1 = __ldg(A.f.U[1 + C1] + a),
                    u2 = __ldg(A.f.U[1 + C2] + a), u4 = __ldg(A.f.U[4] + a);
       const double s0 = __ldg(A.f.sp[0] + a), s1 = __ldg(A.f.sp[1] + a), s2 = __ldg(A.f.sp[2] + a),
@@ -368,20 +368,20 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     // three passes: transverse field (-1..n+2), flow state, species + face field
     unrolled<NT, kGlobalUnroll>(L * P, [&](int t) {
       const int i = t / P - 1, p = t % P;
-      const long long a = pc.at(p, i);
+      const int a = pc.at(p, i);
       Fb(F_B1, i, p) = d2f(__ldg(A.f.bcc[C1] + a));
       Fb(F_B2, i, p) = d2f(__ldg(A.f.bcc[C2] + a));
     });
     unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
       const int i = 1 + t / P, p = t % P;
-      const long long a = pc.at(p, i);
+      const int a = pc.at(p, i);
       const double u0 = __ldg(A.f.U[0] + a), un = __ldg(A.f.U[1 + DIR] + a), u1 = __ldg(A.f.U[1 + C1] + a),
                    u2 = __ldg(A.f.U[1 + C2] + a), u4 = __ldg(A.f.U[4] + a);
       load_flow(i, p, u0, un, u1, u2, u4);
     });
     unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
       const int i = 1 + t / P, p = t % P;
-      const long long a = pc.at(p, i);
+      const int a = pc.at(p, i);
       const double s0 = __ldg(A.f.sp[0] + a), s1 = __ldg(A.f.sp[1] + a), s2 = __ldg(A.f.sp[2] + a),
                    s3 = __ldg(A.f.sp[3] + a), s4 = __ldg(A.f.sp[4] + a), bn = __ldg(A.f.U[5 + DIR] + a),
                    bnc = __ldg(A.f.bcc[DIR] + a);
@@ -579,7 +579,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
     const bool act = pc.active(p);
-    long long a = pc.at(p, i);
+    const int a = pc.at(p, i);
     // FP64 inputs of the position: loaded here together (hoisted) or by
     // get() where they are used
     const double *src[8] = {A.f.U[0], A.f.U[1 + DIR], A.f.U[1 + C1], A.f.U[1 + C2],
@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   });
   __syncthreads();
   // ------------------------- K: species 0-3 finish, 4-7 reconstruction
-  auto species_new = [&](int s, double n0, long long a, int i, int p, int fb, bool act) {
+  auto species_new = [&](int s, double n0, int a, int i, int p, int fb, bool act) {
     const float rw = cx(C_RDX, i);
     float dn = (Fb(fb, i, p) - Fb(fb, i - 1, p)) * rw;
     float nf = d2f(n0) + dn;   // remapped value, before the floor
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
     const bool act = pc.active(p);
-    long long a = pc.at(p, i);
+    const int a = pc.at(p, i);
     double pre[8];
     if constexpr (((kHoistLoads >> DIR) & 1) != 0) {
 #pragma unroll
@@ -713,7 +713,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
   unrolled<NT, kGlobalUnroll>(N * P, [&](int t) {
     int i = 1 + t / P, p = t % P;
     const bool act = pc.active(p);
-    long long a = pc.at(p, i);
+    const int a = pc.at(p, i);
     const double *src[4] = {A.f.sp[4], A.f.sp[5], A.f.sp[6], A.f.sp[7]};
     double pre[4];
     if constexpr (((kHoistLoads >> DIR) & 1) != 0) {
