@@ -122,7 +122,7 @@ constexpr int kSourceDeferThreads = 512;
 // conversions are integer ones.
 template <bool CHEM>
 struct Cell32 {
-  long long a;
+  int a;   // 32-bit cell offset (the padded grid has fewer than 2^31 cells)
   float T0, div, g1, NN, nimc, nkbi, dts, basef, CooL, dx0;
   double base;
   bool stiff;
@@ -137,14 +137,14 @@ __device__ __forceinline__ Cell32<CHEM> source32_prep(const Source32Args &A, lon
   split3(t, nx, ny, i, j, k);
   i += 1; j += 1; k += 1;
   Cell32<CHEM> c;
-  const long long a = gidx(g, i, j, k);
+  const int a = (int)gidx(g, i, j, k);
   c.a = a;
   const float kb = d2f(A.ph.kb), Kc = d2f(A.ph.kcond);
   const float dt = d2f(A.dt);
   const Fields &f = A.f;
   const float *T = A.T;
   const float *dx = g.dxf[0], *dy = g.dxf[1], *dz = g.dxf[2];
-  const long long sy = g.st[1], sz = g.st[2];
+  const int sy = (int)g.st[1], sz = (int)g.st[2];
   const float T0 = T[a];
   auto flux = [&](float Tl, float Tu, float dl, float du) {
     float rdu = __fdividef(1.0f, dl + du);
@@ -160,7 +160,7 @@ __device__ __forceinline__ Cell32<CHEM> source32_prep(const Source32Args &A, lon
   float S, H2;
   if (!CHEM && A.sh2) {
     S = A.sh2[a];
-    H2 = A.sh2[g.ncell + a];
+    H2 = A.sh2[(int)g.ncell + a];
   } else {
     S = d2f(f.sp[0][a]) + d2f(f.sp[1][a]) + d2f(f.sp[3][a]) + d2f(f.sp[4][a]);
     H2 = d2f(f.sp[2][a]);
