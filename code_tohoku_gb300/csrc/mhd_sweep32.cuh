@@ -76,6 +76,35 @@ __host__ __device__ inline size_t sweep32_smem_bytes(int n, int P, int LS = 0) {
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
+// VLIMIT (vlim_sel) with the cell widths' divisors formed once per cell and
+// shared by all fields of a phase: minmod's 2 dq / (dx0 + dx+-) as
+// dq * (2 / (dx0 + dx+-)), van Albada's slope as a product with
+// 1 / (dx0 + dx-/2 + dx+/2); only the branch the switch s keeps is formed.
+struct LimW {
+  float rp, rm, ra, s;
+};
+__device__ __forceinline__ LimW lim_w(float dxm, float dx0, float dxp, float s) {
+  LimW w;
+  w.s = s;
+  w.rp = w.rm = w.ra = 0.0f;
+  if (s > 0.0f) {
+    w.rp = __fdividef(2.0f, dx0 + dxp);
+    w.rm = __fdividef(2.0f, dx0 + dxm);
+  } else {
+    w.ra = __fdividef(1.0f, dx0 + 0.5f * dxm + 0.5f * dxp);
+  }
+  return w;
+}
+__device__ __forceinline__ float vlim_w(float qm, float q0, float qp, const LimW &w) {
+  if (w.s > 0.0f) {
+    const float dp = (qp - q0) * w.rp, dm = (q0 - qm) * w.rm;
+    return (dp * dm > 0.0f) ? copysignf(fminf(fabsf(dp), fabsf(dm)), dp) : 0.0f;
+  }
+  const float delp = qp - q0, delm = q0 - qm;
+  const float flmt = fmaxf(0.0f, __fdividef(2.0f * delp * delm + 1e-10f, delp * delp + delm * delm + 1e-10f));
+  return flmt * (qp - qm) * w.ra;
+}
+
 // Work loop of a phase: items t = threadIdx.x + k*NT < cnt.  Groups of UNR
 // items that are all in range run as one unrolled block, so the loads of
 // the group can be in flight together; the rest run one by one.
@@ -237,8 +266,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
       if (side == 0 ? inL : inR) Fb(bl[bq], gi, p) = inflow32(rl[bq], side, gi, p);
     }
   };
-  auto vl = [&](int b, int i, int p, float dm, float d0, float dp, float s) {
-    return vlim_sel(Fb(b, i - 1, p), Fb(b, i, p), Fb(b, i + 1, p), dm, d0, dp, s);
+  auto vlw = [&](int b, int i, int p, const LimW &w) {
+    return vlim_w(Fb(b, i - 1, p), Fb(b, i, p), Fb(b, i + 1, p), w);
   };
   auto tsw = [&](float e5, float rho) { return (1.27f * e5 >= 3.0f * kb * rho) ? 0.5f : -0.5f; };
   // Upwind MUSCL fluxes through interface i: the upwind cell c, its
@@ -249,6 +278,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     int c;
     bool left;   // vadt <= 0: the upwind cell is i+1
     float vadt, dm, d0, dp, s, w;
+    LimW lw;   // the limiter's width divisors of cell c
   };
   auto upwind = [&](int i, int p, float vadt) {
     Upwind u;
@@ -260,10 +290,11 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     u.dp = Fb(F_DXL, u.c + 1, p);
     u.s = Fb(F_SW, u.c, p);
     u.w = u.left ? (0.5f * (u.d0 + vadt) * facdep) : (0.5f * (u.d0 - vadt) * facdep);
+    u.lw = lim_w(u.dm, u.d0, u.dp, u.s);
     return u;
   };
   auto flux = [&](int qb, const Upwind &u, int p) {
-    const float gs = vl(qb, u.c, p, u.dm, u.d0, u.dp, u.s);
+    const float gs = vlw(qb, u.c, p, u.lw);
     const float q = Fb(qb, u.c, p);
     return u.left ? -u.vadt * (q - u.w * gs) : -u.vadt * (q + u.w * gs);
   };
@@ -402,11 +433,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     Fb(F_GAM, i, p) = fdiv(5.0f * S + 7.0f * H2, 3.0f * S + 5.0f * H2);
     float dm = cx(C_DX, i - 1), d0 = cx(C_DX, i), dp = cx(C_DX, i + 1);
     float s = tsw(Fb(F_P, i, p), Fb(F_R, i, p));
-    Fb(F_G0, i, p) = vl(F_R, i, p, dm, d0, dp, s);
-    Fb(F_G1, i, p) = vl(F_VN, i, p, dm, d0, dp, s);
-    Fb(F_G2, i, p) = vl(F_P, i, p, dm, d0, dp, s);
-    Fb(F_G3, i, p) = vl(F_B1, i, p, dm, d0, dp, s);
-    Fb(F_G4, i, p) = vl(F_B2, i, p, dm, d0, dp, s);
+    const LimW w = lim_w(dm, d0, dp, s);
+    Fb(F_G0, i, p) = vlw(F_R, i, p, w);
+    Fb(F_G1, i, p) = vlw(F_VN, i, p, w);
+    Fb(F_G2, i, p) = vlw(F_P, i, p, w);
+    Fb(F_G3, i, p) = vlw(F_B1, i, p, w);
+    Fb(F_G4, i, p) = vlw(F_B2, i, p, w);
   });
   __syncthreads();
   // ------------------------------------------------ C: Riemann (RHS)
@@ -475,11 +507,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A) {
     int i = t / P, p = t % P;
     float dm = Fb(F_DXL, i - 1, p), d0 = Fb(F_DXL, i, p), dp = Fb(F_DXL, i + 1, p);
     float s = tsw(Fb(F_T, i, p), Fb(F_R, i, p));
-    Fb(F_G0, i, p) = vl(F_R, i, p, dm, d0, dp, s);
-    Fb(F_G1, i, p) = vl(F_VT1, i, p, dm, d0, dp, s);
-    Fb(F_G2, i, p) = vl(F_VT2, i, p, dm, d0, dp, s);
-    Fb(F_G3, i, p) = vl(F_B1, i, p, dm, d0, dp, s);
-    Fb(F_G4, i, p) = vl(F_B2, i, p, dm, d0, dp, s);
+    const LimW w = lim_w(dm, d0, dp, s);
+    Fb(F_G0, i, p) = vlw(F_R, i, p, w);
+    Fb(F_G1, i, p) = vlw(F_VT1, i, p, w);
+    Fb(F_G2, i, p) = vlw(F_VT2, i, p, w);
+    Fb(F_G3, i, p) = vlw(F_B1, i, p, w);
+    Fb(F_G4, i, p) = vlw(F_B2, i, p, w);
   });
   __syncthreads();
   // ------------------------------------------------ F: characteristics
