@@ -203,7 +203,7 @@ def run_reference(args, rank):
             "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
                              "kind": "port",
                              "sample": f"{args.steps} steps of the {n}^3 problem; C++ restatement of "
-                                       "MCF3DSGincfca3.f90 (no Fortran compiler on the box)"},
+                                       "MCF3DSGincfca3.f90 (no Fortran compiler on this machine)"},
             "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

@@ -4,7 +4,7 @@ The step has no inter-GPU exchange on one GPU (the whole grid is resident),
 so N GPUs run N independent replicas of the same problem ("replicas only").
 These helpers do the only cross-rank work: agree on the slowest rank's time
 and form the whole-job throughput.  They use torch.distributed with any
-backend (NCCL on the GPU machine, gloo in the CPU tests).
+backend (NCCL on GPUs, gloo in the CPU tests).
 """
 import os
 

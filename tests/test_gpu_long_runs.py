@@ -1,5 +1,5 @@
 """Long runs of the plain FP64 path against the oracle, bit for bit: the
-the benchmark spec bar is 1e-12 relative per cell after 100 steps; these hold every
+required agreement is 1e-12 relative per cell after 100 steps; these hold every
 interior value identical after 100 steps of the decaying turbulence and of
 the KI colliding flows, and after 50 steps of the shipped deck's setup
 (inflow boundaries, chemistry network and species cooling), at sizes the
