@@ -113,14 +113,18 @@ __global__ void __launch_bounds__(128) emf32_kernel(CT32Args A) {
   const float facm = A.facm, dt = A.dt;
   const float *dxe = g.dxf[da], *dye = g.dxf[db];
   const float dxm = dxe[aa], dx0 = dxe[aa + 1], dym = dye[bb], dy0 = dye[bb + 1];
-  // VLIMIT of a face array along direction d at cell c (T switch of cell c)
-  auto slope = [&](const float *q, long long c, long long sd, const float *dxx, int pos) {
-    return vlim_sel(q[c - sd], q[c], q[c + sd], dxx[pos], dxx[pos + 1], dxx[pos + 2], sw[c]);
+  // VLIMIT of two face arrays along direction d at cell c (T switch of cell
+  // c): the same widths and switch, so the divisors are formed once
+  auto slopes = [&](const float *q, const float *r, long long c, long long sd, const float *dxx, int pos,
+                    float &sq, float &sr) {
+    const LimW w = lim_w(dxx[pos], dxx[pos + 1], dxx[pos + 2], sw[c]);
+    sq = vlim_w(q[c - sd], q[c], q[c + sd], w);
+    sr = vlim_w(r[c - sd], r[c], r[c + sd], w);
   };
   auto load1 = [&](long long p, int bpos, float &a1p, float &a1m, float &da1p, float &da1m) {
     float v = Vx[p], b = Bxf[p];
-    float q1 = slope(Vx, p, sb, dye, bpos);
-    float q3 = slope(Bxf, p, sb, dye, bpos);
+    float q1, q3;
+    slopes(Vx, Bxf, p, sb, dye, bpos, q1, q3);
     a1p = v + b * dsqinv;
     da1p = (q1 + q3 * dsqinv) * facm;
     a1m = v - b * dsqinv;
@@ -128,8 +132,8 @@ __global__ void __launch_bounds__(128) emf32_kernel(CT32Args A) {
   };
   auto load2 = [&](long long p, int apos, float &a2m, float &a2p, float &da2m, float &da2p) {
     float v = Vy[p], b = Byf[p];
-    float q2 = slope(Vy, p, sa, dxe, apos);
-    float q4 = slope(Byf, p, sa, dxe, apos);
+    float q2, q4;
+    slopes(Vy, Byf, p, sa, dxe, apos, q2, q4);
     a2m = v - b * dsqinv;
     da2m = (q2 - q4 * dsqinv) * facm;
     a2p = v + b * dsqinv;

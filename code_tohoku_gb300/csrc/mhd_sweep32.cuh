@@ -76,34 +76,6 @@ __host__ __device__ inline size_t sweep32_smem_bytes(int n, int P, int LS = 0) {
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
-// VLIMIT (vlim_sel) with the cell widths' divisors formed once per cell and
-// shared by all fields of a phase: minmod's 2 dq / (dx0 + dx+-) as
-// dq * (2 / (dx0 + dx+-)), van Albada's slope as a product with
-// 1 / (dx0 + dx-/2 + dx+/2); only the branch the switch s keeps is formed.
-struct LimW {
-  float rp, rm, ra, s;
-};
-__device__ __forceinline__ LimW lim_w(float dxm, float dx0, float dxp, float s) {
-  LimW w;
-  w.s = s;
-  w.rp = w.rm = w.ra = 0.0f;
-  if (s > 0.0f) {
-    w.rp = __fdividef(2.0f, dx0 + dxp);
-    w.rm = __fdividef(2.0f, dx0 + dxm);
-  } else {
-    w.ra = __fdividef(1.0f, dx0 + 0.5f * dxm + 0.5f * dxp);
-  }
-  return w;
-}
-__device__ __forceinline__ float vlim_w(float qm, float q0, float qp, const LimW &w) {
-  if (w.s > 0.0f) {
-    const float dp = (qp - q0) * w.rp, dm = (q0 - qm) * w.rm;
-    return (dp * dm > 0.0f) ? copysignf(fminf(fabsf(dp), fabsf(dm)), dp) : 0.0f;
-  }
-  const float delp = qp - q0, delm = q0 - qm;
-  const float flmt = fmaxf(0.0f, __fdividef(2.0f * delp * delm + 1e-10f, delp * delp + delm * delm + 1e-10f));
-  return flmt * (qp - qm) * w.ra;
-}
 
 // Work loop of a phase: items t = threadIdx.x + k*NT < cnt.  Groups of UNR
 // items that are all in range run as one unrolled block, so the loads of
