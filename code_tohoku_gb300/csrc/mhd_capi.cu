@@ -728,11 +728,15 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   for (int q = 0; q < (late ? 5 : 8); q++)
     CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
   if (late) {
-    CKR(cudaEventRecord(h->ev_io[2], h->stream));   // after everything queued before (readers included)
-    CKR(cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0));
-    for (int q = 5; q < 8; q++)
-      CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->io_stream));
-    CKR(cudaEventRecord(h->ev_io[2], h->io_stream));
+    cudaError_t e = cudaEventRecord(h->ev_io[2], h->stream);   // after everything queued before (readers included)
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0);
+    for (int q = 5; q < 8 && e == cudaSuccess; q++)
+      e = cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->io_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev_io[2], h->io_stream);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(h->io_stream);   // no copy from the caller's buffers outlives the call
+      return fail(h, MHD_ERR_CUDA, "species copy stream: %s", cudaGetErrorString(e));
+    }
   }
   // the copy stream may hold copies from the caller's input buffers and into
   // its output buffers: every exit below waits for it, so the buffers are
