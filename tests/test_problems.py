@@ -72,3 +72,33 @@ def test_turbulence_state():
         a = st.U[q]
         assert np.array_equal(a[:, :, 0:2], a[:, :, 8:10]) and np.array_equal(a[:, :, 10:12], a[:, :, 2:4])
         assert np.array_equal(a[:, 0:2, :], a[:, 8:10, :]) and np.array_equal(a[0:2], a[8:10])
+
+
+def test_colliding_flows_state():
+    """The benchmark workload: 3 uG at 45 deg in x-y, converging +-20 km/s
+    flows, free x and periodic y, z boundaries, T0 = 6000 K, lognormal
+    density with a 10 % log rms, WNM species proportional to rho."""
+    st = problems.colliding_flows(16)
+    p = st.params
+    assert p.bc == (1, 1, 3, 3, 3, 3) and p.ifthrm == 2 and p.dissip == 1
+    inner = (slice(2, -2),) * 3
+    bx, by = st.U[5], st.U[6]
+    assert np.allclose(np.hypot(bx, by), 3.0 / 0.448, rtol=1e-15)
+    assert np.allclose(bx, by, rtol=1e-15) and np.all(st.U[7] == 0.0)
+    lg = np.log(st.U[0][inner] / problems.MU)
+    assert math.isclose(np.sqrt(np.mean(lg * lg)), 0.1, rel_tol=1e-12)
+    vx = st.U[1][inner][0, 0]
+    assert vx[0] > 0.9 * 20.0 / 0.9778 and vx[-1] < -0.9 * 20.0 / 0.9778   # converging at the mid-plane
+    # evaluated at the right faces x(i) (:438): antisymmetric about x(n/2) = L/2
+    # over cells 1..n-1, zero at cell n/2
+    assert np.allclose(vx[:-1], -vx[:-1][::-1], atol=1e-12) and vx[len(vx) // 2 - 1] == 0.0
+    # free x sides: both ghost columns copy the first / last interior cell
+    for g in (0, 1):
+        assert np.array_equal(st.U[:, :, :, g], st.U[:, :, :, 2])
+        assert np.array_equal(st.U[:, :, :, -1 - g], st.U[:, :, :, -3])
+    # species in fixed proportion to rho; pressure uniform at the mean T0
+    ratio = st.species[:, 2:-2, 2:-2, 2:-2] / st.U[0][inner]
+    assert np.allclose(ratio, ratio[:, :1, :1, :1], rtol=1e-14)
+    ntot = sum(st.species[s][inner] for s in range(5))
+    assert np.all(st.U[4] == st.U[4][2, 2, 2])
+    assert math.isclose(st.U[4][2, 2, 2] / (problems.KB * np.mean(ntot)), 6.0, rel_tol=1e-14)
