@@ -106,6 +106,7 @@ typedef struct mhd_handle mhd_handle;
 
 /* Allocates the resident state for p on p->device.  No data yet. */
 int mhd_create(const mhd_params *p, mhd_handle **out);
+/* Frees the handle and its device memory; a NULL handle is a no-op (MHD_OK). */
 int mhd_destroy(mhd_handle *h);
 
 /* INITIA/restart read: copies the full arrays (ghosts included) and runs

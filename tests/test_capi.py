@@ -65,3 +65,39 @@ def test_create_without_gpu_reports_no_device():
     assert L.mhd_create(ctypes.byref(p), ctypes.byref(h)) == 6   # MHD_ERR_NO_DEVICE
     with pytest.raises(native.MhdError):
         native.Mhd3D(MhdParams(16, 16, 16))
+
+
+def test_null_handle_is_an_argument_error():
+    """Every entry point that takes a handle rejects NULL with MHD_ERR_ARG
+    before touching the device (mhd_destroy(NULL) is a no-op, like free)."""
+    L = ctypes.CDLL(build.build())   # untyped: plain C calls
+    buf = (ctypes.c_double * 64)()
+    d, i = ctypes.c_double(), ctypes.c_int()
+    dt = ctypes.c_double(0.1)
+    calls = {
+        "mhd_upload": lambda: L.mhd_upload(None, buf, buf, buf, buf, buf, buf, buf, buf),
+        "mhd_download": lambda: L.mhd_download(None, buf, buf, buf),
+        "mhd_download_columns": lambda: L.mhd_download_columns(None, buf),
+        "mhd_timestep": lambda: L.mhd_timestep(None, ctypes.byref(d), ctypes.byref(i)),
+        "mhd_source": lambda: L.mhd_source(None, dt),
+        "mhd_sweep": lambda: L.mhd_sweep(None, 0, dt),
+        "mhd_ct": lambda: L.mhd_ct(None, dt),
+        "mhd_dissip": lambda: L.mhd_dissip(None),
+        "mhd_advance": lambda: L.mhd_advance(None, dt),
+        "mhd_step": lambda: L.mhd_step(None, ctypes.c_double(1e30), ctypes.byref(d), ctypes.byref(i)),
+        "mhd_step_host": lambda: L.mhd_step_host(None, buf, buf, buf, buf, ctypes.c_double(1e30),
+                                                 ctypes.byref(d), ctypes.byref(i)),
+        "mhd_evolve": lambda: L.mhd_evolve(None, 1, ctypes.c_double(1e30), ctypes.byref(i)),
+        "mhd_set_inflow": lambda: L.mhd_set_inflow(None, None, None, ctypes.c_double(1.0)),
+        "mhd_get_time": lambda: L.mhd_get_time(None, ctypes.byref(d), ctypes.byref(i)),
+        "mhd_set_time": lambda: L.mhd_set_time(None, ctypes.c_double(0.0), 1),
+        "mhd_diagnostics": lambda: L.mhd_diagnostics(None, buf),
+        "mhd_synchronize": lambda: L.mhd_synchronize(None),
+        "mhd_set_stream": lambda: L.mhd_set_stream(None, None),
+        "mhd_last_error": lambda: L.mhd_last_error(None, ctypes.create_string_buffer(64), 64),
+        "mhd_reset_counters": lambda: L.mhd_reset_counters(None),
+        "mhd_surrogate_load": lambda: L.mhd_surrogate_load(None, None, ctypes.c_float(1e-3)),
+    }
+    bad = {k: r for k, r in ((k, f()) for k, f in calls.items()) if r != 1}
+    assert not bad, bad
+    assert L.mhd_destroy(None) == 0
