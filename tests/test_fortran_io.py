@@ -164,3 +164,13 @@ def test_reservoir_files_round_trip(tmp_path):
     assert (back[:, :, :2] == np.float32(1.25)).all() and (back[:, :, -2:] == np.float32(1.25)).all()
     np.testing.assert_array_equal(back[2:NZ + 2, 0, 2:NX + 2], back[2:NZ + 2, NY, 2:NX + 2])     # y wrap
     np.testing.assert_array_equal(back[NZ + 3, 2:NY + 2, 2:NX + 2], back[3, 2:NY + 2, 2:NX + 2])  # z wrap
+
+
+def test_io_errors_are_reported(tmp_path, state):
+    """A missing restart set and an unwritable output directory come back as
+    the I/O error code (-2, OSError here), not as a partial state."""
+    U, sp, _, phi = state
+    with pytest.raises(OSError):
+        fio.read_restart(str(tmp_path / "empty"), U.shape[1:], (1, 1, 1))
+    with pytest.raises(OSError):
+        fio.write_restart(str(tmp_path / "no" / "such" / "dir"), U, sp, phi, (1, 1, 1))
