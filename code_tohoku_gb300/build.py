@@ -1,7 +1,7 @@
 """Builds the CUDA library libmhd_gb300.so in-tree for sm_103a.
 
-Three translation units are compiled in parallel with nvcc and linked into
-one shared library next to this file:
+The translation units below are compiled in parallel with nvcc and linked
+into one shared library next to this file:
   csrc/mhd_fp64.cu  plain FP64 kernels, --fmad=false (bit-exact arithmetic)
   csrc/mhd_fp32.cu  FP32 reconstruction/flux kernels (contraction allowed, FP32
                     denormals flushed, approximate FP32 division and square root)

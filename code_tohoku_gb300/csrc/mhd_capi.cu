@@ -724,9 +724,19 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   // run; the first sweep waits for them.
   const bool late = h->p.ifchem != 2 && h->p.ifrad != 2;
   h->sh2_valid = false;
-  for (int q = 0; q < 8; q++) CKR(cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
-  for (int q = 0; q < (late ? 5 : 8); q++)
-    CKR(cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream));
+  {
+    // a failed enqueue waits for the copies already queued from U_in and
+    // species_in, so no copy from the caller's buffers outlives the call
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < 8 && e == cudaSuccess; q++)
+      e = cudaMemcpyAsync(f.U[q], U_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream);
+    for (int q = 0; q < (late ? 5 : 8) && e == cudaSuccess; q++)
+      e = cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(h->stream);
+      return fail(h, MHD_ERR_CUDA, "state copy: %s", cudaGetErrorString(e));
+    }
+  }
   if (late) {
     cudaError_t e = cudaEventRecord(h->ev_io[2], h->stream);   // after everything queued before (readers included)
     if (e == cudaSuccess) e = cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0);

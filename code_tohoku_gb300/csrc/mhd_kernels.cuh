@@ -1124,9 +1124,8 @@ __device__ __forceinline__ double ntot_imc(const Fields &f, long long a) {
 }
 
 // Couran (:1912-1930) and Stblty (:2784-2822) limits of interior cell t
-// (linear index over nx*ny*nz); c_min/s_min come in as tfinal.  The same
-// arithmetic as dt_kernel's per-cell part, for the allocation-free variant
-// in mhd_noalloc.cu.
+// (linear index over nx*ny*nz); c_min/s_min come in as tfinal.  dt_kernel
+// and the allocation-free variant in mhd_noalloc.cu both call it.
 __device__ __forceinline__ void cell_dt_limits(const Grid &g, const Phys &ph, const Fields &f, long long t,
                                                double &c_min, double &s_min) {
   int nx = g.n[0], ny = g.n[1];
@@ -1295,36 +1294,9 @@ __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned
 
 __global__ void dt_kernel(Grid g, Phys ph, Fields f, unsigned long long *out /* [0]=tCFL [1]=tLMT */, int *err) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   double c_min = ph.tfinal, s_min = ph.tfinal;
-  if (t < (long long)nx * ny * nz) {
-    int i, j, k;
-    split3(t, nx, ny, i, j, k);
-    i += 1; j += 1; k += 1;
-    long long a = gidx(g, i, j, k);
-    double H = f.sp[0][a], pr = f.sp[1][a], H2 = f.sp[2][a], He = f.sp[3][a], Hep = f.sp[4][a];
-    double gam = gam_of(H, pr, He, Hep, H2);
-    double bx = f.bcc[0][a], by = f.bcc[1][a], bz = f.bcc[2][a];
-    double rho = f.U[0][a], p5 = f.U[4][a];
-    double c2 = (gam * p5 + bx * bx + by * by + bz * bz) / rho;
-    double cs = sqrt(c2);
-    double dxi = g.dx[0][i + 1], dyj = g.dx[1][j + 1], dzk = g.dx[2][k + 1];
-    c_min = fmn(c_min, dxi / (cs + fabs(f.U[1][a])));
-    c_min = fmn(c_min, dyj / (cs + fabs(f.U[2][a])));
-    c_min = fmn(c_min, dzk / (cs + fabs(f.U[3][a])));
-    if (ph.ifthrm == 2) {
-      double Nn = pr + H + H2 + He + Hep;
-      double Tn = p5 / (ph.kb * Nn);
-      double dl = fmn(fmn(dxi, dyj), dzk);
-      double g1c = gmi1_of(H, pr, He, Hep, H2);
-      double alpha = g1c * ph.kcond * sqrt(fmn(Tn, 15.0));
-      alpha = 0.4 * Nn * ph.kb / alpha * (dl * dl);
-      double CooL = cool_of(ph, f, a, Tn);
-      double tauC = p5 / g1c / fabs(CooL);
-      tauC = fmx(0.2 * tauC, 2.5e-4);
-      s_min = fmn(s_min, tauC);
-      s_min = fmn(s_min, alpha);
-    }
+  if (t < (long long)g.n[0] * g.n[1] * g.n[2]) {
+    cell_dt_limits(g, ph, f, t, c_min, s_min);
     if (!(c_min > 0.0) || !(s_min > 0.0)) flag(err, ERRB_DT);
   }
   // reduce as bit patterns (values are positive)

@@ -117,6 +117,13 @@ extern "C" int mhd_timestep_noalloc(const mhd_params *p, const mhd_device_state 
   if (!p || !s || !dt || !st || !s->U || !s->species || !s->bcc || !s->dx || !s->dy || !s->dz)
     return MHD_ERR_ARG;
   if (p->nx < 1 || p->ny < 1 || p->nz < 1) return MHD_ERR_ARG;
+  if (p->precision != MHD_PREC_FP64 && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
+  if (p->ifchem != 0 && p->ifchem != 2) return MHD_ERR_ARG;
+  if (p->ifrad != 0 && p->ifrad != 2) return MHD_ERR_ARG;
+  // the species cooling reads the chemistry's electron and particle
+  // densities, and with ifrad = 2 SHIELD's columns too
+  if (p->ifchem == 2 && (!s->nde || !s->ndtot)) return MHD_ERR_ARG;
+  if (p->ifchem == 2 && p->ifrad == 2 && !s->columns) return MHD_ERR_ARG;
   long long ncells = (long long)p->nx * p->ny * p->nz;
   if (ncells > MHD_NOALLOC_MAX_CELLS) return MHD_ERR_TOO_LARGE;
   int prev = 0;
@@ -137,12 +144,19 @@ extern "C" int mhd_timestep_noalloc(const mhd_params *p, const mhd_device_state 
     g.dx[0] = s->dx; g.dx[1] = s->dy; g.dx[2] = s->dz;
     mhd::Phys ph{};
     ph.kb = p->kb; ph.kcond = p->kcond; ph.tfinal = p->tfinal; ph.ifthrm = p->ifthrm;
+    ph.ifchem = p->ifchem; ph.ifrad = p->ifrad;
     mhd::Fields f{};
     for (int q = 0; q < 8; q++) {
       f.U[q] = const_cast<double *>(s->U) + q * g.ncell;
       f.sp[q] = const_cast<double *>(s->species) + q * g.ncell;
     }
     for (int c = 0; c < 3; c++) f.bcc[c] = const_cast<double *>(s->bcc) + c * g.ncell;
+    if (p->ifchem == 2) {
+      f.nde = const_cast<double *>(s->nde);
+      f.ndtot = const_cast<double *>(s->ndtot);
+      if (p->ifrad == 2)
+        for (int q = 0; q < 10; q++) f.col[q] = const_cast<double *>(s->columns) + q * g.ncell;
+    }
     // the error word must start at zero; partials and results are overwritten
     if (cudaMemsetAsync(scratch + kErrWord, 0, sizeof(unsigned long long), sm) != cudaSuccess) { rc = MHD_ERR_CUDA; break; }
     int nblocks = (int)((ncells + kThreads - 1) / kThreads);

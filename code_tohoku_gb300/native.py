@@ -57,7 +57,8 @@ class _Diag(ctypes.Structure):
 class DeviceState(ctypes.Structure):
     """Device pointers (as integers) of arrays in the mhd_upload layout."""
     _fields_ = [("U", ctypes.c_void_p), ("species", ctypes.c_void_p), ("bcc", ctypes.c_void_p),
-                ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p), ("dz", ctypes.c_void_p)]
+                ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p), ("dz", ctypes.c_void_p),
+                ("nde", ctypes.c_void_p), ("ndtot", ctypes.c_void_p), ("columns", ctypes.c_void_p)]
 
 
 _lib = None
@@ -188,10 +189,10 @@ def surrogate_grad(params, x, y, device=0):
     return g, float(loss[0])
 
 
-def timestep_noalloc(params: MhdParams, dev_state: DeviceState, stream=None, device=0):
+def timestep_noalloc(params: MhdParams, dev_state: DeviceState, stream=None, device=0, precision=PREC_FP64):
     """mhd_timestep_noalloc: (dt, limiter) from device arrays the caller owns;
     no device memory is allocated by the library."""
-    ps = params_struct(params, device=device)
+    ps = params_struct(params, precision=precision, device=device)
     dt = ctypes.c_double()
     st = ctypes.c_int()
     r = load().mhd_timestep_noalloc(ctypes.byref(ps), ctypes.byref(dev_state), ctypes.byref(dt),

@@ -210,7 +210,13 @@ int mhd_surrogate_grad(const float *params, const float *x, const float *y, long
  * where new allocations are not allowed -- call this instead with device
  * pointers to arrays they already have, in the layout of mhd_upload: U
  * (8 blocks), species (8 blocks), Bcc (3 blocks, the cell-centred field of
- * CC(4)) and dx, dy, dz (n+4 each).  The result equals mhd_timestep's.
+ * CC(4)) and dx, dy, dz (n+4 each).  With p->ifchem == 2 the species
+ * cooling also reads the chemistry's electron and particle densities nde
+ * and ndtot (one block each, the module arrays of the same names), and
+ * with ifchem == 2 and ifrad == 2 SHIELD's ten column blocks (the layout of
+ * mhd_download_columns); a missing one gives MHD_ERR_ARG, and they are not
+ * read otherwise.  The result equals mhd_timestep's on a handle of
+ * precision MHD_PREC_FP64 holding the same arrays.
  *
  * The kernels' scratch is a fixed file-scope device array (about 1 MB) that
  * every GPU loading the library keeps until exit, so grids are limited to
@@ -225,6 +231,8 @@ int mhd_surrogate_grad(const float *params, const float *x, const float *y, long
 typedef struct mhd_device_state {
   const double *U, *species, *bcc;
   const double *dx, *dy, *dz;
+  const double *nde, *ndtot;     /* ifchem == 2 only, else may be NULL     */
+  const double *columns;         /* ifchem == 2 and ifrad == 2, else NULL  */
 } mhd_device_state;
 int mhd_timestep_noalloc(const mhd_params *p, const mhd_device_state *s, double *dt, int *st, void *stream);
 

@@ -1,5 +1,7 @@
 """Writes the golden fixtures under tests/golden/ from the reference's own
-output files (run once, in a checkout that has the reference mounted).
+output files (run once, in a checkout that has the reference mounted):
+
+    python tests/golden/make_fixtures.py <path of the reference checkout>
 
 Sources (files the reference ships next to the code that produced them):
   KIcool/cooling.dat   per-step trace of KIcool/1DMHDwCC3.f90 (:249, :277)
@@ -17,11 +19,13 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fixtures.py <path of the reference checkout>")
+    REF = sys.argv[1]
     ki = os.path.join(REF, "KIcool")
     trace = np.loadtxt(os.path.join(ki, "cooling.dat"))
     keep = np.r_[0:201, 201:len(trace):10, len(trace) - 1]
