@@ -26,9 +26,17 @@ in the stiff regime of the KI cooling (30x density, dt = 0.05), where the
 surrogate replaces the implicit bisection: FP64, FP32 exact and FP32 +
 surrogate from the same state, with the pressure error against FP64.
 
+`config2` is the 128^3 decaying Mach-5 MHD turbulence (periodic, plain FP64,
+100 steps at CFL 0.4) with its mass / momentum drift and max |div B|, and the
+chosen form beside it; `config5` is the 512^3 colliding flow (10 pc
+perturbation scale) in the chosen form with the trained surrogate, 100
+steps, with event times and HBM roofline fractions per phase of the step,
+next to the plain FP64 path at the same size.
+
 `--impl reference` times that CPU restatement alone (the reference itself is
 Fortran + MPI and no Fortran compiler exists on this machine; the restatement
-reproduces its golden outputs) on a 64^3 sample of the same workload.
+reproduces its golden outputs) on the same 256^3 problem: --warmup untimed
+and --steps timed full steps.
 """
 import argparse
 import json
@@ -42,6 +50,10 @@ sys.path.insert(0, ROOT)
 
 B_ALG_STEP = 552.0      # algorithmic bytes per zone-update of the whole step
 B_ALG_SWEEP = 104.0     # per sweep: read rho, v3, p, face-B3 (64) + write rho, v3, p (40)
+# algorithmic bytes per zone of each phase of the step (they add up to B_ALG_STEP)
+B_ALG_PHASE = {"timestep": 64.0, "source_1": 48.0, "sweep_x": 104.0, "sweep_y": 104.0, "sweep_z": 104.0,
+               "ct": 80.0, "source_2": 48.0, "dissip": 0.0}
+SWEEP_NAMES = ("sweep_x", "sweep_y", "sweep_z")
 
 
 def parse():
@@ -56,6 +68,8 @@ def parse():
     ap.add_argument("--no-stiff", action="store_true", help="skip the stiff-cooling SOURCE comparison")
     ap.add_argument("--l1-steps", type=int, default=100,
                     help="FP64 steps of the accuracy comparison (the chosen form runs to the same time)")
+    ap.add_argument("--no-config2", action="store_true", help="skip the 128^3 turbulence sub-run")
+    ap.add_argument("--no-config5", action="store_true", help="skip the 512^3 sub-run")
     ap.add_argument("--sur-steps", type=int, default=2000)
     ap.add_argument("--sur-data", type=int, default=1 << 24)
     return ap.parse_args()
@@ -77,16 +91,21 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per zone of one sweep launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "sweep_fp32_traffic.txt")
+def profile_value(fname, key):
+    """A `key=value` figure from a committed ncu summary under profiles/."""
+    path = os.path.join(ROOT, "profiles", fname)
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_zone_fp32_sweep="):
+            if line.startswith(key + "="):
                 return float(line.split("=")[1])
     except OSError:
         pass
     return None
+
+
+def ncu_traffic():
+    """DRAM bytes per zone of one sweep launch from the committed ncu summary."""
+    return profile_value("sweep_fp32_traffic.txt", "dram_bytes_per_zone_fp32_sweep")
 
 
 class ClockSampler:
@@ -157,9 +176,10 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n=64, steps=2):
-    """The oracle (C++ restatement, OpenMP over host cores) on a 64^3 sample
-    of the same workload: zone-updates/s."""
+def cpu_baseline(n=256, steps=2):
+    """The oracle (C++ restatement, OpenMP over host cores) on the same
+    256^3 problem, a bounded sample of 2 full steps after one untimed step:
+    zone-updates/s."""
     from code_tohoku_gb300 import problems
     from oracle.pyoracle import Oracle3D
     st = problems.colliding_flows(n)
@@ -172,7 +192,8 @@ def cpu_baseline(n=64, steps=2):
     el = time.perf_counter() - t
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     return {"value": n ** 3 * steps / el, "unit": "zone-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} steps of the {n}^3 colliding-flow problem (same physics, seed, box)"}
+            "sample": f"{steps} full steps of the {n}^3 colliding-flow problem (the headline workload), "
+                      "after one untimed step"}
 
 
 def run_reference(args, rank):
@@ -182,7 +203,7 @@ def run_reference(args, rank):
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     from code_tohoku_gb300 import problems
     from oracle.pyoracle import Oracle3D
-    n = 64
+    n = args.n
     st = problems.colliding_flows(n)
     o = Oracle3D(st.params)
     o.upload(st)
@@ -198,12 +219,13 @@ def run_reference(args, rank):
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "colliding WNM flows with KI cooling, 64^3 sample of the 256^3 problem",
+            "config": {"workload": f"colliding WNM flows with KI cooling, {n}^3, free x / periodic y,z",
                        "n": n, "precision": "fp64"},
             "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
                              "kind": "port",
-                             "sample": f"{args.steps} steps of the {n}^3 problem; C++ restatement of "
-                                       "MCF3DSGincfca3.f90 (no Fortran compiler on this machine)"},
+                             "sample": f"{args.steps} full steps of the {n}^3 problem after {args.warmup} "
+                                       "untimed ones; C++ restatement of MCF3DSGincfca3.f90 (no Fortran "
+                                       "compiler on this machine)"},
             "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -234,62 +256,94 @@ def main():
                                        seed=1, device=dev)
     sur_train_s = time.perf_counter() - t0
 
-    def make(prec, cooling=native.COOL_EXACT):
-        g = native.Mhd3D(st.params, precision=prec, cooling=cooling, device=dev)
+    def make(prec, cooling=native.COOL_EXACT, state=None):
+        state = st if state is None else state
+        g = native.Mhd3D(state.params, precision=prec, cooling=cooling, device=dev)
         g.set_stream(stream.cuda_stream)
         if cooling == native.COOL_SURROGATE:
             g.surrogate_load(sur_params, 1e-3)
-        g.upload(st)
+        g.upload(state)
         return g
 
     def barrier():
         replicas.barrier()
         torch.cuda.synchronize()
 
-    def step_timed(g, ev):
-        """One EVOLVE iteration through the C ABI, with events around the sweeps."""
-        dt, _ = g.timestep()
-        g.source(0.5 * dt)
+    def step_timed(g, rec, dissip):
+        """One EVOLVE iteration through the C ABI (the calls mhd_step makes),
+        with CUDA events on the handle's stream around every phase when rec
+        (phase -> list of event pairs) is given."""
+        def phase(name, fn, *a):
+            if rec is None:
+                return fn(*a)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = fn(*a)
+            e1.record(stream)
+            rec.setdefault(name, []).append((e0, e1))
+            return r
+        dt, _ = phase("timestep", g.timestep)
+        phase("source_1", g.source, 0.5 * dt)
         order = ((0, 1, 2), (1, 2, 0), (2, 0, 1), (0, 2, 1), (1, 0, 2), (2, 1, 0))[g.ifevo - 1]
         for d in order:
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            g.sweep(d, dt)
-            b.record(stream)
-            ev.append((a, b))
+            phase(SWEEP_NAMES[d], g.sweep, d, dt)
         g.ifevo = g.ifevo % 6 + 1
-        g.ct(dt)
-        g.source(0.5 * dt)
-        if st.params.dissip:
-            g.dissip()
+        phase("ct", g.ct, dt)
+        phase("source_2", g.source, 0.5 * dt)
+        if dissip:
+            phase("dissip", g.dissip)
         g.set_time(g.time + dt, g.ifevo)
         return dt
 
-    def timed_run(prec, cooling=native.COOL_EXACT):
-        g = make(prec, cooling)
+    def phase_ms(rec):
+        return {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in rec.items()}
+
+    def phase_roofline(pms, n3, hbm):
+        """Per phase: mean event time, algorithmic bytes / time, fraction of HBM."""
+        out = {}
+        for k, ms in pms.items():
+            gbs = B_ALG_PHASE[k] * n3 / (ms * 1e-3) / 1e9 if B_ALG_PHASE[k] else None
+            out[k] = {"ms": ms, "alg_bytes_per_zone": B_ALG_PHASE[k], "achieved_gbs": gbs,
+                      "frac_of_measured_hbm": gbs / hbm if gbs else None}
+        return out
+
+    def timed_run(prec, cooling=native.COOL_EXACT, state=None, steps=None, warmup=None, fresh=False):
+        """Warm-up steps, then `steps` timed steps; fresh: upload the initial
+        state again after the warm-up, so the timed steps are steps 1..steps
+        of the run."""
+        state = st if state is None else state
+        steps = args.steps if steps is None else steps
+        warmup = args.warmup if warmup is None else warmup
+        g = make(prec, cooling, state)
+        g.diag0 = g.diagnostics()
         g.ifevo = 1
-        for _ in range(args.warmup):
-            step_timed(g, [])
-        ev = []
+        for _ in range(warmup):
+            step_timed(g, None, state.params.dissip)
+        if fresh:
+            g.upload(state)
+            g.set_time(0.0, 1)
+            g.ifevo = 1
+        rec = {}
         barrier()
         launches0 = g.kernel_launches
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         with ClockSampler(dev) as clk:
             e0.record(stream)
-            for _ in range(args.steps):
-                step_timed(g, ev)
+            for _ in range(steps):
+                step_timed(g, rec, state.params.dissip)
             e1.record(stream)
             barrier()
         ms = e0.elapsed_time(e1)
-        sweep_ms = [a.elapsed_time(b) for a, b in ev]
         launches = g.kernel_launches - launches0
-        return g, ms, sweep_ms, launches, clk.summary()
+        return g, ms, phase_ms(rec), launches, clk.summary()
 
+    hbm, which = peaks()
     # chosen form: FP32 reconstruction/flux + FP64 accumulation + surrogate
-    g32, ms32, sw32, launches32, clocks = timed_run(native.PREC_FP32, native.COOL_SURROGATE)
+    g32, ms32, ph32, launches32, clocks = timed_run(native.PREC_FP32, native.COOL_SURROGATE)
     d32 = g32.diagnostics()
+    sw32 = [ph32[k] for k in SWEEP_NAMES]
     ms32 = replicas.max_over_ranks(ms32)
     value = world * n3 * args.steps / (ms32 * 1e-3)
     # ablation: the same FP32 form with the exact cooling integrator
@@ -297,13 +351,28 @@ def main():
     dx_ = gx.diagnostics()
     del gx
 
+    # the FP64 pipe of this GPU, measured: the plain form's roofline
+    fp64_peak = native.fp64_peak(dev)
+
     # plain FP64 form, same workload
     fp64 = None
     l1 = None
     if not args.no_fp64:
-        g64, ms64, sw64, launches64, _ = timed_run(native.PREC_FP64)
+        g64, ms64, ph64, launches64, _ = timed_run(native.PREC_FP64)
+        sweep64 = sum(ph64[k] for k in SWEEP_NAMES) / 3
         fp64 = {"value": n3 * args.steps / (ms64 * 1e-3), "unit": "zone-updates/s",
-                "ms_per_step": ms64 / args.steps, "sweep_ms": sum(sw64) / len(sw64)}
+                "ms_per_step": ms64 / args.steps, "sweep_ms": sweep64, "phase_ms": ph64}
+        # FP64 operations per zone of one plain sweep launch (ncu instruction
+        # counts: 2 per DFMA, 1 per DADD / DMUL), against the measured FMA rate
+        fl = profile_value("sweep_fp64_pipe.txt", "fp64_flops_per_zone_fp64_sweep")
+        pipe = profile_value("sweep_fp64_pipe.txt", "fp64_pipe_active_pct")
+        if fl:
+            ach = fl * n3 / (sweep64 * 1e-3) / 1e9
+            fp64["roofline"] = {"bound": "fp64 pipe", "kernel": "sweep_kernel<DIR, P, double>",
+                                "achieved": ach, "peak": fp64_peak["fma_gflops"], "unit": "GFLOP/s",
+                                "frac": ach / fp64_peak["fma_gflops"], "flops_per_zone": fl,
+                                "peak_source": "mhd_fp64_peak (measured in this run: dependent FMA chains)",
+                                "ncu_fp64_pipe_active_pct": pipe}
         # L1 error of the chosen form against FP64 at the same physical time:
         # FP64 runs --l1-steps steps in all, the chosen form runs to that
         # time (each form takes its own dt, like a run; the last step of the
@@ -411,9 +480,87 @@ def main():
             stiff["fp32_surrogate"]["fallback_cells"] /
             max(1, stiff["fp32_surrogate"]["fallback_cells"] + stiff["fp32_surrogate"]["surrogate_cells"]))
 
+    def drift(d0, d1, scale):
+        """Mass and momentum change over a run; momentum relative to the sum
+        of rho |v| dV of the initial state."""
+        return {"mass_rel": (d1["mass"] - d0["mass"]) / d0["mass"],
+                "momentum_rel": [(b - a) / scale for a, b in zip(d0["momentum"], d1["momentum"])],
+                "divb_max": d1["divb_max"]}
+
+    def rho_absv(state):
+        c = (slice(2, -2),) * 3
+        dV = float(state.dx[2] * state.dy[2] * state.dz[2])
+        return sum(float((state.U[0][c] * np.abs(state.U[q][c])).sum()) for q in (1, 2, 3)) * dV
+
+    # config 2: 128^3 decaying Mach-5 MHD turbulence, plain FP64, steps 1..100
+    # at CFL 0.4 (the timed steps start from the initial state), and the
+    # chosen form over the same steps; L1 at the FP64 run's final time
+    config2 = None
+    if not args.no_config2:
+        t2 = problems.turbulence(128)
+        n2 = 128 ** 3
+        g2, ms2, ph2, _, _ = timed_run(native.PREC_FP64, state=t2, steps=100, warmup=args.warmup, fresh=True)
+        gc, msc, phc, _, _ = timed_run(native.PREC_FP32, state=t2, steps=100, warmup=args.warmup, fresh=True)
+        sc2 = rho_absv(t2)
+        d64, dc = g2.diagnostics(), gc.diagnostics()
+        t_end = g2.time
+        gc.evolve(20, tsave=t_end)
+        Uc, _, bc_ = gc.download()
+        U6, _, b6 = g2.download()
+        c = (slice(2, -2),) * 3
+
+        def l1r(a, b):
+            return float(np.abs(a - b).mean() / np.abs(b).mean())
+        config2 = {"workload": "decaying MHD turbulence 128^3, periodic, rms Mach 5, beta 1, k^-4 on |k| = 1..8 "
+                               "(ran0 seed 1), CFL 0.4, no cooling, DISSIP off",
+                   "steps": 100, "steps_start_from": "t = 0 (a fresh upload after the warm-up)",
+                   "plain_fp64": {"value": n2 * 100 / (ms2 * 1e-3), "unit": "zone-updates/s",
+                                  "ms_per_step": ms2 / 100, "phase_ms": ph2, "time": t_end,
+                                  "conservation": drift(g2.diag0, d64, sc2)},
+                   "chosen_form": {"value": n2 * 100 / (msc * 1e-3), "unit": "zone-updates/s",
+                                   "ms_per_step": msc / 100, "phase_ms": phc,
+                                   "conservation": drift(gc.diag0, dc, sc2),
+                                   "l1_vs_fp64_at_same_time": {"rho": l1r(Uc[0][c], U6[0][c]),
+                                                               "p": l1r(Uc[4][c], U6[4][c]),
+                                                               "B": l1r(bc_[(slice(None),) + c], b6[(slice(None),) + c]),
+                                                               "time": gc.time}},
+                   "momentum_note": "the reference's MOC limiter reads the energy-based T inside a pencil and "
+                                    "the pre-sweep pressure in its ghosts, so at Mach 5 a periodic interface "
+                                    "can get two different slopes; the drift is the reference's own (the FP64 "
+                                    "path equals the oracle bit for bit)"}
+        del g2, gc
+
+    # config 5: the 512^3 colliding flow (10 pc perturbation scale) in the
+    # chosen form with the trained surrogate, steps 1..100 with event times
+    # per phase, and the plain FP64 path at the same size (3 steps)
+    config5 = None
+    if not args.no_config5:
+        st5 = problems.colliding_flows(512, pert_scale=10.0)
+        n5 = 512 ** 3
+        g5, ms5, ph5, launches5, clk5 = timed_run(native.PREC_FP32, native.COOL_SURROGATE, state=st5, steps=100,
+                                                 warmup=args.warmup, fresh=True)
+        d5 = g5.diagnostics()
+        d50 = g5.diag0
+        del g5
+        g5b, ms5b, ph5b, _, _ = timed_run(native.PREC_FP64, state=st5, steps=3, warmup=1)
+        del g5b
+        config5 = {"workload": "colliding WNM flows with KI cooling, 512^3, 20 pc box, 10 pc perturbation scale, "
+                               "free x / periodic y,z",
+                   "chosen_form": {"value": n5 * 100 / (ms5 * 1e-3), "unit": "zone-updates/s", "steps": 100,
+                                   "ms_per_step": ms5 / 100, "gpu_launches": launches5, "clocks": clk5,
+                                   "phases": phase_roofline(ph5, n5, hbm),
+                                   "step_frac_of_measured_hbm": B_ALG_STEP * n5 * 100 / (ms5 * 1e-3) / 1e9 / hbm,
+                                   "surrogate_cells": d5["surrogate_cells"], "fallback_cells": d5["fallback_cells"],
+                                   "imc_cells": d5["imc_cells"], "divb_max": d5["divb_max"],
+                                   "mass_change_rel": (d5["mass"] - d50["mass"]) / d50["mass"]},
+                   "plain_fp64": {"value": n5 * 3 / (ms5b * 1e-3), "unit": "zone-updates/s", "steps": 3,
+                                  "ms_per_step": ms5b / 3, "phases": phase_roofline(ph5b, n5, hbm)},
+                   "resident_gb": {"fp64_state_and_scratch": 28 * 8 * 516 ** 3 / 1e9,
+                                   "fp32_scratch": 15 * 4 * 516 ** 3 / 1e9}}
+        config5["speedup_vs_fp64"] = config5["chosen_form"]["value"] / config5["plain_fp64"]["value"]
+
     if rank != 0:
         return
-    hbm, which = peaks()
     sweep_ms = sum(sw32) / len(sw32)
     achieved = B_ALG_SWEEP * n3 / (sweep_ms * 1e-3) / 1e9
     tr = ncu_traffic()
@@ -440,7 +587,11 @@ def main():
                           "imc_cells": d32["imc_cells"],
                           "fallback_fraction": (d32["fallback_cells"] / max(1, d32["fallback_cells"] + d32["surrogate_cells"]))},
             "step_zone_updates_roof": hbm * 1e9 / B_ALG_STEP,
-            "e2e": e2e, "gpu_launches": launches32, "roofline": roof, "clocks": clocks}
+            "e2e": e2e, "gpu_launches": launches32, "roofline": roof, "clocks": clocks,
+            "phases": phase_roofline(ph32, n3, hbm), "fp64_peak_measured": fp64_peak,
+            "diagnostics": {"divb_max": d32["divb_max"], "mass_change_rel": (d32["mass"] - g32.diag0["mass"]) / g32.diag0["mass"],
+                            "note": "x boundaries are open (free), so mass changes by the boundary flux"},
+            "config2": config2, "config5": config5}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)

@@ -9,6 +9,7 @@ into one shared library next to this file:
   csrc/mhd_surrogate.cu  surrogate data, training and evaluation kernels
                     (--fmad=false: its FP64 labels match the CPU IMC bit for bit)
   csrc/mhd_noalloc.cu  the allocation-free time step
+  csrc/mhd_peak.cu  the FP64 throughput measurement (the plain path's roofline)
   csrc/mhd_io.cpp   host code: the reference's output and restart files
 """
 import os
@@ -29,6 +30,7 @@ UNITS = {
     "mhd_capi.cu": ["--fmad=false"],
     "mhd_surrogate.cu": ["--fmad=false"],
     "mhd_noalloc.cu": ["--fmad=false"],
+    "mhd_peak.cu": [],
     "mhd_io.cpp": [],
 }
 

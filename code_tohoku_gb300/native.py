@@ -28,7 +28,7 @@ EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_times
            "mhd_set_time", "mhd_set_inflow", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
            "mhd_kernel_launches", "mhd_reset_counters", "mhd_surrogate_nparams", "mhd_surrogate_load",
            "mhd_surrogate_train", "mhd_surrogate_label", "mhd_surrogate_eval", "mhd_surrogate_grad",
-           "mhd_timestep_noalloc")
+           "mhd_timestep_noalloc", "mhd_fp64_peak")
 
 
 class MhdError(RuntimeError):
@@ -133,6 +133,8 @@ def load(build_if_missing=True):
     L.mhd_timestep_noalloc.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(DeviceState), _P,
                                        ctypes.POINTER(ctypes.c_int), ctypes.c_void_p]
     L.mhd_timestep_noalloc.restype = ctypes.c_int
+    L.mhd_fp64_peak.argtypes = [ctypes.c_int, _P, _P, _P]
+    L.mhd_fp64_peak.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -199,6 +201,14 @@ def timestep_noalloc(params: MhdParams, dev_state: DeviceState, stream=None, dev
                                     ctypes.byref(st), ctypes.c_void_p(stream) if stream else None)
     _sck(r, "mhd_timestep_noalloc")
     return dt.value, st.value
+
+
+def fp64_peak(device=0):
+    """mhd_fp64_peak: measured FP64 FMA GFLOP/s, divisions and square roots
+    in billions per second."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _sck(load().mhd_fp64_peak(device, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "mhd_fp64_peak")
+    return {"fma_gflops": a.value, "div_per_ns": b.value, "sqrt_per_ns": c.value}
 
 
 def params_struct(p: MhdParams, precision=PREC_FP64, cooling=COOL_EXACT, device=0):

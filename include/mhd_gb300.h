@@ -202,6 +202,14 @@ int mhd_surrogate_eval(const float *params, const float *x, float *out, long lon
 int mhd_surrogate_grad(const float *params, const float *x, const float *y, long long n, float *grad,
                        float *loss, int device);
 
+/* ---- Device measurement (no counterpart in the reference) ----
+ * Measured FP64 throughput of one device: fused multiply-adds (GFLOP/s, two
+ * per FMA), divisions and square roots (billions per second), each from
+ * eight independent dependent chains per thread, timed with CUDA events.
+ * The plain FP64 form is bound by this pipe, not by HBM; bench.py quotes its
+ * roofline against these numbers. */
+int mhd_fp64_peak(int device, double *fma_gflops, double *div_gps, double *sqrt_gps);
+
 /* ---- Time-step limits without device allocation ----
  * No counterpart in the reference (which has no device memory at all).
  * mhd_timestep needs a handle, and a handle allocates its state with

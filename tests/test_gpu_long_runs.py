@@ -1,7 +1,7 @@
 """Long runs of the plain FP64 path against the oracle, bit for bit: the
 required agreement is 1e-12 relative per cell after 100 steps; these hold every
 interior value identical after 100 steps of the decaying turbulence and of
-the KI colliding flows, and after 50 steps of the shipped deck's setup
+the KI colliding flows (and of the turbulence at 64^3), and after 50 steps of the shipped deck's setup
 (inflow boundaries, chemistry network and species cooling), at sizes the
 oracle runs in seconds."""
 import pytest
@@ -22,6 +22,15 @@ def run(g, o, steps):
 
 def test_turbulence_100_steps_bit_exact():
     g, o = pair(problems.turbulence(24, kmax=6))
+    run(g, o, 100)
+    compare(g, o)
+
+
+def test_config2_turbulence_64_cubed_100_steps_bit_exact():
+    """The decaying Mach-5 MHD turbulence workload (k^-4 on |k| = 1..8, ran0
+    seed 1, beta 1, CFL 0.4) at 64^3: steps 1..100 bit for bit, the time
+    step of every step included."""
+    g, o = pair(problems.turbulence(64))
     run(g, o, 100)
     compare(g, o)
 
