@@ -50,6 +50,10 @@ struct mhd_handle {
   float *rn32 = nullptr, *sw32 = nullptr;
   float *emf32[3] = {nullptr, nullptr, nullptr};
   float *coordsf = nullptr;
+  // chosen form's time step: per-warp lower ends of the FP32 screen and
+  // its four words (smallest upper ends, floor flag)
+  float *dtlo = nullptr;
+  unsigned *dtwords = nullptr;
   float *dtf = nullptr;                  // BC=4 reservoir (device)
   bool inflow_set = false;
   double *divv = nullptr;
@@ -258,6 +262,13 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
       mhd_destroy(h);
       return MHD_ERR_CUDA;
     }
+    const size_t nw = (size_t)dt_screen_warps(g);
+    if (cudaMalloc(&h->dtlo, (3 * nw + 4) * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      mhd_destroy(h);
+      return MHD_ERR_CUDA;
+    }
+    h->dtwords = reinterpret_cast<unsigned *>(h->dtlo + 3 * nw);
     float *fq = h->fblock;
     h->temp32 = fq; fq += g.ncell;
     h->sh2_32 = fq; fq += 2 * g.ncell;
@@ -299,6 +310,7 @@ int mhd_destroy(mhd_handle *h) {
   cudaFree(h->divv);
   cudaFree(h->diag_part);
   cudaFree(h->dtred);
+  cudaFree(h->dtlo);
   cudaFree(h->err);
   cudaFree(h->sur_master);
   cudaFree(h->sur_net);
@@ -423,16 +435,35 @@ int mhd_timestep(mhd_handle *h, double *dt, int *st) {
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
   CKR(cudaMemsetAsync(h->dtred, 0xff, 2 * sizeof(unsigned long long), h->stream));
-  // the time step reads S and H2 of the interior cells from SOURCE's
-  // arrays while the species are unchanged since (the same floats)
-  if (h->p.precision == MHD_PREC_FP32)
-    CK(dt_reduce_fp32(h->g, h->ph, h->f, h->sh2_valid ? h->sh2_32 : nullptr, h->dtred, h->err, h->stream));
-  else CK(dt_reduce(h->g, h->ph, h->f, h->dtred, h->err, h->stream));
+  const bool fp32 = h->p.precision == MHD_PREC_FP32;
+  if (fp32) {
+    // an FP32 screen of every cell, then the FP64 limits of the cells that
+    // can hold the minimum: the same dt as the plain form, bit for bit.  The
+    // screen reads S and H2 of the interior cells from SOURCE's arrays while
+    // the species are unchanged since (the same floats).
+    CKR(cudaMemsetAsync(h->dtwords, 0xff, 3 * sizeof(unsigned), h->stream));
+    CKR(cudaMemsetAsync(h->dtwords + 3, 0, sizeof(unsigned), h->stream));
+    CK(dt_screen_fp32(h->g, h->ph, h->f, h->sh2_valid ? h->sh2_32 : nullptr, h->dtlo, h->dtwords, h->err,
+                      h->stream));
+    CK(dt_refine(h->g, h->ph, h->f, h->dtlo, h->dtwords, h->dtred, h->stream));
+    CKR(cudaMemcpyAsync(h->h_small + 6, h->dtwords + 3, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+  } else {
+    CK(dt_reduce(h->g, h->ph, h->f, h->dtred, h->err, h->stream));
+  }
   CKR(cudaMemcpyAsync(h->h_small, h->dtred, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
   TRY(check_err(h));
   double tcfl, tlmt;
   memcpy(&tcfl, &h->h_small[0], sizeof(double));
   memcpy(&tlmt, &h->h_small[1], sizeof(double));
+  if (fp32) {
+    // a limit no screened cell reached keeps its starting value, tfinal; a
+    // cooling time at its floor is 2.5e-4 exactly (Stblty :2806)
+    if (h->h_small[0] == ~0ull) tcfl = h->p.tfinal;
+    if (h->h_small[1] == ~0ull) tlmt = h->p.tfinal;
+    unsigned floored;
+    memcpy(&floored, &h->h_small[6], sizeof floored);
+    if (floored && h->p.ifthrm == 2 && 2.5e-4 < tlmt) tlmt = 2.5e-4;
+  }
   // EVOLVE:569-596 with one rank
   double d = h->p.tfinal;
   double c = h->p.cfl * tcfl;

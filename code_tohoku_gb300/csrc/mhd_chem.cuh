@@ -82,7 +82,7 @@ __device__ __forceinline__ R shield_tau_source(R pr, R kb, const CellSpecies<R> 
 // and CO cooling minus photo-electric, cosmic-ray and photo-destruction
 // heating, T in 1e3 K
 template <class R>
-__device__ __forceinline__ R fcool_species(R T, const CellSpecies<R> &c) {
+__device__ __forceinline__ R fcool_species(R T, const CellSpecies<R> &c, R *mag = nullptr) {
   const R G0 = R(1), xo = R(3.2e-4), dv = R(2);
   const R Ntot1 = c.col[COL_NTOT1], Ntot2 = c.col[COL_NTOT2], NH21 = c.col[COL_NH21], NH22 = c.col[COL_NH22];
   const R NCO1 = c.col[COL_NCO1], NCO2 = c.col[COL_NCO2], tC1 = c.col[COL_TC1], tC2 = c.col[COL_TC2];
@@ -122,6 +122,9 @@ __device__ __forceinline__ R fcool_species(R T, const CellSpecies<R> &c) {
   R SHLD1 = R(0.965) / (s1 * s1) + R(0.035) / dsq(R(1) + x1) * mexp(R(-8.5e-4) * dsq(R(1) + x1));
   R SHLD2 = R(0.965) / (s2 * s2) + R(0.035) / dsq(R(1) + x2) * mexp(R(-8.5e-4) * dsq(R(1) + x2));
   R Gampd = c.H2 * R(4.16362e4) * G0 * ATN2 * (SHLD1 + SHLD2) * R(0.5);
+  // mag: the sum of the magnitudes of the terms, which bounds the rounding
+  // error of the difference (the chosen form's time-step screen)
+  if (mag) *mag = Laml + Lamc + Lamo + Lamd + LCOr + LCOH + LCOH2 + Gampe + Gamcr + Gampd;
   return Laml + Lamc + Lamo + Lamd + LCOr + LCOH + LCOH2 - Gampe - Gamcr - Gampd;
 }
 

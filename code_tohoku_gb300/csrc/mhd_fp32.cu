@@ -122,12 +122,17 @@ cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s) {
   if (dir == 1) return launch32_d<1>(a, s);
   return launch32_d<2>(a, s);
 }
-cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, unsigned long long *out,
-                           int *err, cudaStream_t s) {
+int dt_screen_warps(const Grid &g) {
+  const long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+  return (int)((n + 31) / 32);
+}
+cudaError_t dt_screen_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, float *lo,
+                           unsigned *words, int *err, cudaStream_t s) {
   long long n = (long long)g.n[0] * g.n[1] * g.n[2];
   // a thread per cell: with a capped grid of 4864 blocks (~13 cells per
   // thread, 50x fewer atomics) the 256^3 kernel took 385 us against 333-358
-  dt32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, sh2, out, err);
+  DtScreen sc{lo, words, dt_screen_warps(g)};
+  dt32_screen_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, sh2, sc, err);
   return cudaGetLastError();
 }
 

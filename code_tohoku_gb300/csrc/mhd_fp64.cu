@@ -101,6 +101,13 @@ cudaError_t dt_reduce(const Grid &g, const Phys &ph, const Fields &f, unsigned l
   return cudaGetLastError();
 }
 
+cudaError_t dt_refine(const Grid &g, const Phys &ph, const Fields &f, const float *lo, const unsigned *words,
+                      unsigned long long *out, cudaStream_t s) {
+  long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+  dt_refine_kernel<<<nblk(n, 256), 256, 0, s>>>(g, ph, f, lo, words, (int)((n + 31) / 32), out);
+  return cudaGetLastError();
+}
+
 cudaError_t divv(const Grid &g, const Fields &f, double *d, cudaStream_t s) {
   long long n = 2LL * 12 * (g.n[1] + 2) * (g.n[2] + 2);
   divv_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f, d);

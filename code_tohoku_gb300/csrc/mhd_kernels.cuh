@@ -1070,6 +1070,17 @@ __device__ __forceinline__ float fcool_ki(float T, float NN) {
   return (NN * NN * (Laml + Lamc) - NN) * 3.94656e1f;
 }
 
+// the KI form in FP32 with the sum of the magnitudes of its cooling and
+// heating terms (mag), which bounds the rounding error of their difference
+__device__ __forceinline__ float fcool_ki_mag(float T, float NN, float &mag) {
+  float Laml = 1.0e7f * __expf(-1.184e5f / (T * 1.0e3f + 1.0e3f));
+  Laml = fmn(Laml, 5.e3f);
+  float Lamc = 1.4e-2f * sqrtf(T * 1.0e3f) * __expf(-9.2e1f / (T * 1.0e3f));
+  const float A = NN * NN * (Laml + Lamc);
+  mag = (A + NN) * 3.94656e1f;
+  return (A - NN) * 3.94656e1f;
+}
+
 // the cooling function of the run at temperature T of cell a: the KI form
 // (NN = rho/1.27) or, with ifchem = 2, the species form
 __device__ __forceinline__ double cool_of(const Phys &ph, const Fields &f, long long a, double T) {
@@ -1325,6 +1336,40 @@ __global__ void dt_kernel(Grid g, Phys ph, Fields f, unsigned long long *out /* 
       atomicMin(&out[0], cb);
       atomicMin(&out[1], sb);
     }
+  }
+}
+
+// The chosen form's time step, second kernel: the warps whose FP32 interval
+// (dt32_screen_kernel) reaches the smallest upper end of a limit recompute
+// their cells with cell_dt_limits -- dt_kernel's FP64 arithmetic -- and
+// reduce like dt_kernel.  Every other cell's FP64 limits are surely larger
+// than some cell's, so the result is dt_kernel's bit for bit.  lo: [3][nwarps]
+// lower ends (c, tau, alpha); words[0..2]: smallest upper ends as float bits,
+// words[3]: some cooling time is at its floor, whose FP64 value the host adds.
+__global__ void __launch_bounds__(256) dt_refine_kernel(Grid g, Phys ph, Fields f, const float *lo,
+                                                        const unsigned *words, int nwarps,
+                                                        unsigned long long *out /* [0]=tCFL [1]=tLMT */) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long w = t >> 5;
+  if (w >= nwarps) return;   // whole warps
+  bool cand = lo[w] <= __uint_as_float(words[0]);
+  if (ph.ifthrm == 2) {
+    cand = cand || lo[2 * nwarps + w] <= __uint_as_float(words[2]);
+    if (!words[3]) cand = cand || lo[nwarps + w] <= __uint_as_float(words[1]);
+  }
+  if (!cand) return;         // the same for every lane of the warp
+  double c_min = ph.tfinal, s_min = ph.tfinal;
+  if (t < (long long)g.n[0] * g.n[1] * g.n[2]) cell_dt_limits(g, ph, f, t, c_min, s_min);
+  unsigned long long cb = dbits(c_min > 0.0 ? c_min : 0.0), sb = dbits(s_min > 0.0 ? s_min : 0.0);
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long c2 = __shfl_xor_sync(0xffffffffu, cb, o);
+    unsigned long long s2 = __shfl_xor_sync(0xffffffffu, sb, o);
+    cb = c2 < cb ? c2 : cb;
+    sb = s2 < sb ? s2 : sb;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&out[0], cb);
+    atomicMin(&out[1], sb);
   }
 }
 

@@ -24,10 +24,14 @@ cudaError_t source_fp32(const Source32Args &a, cudaStream_t s);
 // (and store S = H+p+He+He+ and H2 in sh2, 2 ncell floats), else from them
 cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *sh2,
                       bool from_species, cudaStream_t s);
-// sh2: S and H2 of every cell (SOURCE's arrays) when they are current, or
-// null to form them from the species
-cudaError_t dt_reduce_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, unsigned long long *out,
-                           int *err, cudaStream_t s);
+// The chosen form's time step, first kernel (FP32 screen, see
+// dt32_screen_kernel): lo gets 3 * nwarps lower ends, words[0..2] the
+// smallest upper ends (start them at 0xffffffff) and words[3] the floor
+// flag (start at 0).  sh2: S and H2 of every cell (SOURCE's arrays) when
+// they are current, or null to form them from the species.
+int dt_screen_warps(const Grid &g);
+cudaError_t dt_screen_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, float *lo,
+                           unsigned *words, int *err, cudaStream_t s);
 cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
 cudaError_t ct_prep_fp32(const Grid &g, const Fields &f, double *const vf[3], double kb, const CT32Args &a,
                          cudaStream_t s);
@@ -56,6 +60,10 @@ cudaError_t shield_scan(const Grid &g, const Fields &f, const double *tau, doubl
 cudaError_t chem_step_fp32(const Grid &g, const Phys &ph, const Fields &f, double dt, int *err, cudaStream_t s);
 cudaError_t dt_reduce(const Grid &g, const Phys &ph, const Fields &f, unsigned long long *out, int *err,
                       cudaStream_t s);
+// second kernel of the chosen form's time step: the FP64 limits of the
+// screened candidates, reduced into out like dt_reduce (start at ~0)
+cudaError_t dt_refine(const Grid &g, const Phys &ph, const Fields &f, const float *lo, const unsigned *words,
+                      unsigned long long *out, cudaStream_t s);
 cudaError_t divv(const Grid &g, const Fields &f, double *d, cudaStream_t s);
 cudaError_t dissip(const Grid &g, const Fields &f, const double *d, int e, cudaStream_t s);
 cudaError_t diag(const Grid &g, const Phys &ph, const Fields &f, double *part, int *nblocks, cudaStream_t s);

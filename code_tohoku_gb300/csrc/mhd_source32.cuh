@@ -322,16 +322,40 @@ __global__ void __launch_bounds__(128) source32_stiff_kernel(Source32Args A) {
   }
 }
 
-// dt for the chosen form: the Courant limit (:1912-1930) and the thermal
-// limit of Stblty (:2784-2822) in FP32; the per-cell minima are widened to
-// FP64 bit patterns for the same order-independent atomicMin reduction.
-// Grid-stride loop over the cells (the launch uses a thread per cell).
-__global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, const float *sh2, unsigned long long *out,
-                                                   int *err) {
-  int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  float c_min = d2f(ph.tfinal), s_min = c_min;
-  const long long ncells = (long long)nx * ny * nz, stride = (long long)gridDim.x * blockDim.x;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ncells; t += stride) {
+// dt for the chosen form, first of two kernels: an FP32 screen of every
+// cell.  The chosen form takes the same time step as the plain FP64 form
+// (the CFL minimum stays FP64): this kernel computes the Courant limit
+// (:1912-1930) and the two thermal limits of Stblty (:2784-2822) of each
+// cell in FP32 together with an interval that surely holds the FP64 value,
+// [v (1 - eta), v (1 + eta)] with eta = 2^-10, far wider than the FP32
+// rounding of these products, sums and quotients of positive terms; the
+// cooling time divides by |Lambda|, a difference of cooling and heating, so
+// its interval widens |Lambda| by 2^-8 of the sum of the terms' magnitudes
+// (and is unbounded above where that covers 0).  The floor 2.5e-4 of the
+// cooling time is exact: a cell whose interval lies below it has the floor
+// as its FP64 value.  Each warp stores the lower ends of its three limits;
+// the block minima of the upper ends go to words[0..2] (non-negative floats
+// order like their bit patterns) and words[3] records a floored cell.
+// dt_refine_kernel then recomputes in FP64 only the warps whose lower ends
+// reach the smallest upper end -- the only cells that can hold the minimum.
+struct DtScreen {
+  float *lo;          // [3][nwarps]: per warp, the smallest lower end of c, tau, alpha
+  unsigned *words;    // [0..2] smallest upper ends (float bits), [3] a cooling time at the floor
+  int nwarps;
+};
+constexpr float kDtEta = 1.0f / 1024.0f;
+constexpr float kDtEtaCool = 1.0f / 256.0f;
+
+__global__ void __launch_bounds__(256) dt32_screen_kernel(Grid g, Phys ph, Fields f, const float *sh2, DtScreen sc,
+                                                          int *err) {
+  const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  const long long ncells = (long long)nx * ny * nz;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const float INF = __int_as_float(0x7f800000);
+  const float dn = 1.0f - kDtEta, up = 1.0f + kDtEta;
+  float lo[3] = {INF, INF, INF}, hi[3] = {INF, INF, INF};   // c, tau, alpha
+  bool floored = false;
+  if (t < ncells) {
     int i, j, k;
     split3(t, nx, ny, i, j, k);
     i += 1; j += 1; k += 1;
@@ -345,48 +369,66 @@ __global__ void __launch_bounds__(256) dt32_kernel(Grid g, Phys ph, Fields f, co
       S = d2f(f.sp[0][a]) + d2f(f.sp[1][a]) + d2f(f.sp[3][a]) + d2f(f.sp[4][a]);
       H2 = d2f(f.sp[2][a]);
     }
-    float rg = __fdividef(1.0f, 3.0f * S + 5.0f * H2);
+    float rg = __fdiv_rn(1.0f, 3.0f * S + 5.0f * H2);
     float gam = (5.0f * S + 7.0f * H2) * rg;
     float bx = d2f(f.bcc[0][a]), by = d2f(f.bcc[1][a]), bz = d2f(f.bcc[2][a]);
     float rho = d2f(f.U[0][a]), p5 = d2f(f.U[4][a]);
-    float cs = sqrtf(__fdividef(gam * p5 + bx * bx + by * by + bz * bz, rho));
+    float cs = sqrtf(__fdiv_rn(gam * p5 + bx * bx + by * by + bz * bz, rho));
     float dxi = g.dxf[0][i + 1], dyj = g.dxf[1][j + 1], dzk = g.dxf[2][k + 1];
-    c_min = fminf(c_min, __fdividef(dxi, cs + fabsf(d2f(f.U[1][a]))));
-    c_min = fminf(c_min, __fdividef(dyj, cs + fabsf(d2f(f.U[2][a]))));
-    c_min = fminf(c_min, __fdividef(dzk, cs + fabsf(d2f(f.U[3][a]))));
+    float c = fminf(fminf(__fdiv_rn(dxi, cs + fabsf(d2f(f.U[1][a]))), __fdiv_rn(dyj, cs + fabsf(d2f(f.U[2][a])))),
+                    __fdiv_rn(dzk, cs + fabsf(d2f(f.U[3][a]))));
+    lo[0] = c * dn;
+    hi[0] = c * up;
+    bool bad = !(c > 0.0f);
     if (ph.ifthrm == 2) {
       float Nn = S + H2;
       const float kb = d2f(ph.kb);
-      float Tn = __fdividef(p5, kb * Nn);
+      float Tn = __fdiv_rn(p5, kb * Nn);
       float dl = fminf(fminf(dxi, dyj), dzk);
       float g1c = (2.0f * S + 2.0f * H2) * rg;
-      float alpha = __fdividef(0.4f * Nn * kb, g1c * d2f(ph.kcond) * sqrtf(fminf(Tn, 15.0f))) * (dl * dl);
+      float alpha = __fdiv_rn(0.4f * Nn * kb, g1c * d2f(ph.kcond) * sqrtf(fminf(Tn, 15.0f))) * (dl * dl);
+      lo[2] = alpha * dn;
+      hi[2] = alpha * up;
+      float mag;
       float CooL = (ph.ifchem == 2)
-                       ? fcool_species<float>(Tn, cell_species<float>(f, a, [](double v) { return d2f(v); }))
-                       : fcool_ki(Tn, rho * (1.0f / 1.27f));
-      float tauC = fmaxf(__fdividef(0.2f * p5, g1c * fabsf(CooL)), 2.5e-4f);
-      s_min = fminf(s_min, fminf(tauC, alpha));
+                       ? fcool_species<float>(Tn, cell_species<float>(f, a, [](double v) { return d2f(v); }), &mag)
+                       : fcool_ki_mag(Tn, rho * (1.0f / 1.27f), mag);
+      const float ac = fabsf(CooL), e = kDtEtaCool * mag, num = 0.2f * p5;
+      const float tlo = __fdiv_rn(num, g1c * (ac + e)) * dn;
+      const float thi = ac > e ? __fdiv_rn(num, g1c * (ac - e)) * up : INF;
+      // the floor of the cooling time, bracketed in FP32
+      const float flo = 2.5e-4f * (1.0f - 1e-6f), fhi = 2.5e-4f * (1.0f + 1e-6f);
+      floored = thi <= flo;
+      lo[1] = fmaxf(tlo, flo);
+      hi[1] = fmaxf(thi, fhi);
+      bad = bad || !(alpha > 0.0f) || !(lo[1] > 0.0f);
     }
-    if (!(c_min > 0.0f) || !(s_min > 0.0f)) flag(err, ERRB_DT);
+    if (bad) flag(err, ERRB_DT);
   }
-  unsigned long long cb = (unsigned long long)__double_as_longlong(f2d(c_min > 0.0f ? c_min : 0.0f));
-  unsigned long long sb = (unsigned long long)__double_as_longlong(f2d(s_min > 0.0f ? s_min : 0.0f));
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long c2 = __shfl_xor_sync(0xffffffffu, cb, o), s2 = __shfl_xor_sync(0xffffffffu, sb, o);
-    cb = c2 < cb ? c2 : cb;
-    sb = s2 < sb ? s2 : sb;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      lo[q] = fminf(lo[q], __shfl_xor_sync(0xffffffffu, lo[q], o));
+      hi[q] = fminf(hi[q], __shfl_xor_sync(0xffffffffu, hi[q], o));
+    }
+  floored = __any_sync(0xffffffffu, floored);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long gw = t >> 5;
+  if (lane == 0 && gw < sc.nwarps) {
+    sc.lo[gw] = lo[0];
+    sc.lo[sc.nwarps + gw] = lo[1];
+    sc.lo[2 * sc.nwarps + gw] = lo[2];
   }
-  __shared__ unsigned long long wc[8], ws[8];
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) { wc[w] = cb; ws[w] = sb; }
+  __shared__ float wh[3][8];
+  if (lane == 0)
+    for (int q = 0; q < 3; q++) wh[q][w] = hi[q];
+  if (lane == 0 && floored) atomicOr(&sc.words[3], 1u);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
-      cb = wc[q] < cb ? wc[q] : cb;
-      sb = ws[q] < sb ? ws[q] : sb;
-    }
-    atomicMin(&out[0], cb);
-    atomicMin(&out[1], sb);
+  if (threadIdx.x < 3) {
+    float m = wh[threadIdx.x][0];
+    for (int q = 1; q < (int)(blockDim.x >> 5); q++) m = fminf(m, wh[threadIdx.x][q]);
+    atomicMin(&sc.words[threadIdx.x], __float_as_uint(m));
   }
 }
 

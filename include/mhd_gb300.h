@@ -123,7 +123,9 @@ int mhd_download(mhd_handle *h, double *U, double *species, double *bcc);
 int mhd_download_columns(mhd_handle *h, double *columns);
 
 /* Couran + Stblty + min (EVOLVE:569-599 for the whole grid).  *dt is
- * min(tfinal, CFL*tCFL, tLMT); *st is 1 (FastSpd) or 2 (Conduct). */
+ * min(tfinal, CFL*tCFL, tLMT); *st is 1 (FastSpd) or 2 (Conduct).  Both
+ * precisions return the FP64 minimum: the chosen form screens the cells in
+ * FP32 and recomputes in FP64 those that can hold it. */
 int mhd_timestep(mhd_handle *h, double *dt, int *st);
 int mhd_source(mhd_handle *h, double dt);             /* SOURCE(dt)        */
 int mhd_sweep(mhd_handle *h, int dir, double dt);     /* dir 0=x,1=y,2=z   */
@@ -223,8 +225,9 @@ int mhd_fp64_peak(int device, double *fma_gflops, double *div_gps, double *sqrt_
  * and ndtot (one block each, the module arrays of the same names), and
  * with ifchem == 2 and ifrad == 2 SHIELD's ten column blocks (the layout of
  * mhd_download_columns); a missing one gives MHD_ERR_ARG, and they are not
- * read otherwise.  The result equals mhd_timestep's on a handle of
- * precision MHD_PREC_FP64 holding the same arrays.
+ * read otherwise.  The result equals mhd_timestep's on a handle of either
+ * precision holding the same arrays (the chosen form keeps the CFL minimum
+ * in FP64).
  *
  * The kernels' scratch is a fixed file-scope device array (about 1 MB) that
  * every GPU loading the library keeps until exit, so grids are limited to

@@ -71,3 +71,45 @@ def test_fp32_close_to_oracle_on_any_grid(shape):
     # the ghost x-columns the y and z sweeps compute along are never stored:
     # nothing non-finite reaches the padded arrays
     assert np.isfinite(Ug).all() and np.isfinite(sg).all()
+
+
+def _states_for_dt():
+    from test_chem_oracle import chem_state, shield_state
+    from test_gpu_inflow import shock_tube
+    stiff = problems.colliding_flows(24)
+    stiff.U[0] *= 30.0
+    stiff.species *= 30.0
+    cs = chem_state(12, seed=9)
+    cs.params = cs.params.replace(ifthrm=2)
+    ss = shield_state(12, seed=10)
+    ss.params = ss.params.replace(ifthrm=2)
+    return {"colliding_flows": problems.colliding_flows(32), "turbulence": problems.turbulence(24, kmax=4),
+            "stiff_floored": stiff, "chemistry": cs, "chemistry_shield": ss,
+            "uniform_shock_tube": shock_tube(16, 8, 8)}
+
+
+@pytest.mark.parametrize("name", ["colliding_flows", "turbulence", "stiff_floored", "chemistry",
+                                  "chemistry_shield", "uniform_shock_tube"])
+def test_chosen_form_time_step_is_the_fp64_one(name):
+    """The CFL minimum stays FP64: the chosen form's FP32 screen plus the
+    FP64 recomputation of its candidates gives dt_kernel's result bit for
+    bit -- on the uploaded state, and (without the chemistry, whose FP32
+    network keeps nde and ndtot the upload would rebuild) after steps of
+    the chosen form, compared with an FP64 handle holding that state."""
+    st = _states_for_dt()[name]
+    g32 = native.Mhd3D(st.params, precision=native.PREC_FP32)
+    g32.upload(st)
+    g64 = native.Mhd3D(st.params)
+    g64.upload(st)
+    assert g32.timestep() == g64.timestep()
+    if getattr(st.params, "ifchem", 0) == 2:
+        return
+    for _ in range(3):
+        g32.step()
+    U, sp, _ = g32.download(with_bcc=False)
+    s2 = st.copy()
+    s2.U[...] = U
+    s2.species[...] = sp
+    g64b = native.Mhd3D(st.params)
+    g64b.upload(s2)
+    assert g32.timestep() == g64b.timestep()

@@ -62,3 +62,28 @@ def test_momentum_drifts_where_the_ghost_switch_differs():
     assert tmax > 3.0
     assert abs(m1 - m0) <= 1e-14 * m0          # mass still holds
     assert np.abs(p1 - p0).max() > 1e-9 * scale
+
+
+def test_div_b_round_off_except_next_to_a_free_x_boundary():
+    """CT keeps div B at round-off in every cell but the last one before a
+    free x boundary: the reference's BC=1 copy writes U(Ncellx) into indices
+    Ncellx+1..Ncellx+N_ol of every exchanged field
+    (3DMHD-feedback/MCF3DSGincfca3-feedback.f90:1261-1265), and for the face
+    field index Ncellx+1 is face n+1/2, so that cell's outer face is no
+    longer the one CT advanced."""
+    st = problems.colliding_flows(24)
+    assert st.params.bc[:2] == (1, 1)
+    o = Oracle3D(st.params)
+    o.upload(st)
+    for _ in range(10):
+        o.step()
+    U, _, _ = o.download()
+    n = 24
+    c = slice(2, 2 + n)
+    d = ((U[5][c, c, 3:3 + n] - U[5][c, c, 2:2 + n]) / st.dx[2]
+         + (U[6][c, 3:3 + n, c] - U[6][c, 2:2 + n, c]) / st.dy[2]
+         + (U[7][3:3 + n, c, c] - U[7][2:2 + n, c, c]) / st.dz[2])
+    a = np.abs(d)
+    bscale = np.abs(U[5:8][(slice(None),) + C]).max() / st.dx[2]
+    assert a[:, :, :n - 1].max() < 1e-13 * bscale
+    assert a[:, :, n - 1].max() > 1e-8 * bscale

@@ -104,3 +104,17 @@ def test_rejects_grids_beyond_the_scratch():
         native.timestep_noalloc(big, ds)
     assert e.value.code == 7
     torch.cuda.synchronize()
+
+
+def test_matches_chosen_form_handle_timestep():
+    """The chosen form keeps the CFL minimum in FP64, so an FP32 handle's
+    mhd_timestep equals the allocation-free result on its arrays."""
+    st = problems.colliding_flows(32)
+    g = native.Mhd3D(st.params, precision=native.PREC_FP32)
+    g.upload(st)
+    for _ in range(2):
+        g.step()
+    ref = g.timestep()
+    ds, keep = _device_arrays(g, st)
+    assert native.timestep_noalloc(st.params, ds, precision=native.PREC_FP32) == ref
+    assert native.timestep_noalloc(st.params, ds, precision=native.PREC_FP32) == ref
