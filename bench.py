@@ -450,7 +450,8 @@ def main():
         p_ref = None
         for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
                                  ("fp32_exact", native.PREC_FP32, native.COOL_EXACT),
-                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE)):
+                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE),
+                                 ("fp32_newton_no_network", native.PREC_FP32, native.COOL_NEWTON)):
             gs = native.Mhd3D(sst.params, precision=prec, cooling=cool, device=dev)
             gs.set_stream(stream.cuda_stream)
             if cool == native.COOL_SURROGATE:
@@ -472,14 +473,66 @@ def main():
             if p_ref is None:
                 p_ref = pp
             stiff[name] = {"ms_per_source": min(times), "bisection_cells": d["imc_cells"],
-                           "surrogate_cells": d["surrogate_cells"], "fallback_cells": d["fallback_cells"],
+                           "guess_accepted_cells": d["surrogate_cells"], "guess_rejected_cells": d["fallback_cells"],
                            "l1_p_vs_fp64": float(np.abs(pp - p_ref).mean() / np.abs(p_ref).mean())}
             del gs
         stiff["surrogate_speedup_vs_fp32_exact"] = (stiff["fp32_exact"]["ms_per_source"] /
                                                     stiff["fp32_surrogate"]["ms_per_source"])
-        stiff["fp32_surrogate"]["fallback_fraction"] = (
-            stiff["fp32_surrogate"]["fallback_cells"] /
-            max(1, stiff["fp32_surrogate"]["fallback_cells"] + stiff["fp32_surrogate"]["surrogate_cells"]))
+        stiff["surrogate_speedup_vs_newton_no_network"] = (stiff["fp32_newton_no_network"]["ms_per_source"] /
+                                                           stiff["fp32_surrogate"]["ms_per_source"])
+        for k in ("fp32_surrogate", "fp32_newton_no_network"):
+            r = stiff[k]
+            r["fallback_fraction"] = r["guess_rejected_cells"] / max(1, r["guess_rejected_cells"] + r["guess_accepted_cells"])
+
+        # The same solvers inside whole steps: the colliding flow at 3000x the
+        # density (n = 3000 cm^-3 at 6000 K cools in ~4e-4 Myr), where the
+        # reference's own time-step control leaves the cells stiff (the
+        # cooling-time limit 0.2 t_cool is floored at 2.5e-4 Myr, Stblty
+        # :2806).  At 30x the step's dt follows 0.2 t_cool and no cell is
+        # stiff; hence this density.  Steps 1..K from the uploaded state, each
+        # event-timed; FP64 runs the same steps for the error.
+        kst = 4
+        wst = problems.colliding_flows(args.n)
+        wst.U[0] *= 3000.0
+        wst.species *= 3000.0
+        wst.U[4] *= 3000.0          # the same 6000 K
+        steps_stiff = {"state": "colliding flow at 3000x density, 6000 K", "steps": kst}
+        u_ref = None
+        for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
+                                 ("fp32_exact", native.PREC_FP32, native.COOL_EXACT),
+                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE),
+                                 ("fp32_newton_no_network", native.PREC_FP32, native.COOL_NEWTON)):
+            gs = native.Mhd3D(wst.params, precision=prec, cooling=cool, device=dev)
+            gs.set_stream(stream.cuda_stream)
+            if cool == native.COOL_SURROGATE:
+                gs.surrogate_load(sur_params, 1e-3)
+            gs.upload(wst)
+            gs.reset_counters()
+            rec = {}
+            barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dts = []
+            gs.ifevo = 1
+            for _ in range(kst):
+                dts.append(step_timed(gs, rec, wst.params.dissip))
+            e1.record(stream)
+            barrier()
+            d = gs.diagnostics()
+            U = gs.download(with_bcc=False)[0]
+            c = (slice(2, -2),) * 3
+            if u_ref is None:
+                u_ref = (U[0][c].copy(), U[4][c].copy())
+            steps_stiff[name] = {"ms_per_step": e0.elapsed_time(e1) / kst, "phase_ms": phase_ms(rec), "dt": dts,
+                                 "bisection_cells": d["imc_cells"], "guess_accepted_cells": d["surrogate_cells"],
+                                 "guess_rejected_cells": d["fallback_cells"],
+                                 "l1_rho_vs_fp64": float(np.abs(U[0][c] - u_ref[0]).mean() / np.abs(u_ref[0]).mean()),
+                                 "l1_p_vs_fp64": float(np.abs(U[4][c] - u_ref[1]).mean() / np.abs(u_ref[1]).mean())}
+            del gs
+        steps_stiff["surrogate_speedup_vs_fp32_exact"] = (steps_stiff["fp32_exact"]["ms_per_step"] /
+                                                          steps_stiff["fp32_surrogate"]["ms_per_step"])
+        stiff["whole_steps"] = steps_stiff
 
     def divb_split(g_, state):
         """max |div B| over the interior cells, and over those not next to a

@@ -44,7 +44,6 @@ struct mhd_handle {
   // pass, cleared by every writer of the species (upload, mhd_step_host,
   // the sweeps, the chemistry network)
   bool sh2_valid = false;
-  int *stiff_list = nullptr;             // SOURCE's stiff cells (FP32 form with a surrogate)
   float *vf32[3] = {nullptr, nullptr, nullptr};
   float *bf32[3] = {nullptr, nullptr, nullptr};
   float *rn32 = nullptr, *sw32 = nullptr;
@@ -146,6 +145,7 @@ int check_err(mhd_handle *h) {
   CKR(cudaStreamSynchronize(h->stream));
   if (e & ERRB_NONFINITE) return fail(h, MHD_ERR_NONFINITE, "non-finite value in the state (time %.17g)", h->time);
   if (e & ERRB_DT) return fail(h, MHD_ERR_DT, "non-positive time-step limit (err at Couran/Stblty)");
+  if (e & ERRB_TC) return fail(h, MHD_ERR_CUDA, "tensor-core completion wait timed out in SOURCE");
   return MHD_OK;
 }
 
@@ -172,12 +172,13 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   for (int q = 0; q < 6; q++)   // codes 1 (free), 3 (periodic), 4 (inflow, x sides only)
     if (!(valid_bc(p->bc[q]) || (q < 2 && p->bc[q] == 4))) return MHD_ERR_ARG;
   if (p->precision != MHD_PREC_FP64 && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
-  if (p->cooling != MHD_COOL_EXACT && p->cooling != MHD_COOL_SURROGATE) return MHD_ERR_ARG;
-  if (p->cooling == MHD_COOL_SURROGATE && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
+  if (p->cooling != MHD_COOL_EXACT && p->cooling != MHD_COOL_SURROGATE && p->cooling != MHD_COOL_NEWTON)
+    return MHD_ERR_ARG;
+  if (p->cooling != MHD_COOL_EXACT && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
   if (p->ifchem != 0 && p->ifchem != 2) return MHD_ERR_ARG;
   if (p->ifrad != 0 && p->ifrad != 2) return MHD_ERR_ARG;
   // the surrogate is trained on the KI cooling function only
-  if (p->cooling == MHD_COOL_SURROGATE && p->ifchem == 2) return MHD_ERR_ARG;
+  if (p->cooling != MHD_COOL_EXACT && p->ifchem == 2) return MHD_ERR_ARG;
   if (p->dissip && p->nx < 11) return MHD_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p->device) return MHD_ERR_NO_DEVICE;
@@ -250,7 +251,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     for (int q = 0; q < 10; q++) h->f.col[q] = h->colblock + (size_t)q * g.ncell;
   }
   if (p->precision == MHD_PREC_FP32) {
-    const size_t nf = 15;   // 14 FP32 arrays + the stiff-cell list of SOURCE
+    const size_t nf = 14;   // 14 FP32 arrays
     size_t fbytes = nf * (size_t)g.ncell * sizeof(float);
     if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess) {
       cudaGetLastError();
@@ -277,7 +278,6 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     h->rn32 = fq; fq += g.ncell;
     h->sw32 = fq; fq += g.ncell;
     for (int c = 0; c < 3; c++) { h->emf32[c] = fq; fq += g.ncell; }
-    h->stiff_list = reinterpret_cast<int *>(fq); fq += g.ncell;
     cudaMemsetAsync(h->fblock, 0, fbytes, h->stream);
   }
   cudaMemsetAsync(h->block, 0, bytes, h->stream);
@@ -505,24 +505,24 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     a.W = (h->p.cooling == MHD_COOL_SURROGATE) ? h->sur_net : nullptr;
     a.tol = h->sur_tol;
     a.T = h->temp32;
-    a.stiff_list = h->stiff_list; a.stiff_count = h->dtred + 5;
     a.sh2 = h->sh2_32;
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
-    // with a surrogate, source_fp32 launches a second (stiff-cell) kernel
-    const int extra = (a.W && h->ph.ifchem != 2) ? 1 : 0;
+    // how stiff cells start their implicit solve: the network, the
+    // frozen-rate Newton start, or the bisection alone
+    const int stiff_mode = h->p.cooling == MHD_COOL_SURROGATE ? STIFF_NETWORK
+                           : h->p.cooling == MHD_COOL_NEWTON  ? STIFF_NEWTON
+                                                              : 0;
     // S and H2 from the species, unless SOURCE formed them from the same
     // species before (the previous step's second SOURCE); an inflow side
     // refills the ghost species from the advected reservoir every time
     const bool inflow = h->ph.in.on[0] || h->ph.in.on[1];
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, !(h->sh2_valid && !inflow), h->stream));
     h->sh2_valid = true;
-    CK(source_fp32(a, h->stream));
-    h->launches += extra;
+    CK(source_fp32(a, stiff_mode, h->stream));
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, false, h->stream));
-    CK(source_fp32(a, h->stream));
-    h->launches += extra;
+    CK(source_fp32(a, stiff_mode, h->stream));
     return MHD_OK;
   }
   SourceArgs a{};

@@ -203,30 +203,43 @@ cudaError_t shield_fp32(const Grid &g, const Phys &ph, const Fields &f, double *
   return shield_scan(g, f, tau, dxh, s);
 }
 
-cudaError_t source_fp32(const Source32Args &a, cudaStream_t s) {
+cudaError_t source_fp32(const Source32Args &a, int stiff_mode, cudaStream_t s) {
   long long n = (long long)a.g.n[0] * a.g.n[1] * a.g.n[2];
   const unsigned nb = (unsigned)((n + 127) / 128);
-  // the species cooling (ifchem = 2) runs without a surrogate (the network
-  // models the KI function only; mhd_create refuses the combination)
+  // the species cooling (ifchem = 2) runs with the bisection only (the
+  // network and the Newton start model the KI function; mhd_create refuses
+  // the combinations)
   if (a.ph.ifchem == 2) {
-    source32_kernel<true, false><<<nb, 128, 0, s>>>(a);
+    source32_kernel<true><<<nb, 128, 0, s>>>(a);
     return cudaGetLastError();
   }
-  if (a.W == nullptr) {
-    source32_kernel<false, false><<<nb, 128, 0, s>>>(a);
+  if (stiff_mode == 0) {
+    source32_kernel<false><<<nb, 128, 0, s>>>(a);
     return cudaGetLastError();
   }
-  // with a surrogate: explicit cells here, stiff cells listed and solved by
-  // a second pass over whole warps of them
-  if (!a.stiff_list || !a.stiff_count) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMemsetAsync(a.stiff_count, 0, sizeof(unsigned long long), s);
-  if (e != cudaSuccess) return e;
-  source32_kernel<false, true><<<(unsigned)((n + kSourceDeferThreads - 1) / kSourceDeferThreads),
-                                 kSourceDeferThreads, 0, s>>>(a);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  const unsigned ns = (unsigned)min((long long)nb, 152LL * 16);
-  source32_stiff_kernel<<<ns, 128, 0, s>>>(a);
+  // a persistent grid: as many 256-cell CTAs as fit at once (for the
+  // network at most four per SM, so their TMEM columns (128 each) fit in
+  // the SM's 512; its launch bounds allow three)
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long tiles = (n + kFusedThreads - 1) / kFusedThreads;
+  cudaError_t e;
+  if (stiff_mode == STIFF_NETWORK) {
+    if (!a.W) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(SurTileSmem<kFusedTiles>);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, source32_fused_kernel<STIFF_NETWORK>, kFusedThreads,
+                                                      smem);
+    if (e != cudaSuccess) return e;
+    per_sm = per_sm < 4 ? per_sm : 4;
+    const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)std::max(per_sm, 1) * sms);
+    source32_fused_kernel<STIFF_NETWORK><<<grid, kFusedThreads, smem, s>>>(a);
+  } else {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, source32_fused_kernel<STIFF_NEWTON>, kFusedThreads, 0);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)std::max(per_sm, 1) * sms);
+    source32_fused_kernel<STIFF_NEWTON><<<grid, kFusedThreads, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

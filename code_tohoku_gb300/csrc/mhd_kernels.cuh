@@ -26,6 +26,7 @@ enum : int {
   ERRB_NONFINITE = 1,
   ERRB_DT = 2,
   ERRB_IMC = 4,
+  ERRB_TC = 8,            // a tensor-core completion wait timed out (the network was switched off)
 };
 
 struct Grid {

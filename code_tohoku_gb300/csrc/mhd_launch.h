@@ -19,7 +19,9 @@ cudaError_t sweep_fp64(int dir, const SweepArgs &a, cudaStream_t s);
 cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s);
 // chosen form (FP32 reconstruction / Riemann / characteristics / EMF)
 cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s);
-cudaError_t source_fp32(const Source32Args &a, cudaStream_t s);
+// stiff_mode 0: the bisection for stiff cells; STIFF_NETWORK / STIFF_NEWTON:
+// the guess-and-polish path of source32_fused_kernel
+cudaError_t source_fp32(const Source32Args &a, int stiff_mode, cudaStream_t s);
 // FP32 temperatures of every padded cell; from_species: from the species
 // (and store S = H+p+He+He+ and H2 in sh2, 2 ncell floats), else from them
 cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double kb, float *T, float *sh2,

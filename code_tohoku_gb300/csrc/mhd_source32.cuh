@@ -60,12 +60,19 @@ struct Source32Args {
   unsigned long long *imc_count;
   unsigned long long *sur_count;   // surrogate accepted
   unsigned long long *fb_count;    // surrogate rejected -> bisection
-  const SurNet *W;                 // surrogate network (null: exact only)
-  float tol;                       // residual tolerance for accepting it
-  int *stiff_list;                 // with a surrogate: cells left to the stiff pass
+  const SurNet *W;                 // surrogate network (null: none)
+  float tol;                       // residual tolerance for accepting a polished guess
   const float *sh2;                // S = H+p+He+He+ and H2 of every cell (temp32), or null
-  unsigned long long *stiff_count; // their number (zeroed before each pass)
 };
+
+// How a stiff cell's implicit solve starts when it does not go straight to
+// the bisection (KI cooling only): from the network's answer, or -- the
+// same solver without the network, for comparison -- from the frozen-rate
+// implicit update P_b / (1 + c Lambda_b / P_b) (the explicit update when
+// Lambda_b heats).
+enum : int { STIFF_NETWORK = 1, STIFF_NEWTON = 2 };
+constexpr int kFusedTiles = 2;                  // 128-cell tiles per CTA of the fused SOURCE
+constexpr int kFusedThreads = 128 * kFusedTiles;
 
 }  // namespace mhd
 
@@ -112,9 +119,6 @@ __global__ void __launch_bounds__(256) temp32_kernel(long long ncell, Fields f, 
     T[t] = __fdividef(d2f(pin[t]), kb * (sh2[t] + sh2[ncell + t]));
   }
 }
-
-// block size of the pass that defers stiff cells (one list append per block)
-constexpr int kSourceDeferThreads = 512;
 
 // One pass of the chosen-form SOURCE for one cell: the quantities of the
 // cell (source32_prep) and the pressure update from the cooling increment
@@ -212,82 +216,17 @@ __device__ __noinline__ float imc32_cell(const Cell32<CHEM> &c) {
   else return imc32(c.basef, c.nkbi, cc, [&](float T) { return fcool_ki(T, c.NN); });
 }
 
-// The surrogate's answer for a stiff cell (warp-collective: every lane of
-// the warp calls it, `on` marks the lanes with a cell): its inputs log10 N,
-// log10 T, log10(dts / t_cool) with t_cool = P/((gamma-1)|Lambda|) at the
-// starting state, the network, two Newton steps on f(P) = P + c Lambda(P) -
-// P_start (c = dt (gamma-1)), and the implicit residual
-// |P + Lambda(P) dt (gamma-1) - P_old| / P_old as the acceptance test.
-// Returns true with dp when accepted.
-__device__ __forceinline__ bool surrogate_cell(const Source32Args &A, const SurNetSmem *net, bool on,
-                                               const Cell32<false> &c, float *dp) {
-  const float Tb = c.basef * c.nkbi;               // temperature the implicit solve starts from
-  const float Lb = fcool_ki(Tb, c.NN);
-  const float r = c.dts * c.g1 * fabsf(Lb) / c.basef;
-  const float x0 = log10f(c.NN), x1 = log10f(Tb), x2 = log10f(fmaxf(r, 1e-30f));
-  const bool inbox = on && x0 >= -2.0f && x0 <= 5.0f && x1 >= -2.0f && x1 <= 1.30103f && x2 >= -3.0f && x2 <= 3.0f;
-  float conf;
-  const float y = surrogate_warp_smem(net, x0, x1, x2, inbox, &conf);
-  if (!inbox) return false;
-  const float cc = c.dts * c.g1;
-  float P = (Tb * exp10f(y)) / c.nkbi;
-  for (int it = 0; it < 2; it++) {
-    float L, dL;
-    fcool_ki_d(P * c.nkbi, c.NN, L, dL);
-    const float fv = P + cc * L - c.basef;
-    const float fp = 1.0f + cc * dL * c.nkbi;
-    if (fp > 0.0f) P = fmaxf(P - fv / fp, 0.1f * P);
-  }
-  const float res = fabsf(P + fcool_ki(P * c.nkbi, c.NN) * cc - c.basef) / c.basef;
-  if (res <= A.tol) {
-    *dp = P - c.basef;
-    atomicAdd(A.sur_count, 1ull);
-    return true;
-  }
-  atomicAdd(A.fb_count, 1ull);
-  return false;
-}
-
-// Thread per cell.  CHEM: the species cooling function (ifchem = 2) instead
-// of the KI one.  DEFER (a surrogate is loaded): stiff cells are appended to
-// A.stiff_list and left to source32_stiff_kernel, so this kernel carries
-// only the registers of the explicit path (used with the KI cooling only);
-// otherwise they are solved here by the bisection.
-template <bool CHEM, bool DEFER>
-__global__ void __launch_bounds__(DEFER ? kSourceDeferThreads : 128) source32_kernel(Source32Args A) {
+// Thread per cell, the bisection for stiff cells (exact cooling).  CHEM:
+// the species cooling function (ifchem = 2) instead of the KI one.
+template <bool CHEM>
+__global__ void __launch_bounds__(128) source32_kernel(Source32Args A) {
   const Grid &g = A.g;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = t < (long long)g.n[0] * g.n[1] * g.n[2];
   const Cell32<CHEM> c = source32_prep<CHEM>(A, valid ? t : 0);
-  const bool stiff = valid && c.stiff;
-  if constexpr (DEFER) {
-    // block-aggregated append of the stiff cells' indices: one atomic per
-    // block on the shared counter; a block without stiff cells passes one
-    // barrier only
-    if (__syncthreads_or(stiff)) {
-      __shared__ unsigned wcnt[kSourceDeferThreads / 32];
-      __shared__ unsigned long long bbase;
-      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-      const unsigned m = __ballot_sync(0xffffffffu, stiff);
-      if (lane == 0) wcnt[w] = __popc(m);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        unsigned tot = 0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); q++) tot += wcnt[q];
-        bbase = atomicAdd(A.stiff_count, (unsigned long long)tot);
-      }
-      __syncthreads();
-      if (stiff) {
-        unsigned long long pos = bbase;
-        for (int q = 0; q < w; q++) pos += wcnt[q];
-        A.stiff_list[pos + __popc(m & ((1u << lane) - 1u))] = (int)t;
-      }
-    }
-    if (!valid || stiff) return;
-  }
   if (!valid) return;
   float dp_cool;
-  if (!stiff) {
+  if (!c.stiff) {
     dp_cool = -(c.g1 * c.CooL * c.dts);
   } else {
     dp_cool = imc32_cell<CHEM>(c) - c.basef;
@@ -296,29 +235,88 @@ __global__ void __launch_bounds__(DEFER ? kSourceDeferThreads : 128) source32_ke
   source32_finish<CHEM>(A, c, dp_cool);
 }
 
-// The stiff cells listed by source32_kernel<false, true> (KI cooling): the
-// surrogate for whole warps of stiff cells, the bisection for the cells it
-// rejects.  Blocks stride over the list; every lane of a block runs the same
-// trips, so the warp-collective network sees full warps.
-__global__ void __launch_bounds__(128) source32_stiff_kernel(Source32Args A) {
-  constexpr bool CHEM = false;
-  const long long cnt = (long long)*A.stiff_count;
-  if ((long long)blockIdx.x * blockDim.x >= cnt) return;   // whole block: no stiff cell for it
-  __shared__ SurNetSmem net;
-  sur_stage(A.W, &net);
-  for (long long e0 = (long long)blockIdx.x * blockDim.x; e0 < cnt; e0 += (long long)gridDim.x * blockDim.x) {
-    const long long e = e0 + threadIdx.x;
-    const bool on = e < cnt;
-    const long long t = A.stiff_list[on ? e : e0];
-    const Cell32<CHEM> c = source32_prep<CHEM>(A, t);
-    float dp_cool = 0.0f;
-    const bool done = surrogate_cell(A, &net, on, c, &dp_cool);
-    if (!on) continue;
-    if (!done) {
-      dp_cool = imc32_cell<CHEM>(c) - c.basef;
-      atomicAdd(A.imc_count, 1ull);
+// Two Newton steps on f(P) = P + c Lambda(P) - P_b (c = dt (gamma-1)) from
+// P, then the implicit residual |P + Lambda(P) c - P_b| / P_b of
+// IMC's equation (MCF3DSGincfca3.f90:2911) as the acceptance test.
+__device__ __forceinline__ bool polish_accept(const Source32Args &A, const Cell32<false> &c, float P, float *dp) {
+  const float cc = c.dts * c.g1;
+  for (int it = 0; it < 2; it++) {
+    float L, dL;
+    fcool_ki_d(P * c.nkbi, c.NN, L, dL);
+    const float fv = P + cc * L - c.basef;
+    const float fp = 1.0f + cc * dL * c.nkbi;
+    if (fp > 0.0f) P = fmaxf(P - fv / fp, 0.1f * P);
+  }
+  const float res = fabsf(P + fcool_ki(P * c.nkbi, c.NN) * cc - c.basef) / c.basef;
+  if (!(res <= A.tol)) return false;
+  *dp = P - c.basef;
+  return true;
+}
+
+// SOURCE with the KI cooling when the stiff cells start from a guess: one
+// persistent kernel over blocks of 256 cells (thread per cell).  Explicit
+// cells update at once; when a block holds stiff cells, its threads form
+// the guess -- MODE STIFF_NETWORK: the surrogate network on the tensor cores
+// for the whole block (sur_tile_forward; the weights are staged and TMEM is
+// allocated by the first such block of the CTA), inputs outside the
+// training box going straight to the bisection -- then polish and test it,
+// and the rejected cells take the bisection.  Counters: sur_count accepted
+// guesses, fb_count rejected ones, imc_count every bisection.
+template <int MODE>
+__global__ void __launch_bounds__(kFusedThreads, 3) source32_fused_kernel(Source32Args A) {
+  extern __shared__ __align__(128) unsigned char fused_smem[];
+  using Tile = SurTileSmem<kFusedTiles>;
+  Tile *s = reinterpret_cast<Tile *>(fused_smem);
+  const long long ncells = (long long)A.g.n[0] * A.g.n[1] * A.g.n[2];
+  const long long step = (long long)gridDim.x * kFusedThreads;
+  const int lane = threadIdx.x & 31;
+  bool ready = false;   // the same on every thread (set under a block-wide condition)
+  uint32_t phase = 0;
+  for (long long t0 = (long long)blockIdx.x * kFusedThreads; t0 < ncells; t0 += step) {
+    const long long t = t0 + threadIdx.x;
+    const bool valid = t < ncells;
+    const Cell32<false> c = source32_prep<false>(A, valid ? t : t0);
+    const bool stiff = valid && c.stiff;
+    float dp_cool = -(c.g1 * c.CooL * c.dts);
+    if (__syncthreads_or(stiff)) {
+      const float Tb = c.basef * c.nkbi;   // temperature the implicit solve starts from
+      const float Lb = fcool_ki(Tb, c.NN);
+      const float cc = c.dts * c.g1;
+      bool use = stiff;
+      float P;
+      if constexpr (MODE == STIFF_NETWORK) {
+        if (!ready) {
+          sur_tile_setup<kFusedTiles>(A.W, s);
+          ready = true;
+        }
+        const float rr = cc * fabsf(Lb) / c.basef;
+        const float x0 = log10f(c.NN), x1 = log10f(Tb), x2 = log10f(fmaxf(rr, 1e-30f));
+        const bool inbox = stiff && x0 >= -2.0f && x0 <= 5.0f && x1 >= -2.0f && x1 <= 1.30103f && x2 >= -3.0f &&
+                           x2 <= 3.0f;
+        float y0 = 0.0f, y1 = 0.0f;
+        const bool ok = sur_tile_forward<kFusedTiles>(s, inbox ? (x0 - SUR_C0) / SUR_S0 : 0.0f,
+                                                      inbox ? (x1 - SUR_C1) / SUR_S1 : 0.0f,
+                                                      inbox ? (x2 - SUR_C2) / SUR_S2 : 0.0f, phase, y0, y1);
+        if (!ok && threadIdx.x == 0) flag(A.err, ERRB_TC);
+        use = inbox && ok;
+        P = (Tb * exp10f(y0)) / c.nkbi;
+      } else {
+        P = Lb > 0.0f ? c.basef / (1.0f + cc * Lb / c.basef) : c.basef - cc * Lb;
+      }
+      const bool acc = use && polish_accept(A, c, P, &dp_cool);
+      const unsigned mu = __ballot_sync(0xffffffffu, use), ma = __ballot_sync(0xffffffffu, acc);
+      const unsigned mb = __ballot_sync(0xffffffffu, stiff && !acc);
+      if (lane == 0) {
+        if (ma) atomicAdd(A.sur_count, (unsigned long long)__popc(ma));
+        if (mu & ~ma) atomicAdd(A.fb_count, (unsigned long long)__popc(mu & ~ma));
+        if (mb) atomicAdd(A.imc_count, (unsigned long long)__popc(mb));
+      }
+      if (stiff && !acc) dp_cool = imc32_cell<false>(c) - c.basef;
     }
-    source32_finish<CHEM>(A, c, dp_cool);
+    if (valid) source32_finish<false>(A, c, dp_cool);
+  }
+  if constexpr (MODE == STIFF_NETWORK) {
+    if (ready) sur_tile_teardown<kFusedTiles>(s, phase);
   }
 }
 

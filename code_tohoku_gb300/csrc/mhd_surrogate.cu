@@ -7,7 +7,7 @@
 //                     (mma.sync m16n8k16, FP32 accumulate), gradients of
 //                     the mean squared error summed into an FP32 vector
 //   sur_adam_kernel   Adam update of the FP32 master parameters
-//   sur_eval_kernel   batch inference (the device code of the fused source)
+//   sur_eval_kernel   batch inference (tcgen05 tiles: the fused SOURCE's network code)
 // and the extern "C" entry points that expose them.
 #include <cuda_runtime.h>
 
@@ -87,16 +87,31 @@ __global__ void sur_pack_kernel(const float *m, SurNet *net) {
   if (t < 8) net->b3[t] = t < 2 ? m[SUR_OB3 + t] : 0.0f;
 }
 
-__global__ void sur_eval_kernel(const SurNet *net, const float *x, float *out, long long n) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  bool act = i < n;
-  float x0 = act ? x[3 * i] : 0.0f, x1 = act ? x[3 * i + 1] : 0.0f, x2 = act ? x[3 * i + 2] : 0.0f;
-  float conf;
-  float y = surrogate_warp(net, x0, x1, x2, act, &conf);
-  if (act) {
-    out[2 * i] = y;
-    out[2 * i + 1] = conf;
+// Batch inference with the fused SOURCE's network code: tcgen05 tiles of
+// 128 samples, two per 256-thread CTA, the weights staged once per CTA.
+__global__ void __launch_bounds__(kFusedThreads) sur_eval_kernel(const SurNet *net, const float *x, float *out,
+                                                                 long long n, int *err) {
+  extern __shared__ __align__(128) unsigned char eval_smem[];
+  auto *s = reinterpret_cast<SurTileSmem<kFusedTiles> *>(eval_smem);
+  sur_tile_setup<kFusedTiles>(net, s);
+  uint32_t phase = 0;
+  for (long long i0 = (long long)blockIdx.x * kFusedThreads; i0 < n; i0 += (long long)gridDim.x * kFusedThreads) {
+    const long long i = i0 + threadIdx.x;
+    const bool act = i < n;
+    const float n0 = act ? (x[3 * i] - SUR_C0) / SUR_S0 : 0.0f;
+    const float n1 = act ? (x[3 * i + 1] - SUR_C1) / SUR_S1 : 0.0f;
+    const float n2 = act ? (x[3 * i + 2] - SUR_C2) / SUR_S2 : 0.0f;
+    float y0 = 0.0f, y1 = 0.0f;
+    if (!sur_tile_forward<kFusedTiles>(s, n0, n1, n2, phase, y0, y1)) {
+      if (threadIdx.x == 0) atomicOr(err, ERRB_TC);
+      break;   // the same on every thread
+    }
+    if (act) {
+      out[2 * i] = y0;
+      out[2 * i + 1] = y1;
+    }
   }
+  sur_tile_teardown<kFusedTiles>(s, phase);
 }
 
 // Loss per sample: (o0 - y)^2 + w_c (o1 - log10(|o0 - y| + 1e-4))^2, the
@@ -368,17 +383,31 @@ int mhd_surrogate_eval(const float *params, const float *x, float *out, long lon
   if (!params || !x || !out || n <= 0) return MHD_ERR_ARG;
   int r = sur_device(device);
   if (r) return r;
-  DevBuf dm, dnet, dx, dout;
+  DevBuf dm, dnet, dx, dout, derr;
   SCK(cudaMalloc(&dm.p, SUR_NPARAM * sizeof(float)));
   SCK(cudaMalloc(&dnet.p, sizeof(SurNet)));
   SCK(cudaMalloc(&dx.p, n * 3 * sizeof(float)));
   SCK(cudaMalloc(&dout.p, n * 2 * sizeof(float)));
+  SCK(cudaMalloc(&derr.p, sizeof(int)));
+  SCK(cudaMemset(derr.p, 0, sizeof(int)));
   SCK(cudaMemcpy(dm.p, params, SUR_NPARAM * sizeof(float), cudaMemcpyHostToDevice));
   SCK(cudaMemcpy(dx.p, x, n * 3 * sizeof(float), cudaMemcpyHostToDevice));
   sur_pack_kernel<<<16, 256>>>(dm.as<float>(), dnet.as<SurNet>());
-  sur_eval_kernel<<<nb(n, 128), 128>>>(dnet.as<SurNet>(), dx.as<float>(), dout.as<float>(), n);
+  // a persistent grid, at most four CTAs per SM (128 TMEM columns each)
+  int sms = 0, per_sm = 0;
+  SCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const size_t smem = sizeof(SurTileSmem<kFusedTiles>);
+  SCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sur_eval_kernel, kFusedThreads, smem));
+  per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+  const long long tiles = (n + kFusedThreads - 1) / kFusedThreads;
+  const unsigned grid = (unsigned)(tiles < (long long)per_sm * sms ? tiles : (long long)per_sm * sms);
+  sur_eval_kernel<<<grid, kFusedThreads, smem>>>(dnet.as<SurNet>(), dx.as<float>(), dout.as<float>(), n,
+                                                  derr.as<int>());
   SCK(cudaGetLastError());
   SCK(cudaMemcpy(out, dout.p, n * 2 * sizeof(float), cudaMemcpyDeviceToHost));
+  int e = 0;
+  SCK(cudaMemcpy(&e, derr.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return MHD_ERR_CUDA;
   return MHD_OK;
 }
 

@@ -19,7 +19,7 @@ ERRORS = {1: "MHD_ERR_ARG", 2: "MHD_ERR_CUDA", 3: "MHD_ERR_NONFINITE", 4: "MHD_E
           5: "MHD_ERR_STATE", 6: "MHD_ERR_NO_DEVICE", 7: "MHD_ERR_TOO_LARGE"}
 NOALLOC_MAX_CELLS = 16777216
 PREC_FP64, PREC_FP32 = 0, 1
-COOL_EXACT, COOL_SURROGATE = 0, 1
+COOL_EXACT, COOL_SURROGATE, COOL_NEWTON = 0, 1, 2
 
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_timestep", "mhd_source",

@@ -56,6 +56,9 @@ extern "C" {
 
 #define MHD_COOL_EXACT 0       /* explicit step or IMC bisection (reference) */
 #define MHD_COOL_SURROGATE 1   /* MLP surrogate with exact fallback          */
+#define MHD_COOL_NEWTON 2      /* the surrogate's Newton polish from the
+                                  frozen-rate implicit start, no network,
+                                  exact fallback (the comparison case)      */
 
 typedef struct mhd_params {
   int nx, ny, nz;              /* interior cells (Ncellx, Ncelly, Ncellz);

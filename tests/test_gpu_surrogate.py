@@ -89,6 +89,20 @@ def test_fp32_source_matches_fp64():
     assert np.abs(p32 - p64).mean() / np.abs(p64).mean() < 1e-5
 
 
+def test_tensor_core_inference_matches_numpy(trained):
+    """The tcgen05 forward (128-row tiles, BF16 operands in shared memory,
+    FP32 accumulators in tensor memory) against the NumPy forward with the
+    same BF16 rounding points; the GPU's SiLU is the tanh form on BF16
+    pairs, so agreement is to BF16 activation rounding.  5001 samples: a
+    partial last tile too."""
+    p, _ = trained
+    x = sample(5001, 21)
+    out = native.surrogate_eval(p, x)
+    ref = S.forward(p, x)["y"]
+    d = np.abs(out - ref)
+    assert d.max() < 0.05 and d.mean() < 5e-3, (d.max(0), d.mean(0))
+
+
 def test_surrogate_takes_over_stiff_cells(trained):
     p, _ = trained
     st = stiff_state()
