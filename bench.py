@@ -339,6 +339,21 @@ def main():
         launches = g.kernel_launches - launches0
         return g, ms, phase_ms(rec), launches, clk.summary()
 
+    def divb_split(g_, state):
+        """max |div B| over the interior cells, and over those not next to a
+        free x boundary (there the reference's face exchange rewrites face
+        n+1, so the last cell's div B is not round-off)."""
+        U_ = g_.download(with_bcc=False)[0]
+        n_ = state.params.nx
+        c = slice(2, 2 + n_)
+        d = ((U_[5][c, c, 3:3 + n_] - U_[5][c, c, 2:2 + n_]) / state.dx[2:2 + n_][None, None, :]
+             + (U_[6][c, 3:3 + n_, c] - U_[6][c, 2:2 + n_, c]) / state.dy[2:2 + n_][None, :, None]
+             + (U_[7][3:3 + n_, c, c] - U_[7][2:2 + n_, c, c]) / state.dz[2:2 + n_][:, None, None])
+        a = np.abs(d)
+        lo = 1 if state.params.bc[0] == 1 else 0
+        hi = n_ - 1 if state.params.bc[1] == 1 else n_
+        return float(a.max()), float(a[:, :, lo:hi].max())
+
     hbm, which = peaks()
     # chosen form: FP32 reconstruction/flux + FP64 accumulation + surrogate
     g32, ms32, ph32, launches32, clocks = timed_run(native.PREC_FP32, native.COOL_SURROGATE)
@@ -533,21 +548,6 @@ def main():
         steps_stiff["surrogate_speedup_vs_fp32_exact"] = (steps_stiff["fp32_exact"]["ms_per_step"] /
                                                           steps_stiff["fp32_surrogate"]["ms_per_step"])
         stiff["whole_steps"] = steps_stiff
-
-    def divb_split(g_, state):
-        """max |div B| over the interior cells, and over those not next to a
-        free x boundary (there the reference's face exchange rewrites face
-        n+1, so the last cell's div B is not round-off)."""
-        U_ = g_.download(with_bcc=False)[0]
-        n_ = state.params.nx
-        c = slice(2, 2 + n_)
-        d = ((U_[5][c, c, 3:3 + n_] - U_[5][c, c, 2:2 + n_]) / state.dx[2:2 + n_][None, None, :]
-             + (U_[6][c, 3:3 + n_, c] - U_[6][c, 2:2 + n_, c]) / state.dy[2:2 + n_][None, :, None]
-             + (U_[7][3:3 + n_, c, c] - U_[7][2:2 + n_, c, c]) / state.dz[2:2 + n_][:, None, None])
-        a = np.abs(d)
-        lo = 1 if state.params.bc[0] == 1 else 0
-        hi = n_ - 1 if state.params.bc[1] == 1 else n_
-        return float(a.max()), float(a[:, :, lo:hi].max())
 
     def drift(d0, d1, scale):
         """Mass and momentum change over a run; momentum relative to the sum

@@ -83,9 +83,10 @@ def _states_for_dt():
     cs.params = cs.params.replace(ifthrm=2)
     ss = shield_state(12, seed=10)
     ss.params = ss.params.replace(ifthrm=2)
+    tube = shock_tube(16, 8, 8)   # two uniform halves: many cells tie for the minimum
+    tube.params = tube.params.replace(bc=(1, 1, 3, 3, 3, 3))
     return {"colliding_flows": problems.colliding_flows(32), "turbulence": problems.turbulence(24, kmax=4),
-            "stiff_floored": stiff, "chemistry": cs, "chemistry_shield": ss,
-            "uniform_shock_tube": shock_tube(16, 8, 8)}
+            "stiff_floored": stiff, "chemistry": cs, "chemistry_shield": ss, "uniform_shock_tube": tube}
 
 
 @pytest.mark.parametrize("name", ["colliding_flows", "turbulence", "stiff_floored", "chemistry",
