@@ -40,6 +40,7 @@ struct mhd_handle {
   double dxh = 0.0;               // SHIELD's half width 0.5 dx(1)
   float *temp32 = nullptr;
   float *sh2_32 = nullptr;               // SOURCE's FP32 S = H+p+He+He+ and H2 (2 ncell floats)
+  int *stiff_list = nullptr;             // SOURCE's stiff cells (guess-and-polish cooling modes)
   // sh2_32 holds S and H2 of the current species: set by SOURCE's first
   // pass, cleared by every writer of the species (upload, mhd_step_host,
   // the sweeps, the chemistry network)
@@ -251,7 +252,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     for (int q = 0; q < 10; q++) h->f.col[q] = h->colblock + (size_t)q * g.ncell;
   }
   if (p->precision == MHD_PREC_FP32) {
-    const size_t nf = 14;   // 14 FP32 arrays
+    const size_t nf = 15;   // 14 FP32 arrays + the stiff-cell list of SOURCE
     size_t fbytes = nf * (size_t)g.ncell * sizeof(float);
     if (cudaMalloc(&h->fblock, fbytes) != cudaSuccess) {
       cudaGetLastError();
@@ -278,6 +279,7 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     h->rn32 = fq; fq += g.ncell;
     h->sw32 = fq; fq += g.ncell;
     for (int c = 0; c < 3; c++) { h->emf32[c] = fq; fq += g.ncell; }
+    h->stiff_list = reinterpret_cast<int *>(fq); fq += g.ncell;
     cudaMemsetAsync(h->fblock, 0, fbytes, h->stream);
   }
   cudaMemsetAsync(h->block, 0, bytes, h->stream);
@@ -506,6 +508,7 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     a.tol = h->sur_tol;
     a.T = h->temp32;
     a.sh2 = h->sh2_32;
+    a.stiff_list = h->stiff_list; a.stiff_count = h->dtred + 5;
     a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
     // how stiff cells start their implicit solve: the network, the
     // frozen-rate Newton start, or the bisection alone
@@ -519,10 +522,12 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, !(h->sh2_valid && !inflow), h->stream));
     h->sh2_valid = true;
     CK(source_fp32(a, stiff_mode, h->stream));
+    h->launches += stiff_mode ? 1 : 0;   // the stiff-cell kernel
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, false, h->stream));
     CK(source_fp32(a, stiff_mode, h->stream));
+    h->launches += stiff_mode ? 1 : 0;
     return MHD_OK;
   }
   SourceArgs a{};

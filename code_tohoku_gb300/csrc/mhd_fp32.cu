@@ -210,36 +210,32 @@ cudaError_t source_fp32(const Source32Args &a, int stiff_mode, cudaStream_t s) {
   // network and the Newton start model the KI function; mhd_create refuses
   // the combinations)
   if (a.ph.ifchem == 2) {
-    source32_kernel<true><<<nb, 128, 0, s>>>(a);
+    source32_kernel<true, false><<<nb, 128, 0, s>>>(a);
     return cudaGetLastError();
   }
   if (stiff_mode == 0) {
-    source32_kernel<false><<<nb, 128, 0, s>>>(a);
+    source32_kernel<false, false><<<nb, 128, 0, s>>>(a);
     return cudaGetLastError();
   }
-  // a persistent grid: as many 256-cell CTAs as fit at once (for the
-  // network at most four per SM, so their TMEM columns (128 each) fit in
-  // the SM's 512; its launch bounds allow three)
-  int dev = 0, sms = 0, per_sm = 0;
+  // guess and polish: the explicit cells in a full-occupancy pass that lists
+  // the stiff ones, then the stiff cells in dense tiles
+  if (!a.stiff_list || !a.stiff_count || (stiff_mode == STIFF_NETWORK && !a.W)) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(a.stiff_count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  source32_kernel<false, true><<<(unsigned)((n + kSourceDeferThreads - 1) / kSourceDeferThreads),
+                                 kSourceDeferThreads, 0, s>>>(a);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // a persistent grid over the list, at most three 256-cell CTAs per SM (the
+  // launch bounds; with the network their TMEM, 128 columns each, fits in
+  // the SM's 512); CTAs beyond the list's length return at once
+  int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long tiles = (n + kFusedThreads - 1) / kFusedThreads;
-  cudaError_t e;
-  if (stiff_mode == STIFF_NETWORK) {
-    if (!a.W) return cudaErrorInvalidValue;
-    const size_t smem = sizeof(SurTileSmem<kFusedTiles>);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, source32_fused_kernel<STIFF_NETWORK>, kFusedThreads,
-                                                      smem);
-    if (e != cudaSuccess) return e;
-    per_sm = per_sm < 4 ? per_sm : 4;
-    const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)std::max(per_sm, 1) * sms);
-    source32_fused_kernel<STIFF_NETWORK><<<grid, kFusedThreads, smem, s>>>(a);
-  } else {
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, source32_fused_kernel<STIFF_NEWTON>, kFusedThreads, 0);
-    if (e != cudaSuccess) return e;
-    const unsigned grid = (unsigned)std::min<long long>(tiles, (long long)std::max(per_sm, 1) * sms);
-    source32_fused_kernel<STIFF_NEWTON><<<grid, kFusedThreads, 0, s>>>(a);
-  }
+  const unsigned grid = (unsigned)std::min<long long>((n + kFusedThreads - 1) / kFusedThreads, 3LL * sms);
+  if (stiff_mode == STIFF_NETWORK)
+    source32_stiff_kernel<STIFF_NETWORK><<<grid, kFusedThreads, sizeof(SurTileSmem<kFusedTiles>), s>>>(a);
+  else
+    source32_stiff_kernel<STIFF_NEWTON><<<grid, kFusedThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -63,6 +63,8 @@ struct Source32Args {
   const SurNet *W;                 // surrogate network (null: none)
   float tol;                       // residual tolerance for accepting a polished guess
   const float *sh2;                // S = H+p+He+He+ and H2 of every cell (temp32), or null
+  int *stiff_list;                 // guess-and-polish modes: the stiff cells left to the second kernel
+  unsigned long long *stiff_count; // their number (zeroed before each pass)
 };
 
 // How a stiff cell's implicit solve starts when it does not go straight to
@@ -71,8 +73,11 @@ struct Source32Args {
 // implicit update P_b / (1 + c Lambda_b / P_b) (the explicit update when
 // Lambda_b heats).
 enum : int { STIFF_NETWORK = 1, STIFF_NEWTON = 2 };
-constexpr int kFusedTiles = 2;                  // 128-cell tiles per CTA of the fused SOURCE
+constexpr int kFusedTiles = 2;                  // 128-cell tiles per CTA of the stiff-cell kernel
 constexpr int kFusedThreads = 128 * kFusedTiles;
+// block size of the explicit pass that lists the stiff cells (one list
+// append per block)
+constexpr int kSourceDeferThreads = 512;
 
 }  // namespace mhd
 
@@ -216,17 +221,46 @@ __device__ __noinline__ float imc32_cell(const Cell32<CHEM> &c) {
   else return imc32(c.basef, c.nkbi, cc, [&](float T) { return fcool_ki(T, c.NN); });
 }
 
-// Thread per cell, the bisection for stiff cells (exact cooling).  CHEM:
-// the species cooling function (ifchem = 2) instead of the KI one.
-template <bool CHEM>
-__global__ void __launch_bounds__(128) source32_kernel(Source32Args A) {
+// Thread per cell.  CHEM: the species cooling function (ifchem = 2) instead
+// of the KI one.  DEFER (a guess-and-polish mode): stiff cells are appended
+// to A.stiff_list and left to source32_stiff_kernel, so this pass keeps the
+// registers and occupancy of the explicit update; otherwise they are
+// solved here by the bisection.
+template <bool CHEM, bool DEFER>
+__global__ void __launch_bounds__(DEFER ? kSourceDeferThreads : 128) source32_kernel(Source32Args A) {
   const Grid &g = A.g;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = t < (long long)g.n[0] * g.n[1] * g.n[2];
   const Cell32<CHEM> c = source32_prep<CHEM>(A, valid ? t : 0);
+  const bool stiff = valid && c.stiff;
+  if constexpr (DEFER) {
+    // block-aggregated append of the stiff cells' indices: one atomic per
+    // block on the shared counter; a block without stiff cells passes one
+    // barrier only
+    if (__syncthreads_or(stiff)) {
+      __shared__ unsigned wcnt[kSourceDeferThreads / 32];
+      __shared__ unsigned long long bbase;
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      const unsigned m = __ballot_sync(0xffffffffu, stiff);
+      if (lane == 0) wcnt[w] = __popc(m);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned tot = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) tot += wcnt[q];
+        bbase = atomicAdd(A.stiff_count, (unsigned long long)tot);
+      }
+      __syncthreads();
+      if (stiff) {
+        unsigned long long pos = bbase;
+        for (int q = 0; q < w; q++) pos += wcnt[q];
+        A.stiff_list[pos + __popc(m & ((1u << lane) - 1u))] = (int)t;
+      }
+    }
+    if (!valid || stiff) return;
+  }
   if (!valid) return;
   float dp_cool;
-  if (!c.stiff) {
+  if (!stiff) {
     dp_cool = -(c.g1 * c.CooL * c.dts);
   } else {
     dp_cool = imc32_cell<CHEM>(c) - c.basef;
@@ -253,71 +287,64 @@ __device__ __forceinline__ bool polish_accept(const Source32Args &A, const Cell3
   return true;
 }
 
-// SOURCE with the KI cooling when the stiff cells start from a guess: one
-// persistent kernel over blocks of 256 cells (thread per cell).  Explicit
-// cells update at once; when a block holds stiff cells, its threads form
-// the guess -- MODE STIFF_NETWORK: the surrogate network on the tensor cores
-// for the whole block (sur_tile_forward; the weights are staged and TMEM is
-// allocated by the first such block of the CTA), inputs outside the
-// training box going straight to the bisection -- then polish and test it,
-// and the rejected cells take the bisection.  Counters: sur_count accepted
-// guesses, fb_count rejected ones, imc_count every bisection.
+// The stiff cells listed by source32_kernel<false, true> (KI cooling), in
+// dense blocks of 256 list entries (thread per cell, two 128-cell tiles):
+// each thread forms its cell's guess -- MODE STIFF_NETWORK: the surrogate
+// network on the tensor cores for the whole block (sur_tile_forward; the
+// weights are staged and TMEM allocated once per CTA, and a CTA without
+// list entries returns before either), inputs outside the training box
+// going straight to the bisection -- then polishes and tests it, and the
+// rejected cells take the bisection.  A persistent grid strides over the
+// list.  Counters: sur_count accepted guesses, fb_count rejected ones,
+// imc_count every bisection.
 template <int MODE>
-__global__ void __launch_bounds__(kFusedThreads, 3) source32_fused_kernel(Source32Args A) {
-  extern __shared__ __align__(128) unsigned char fused_smem[];
+__global__ void __launch_bounds__(kFusedThreads, 3) source32_stiff_kernel(Source32Args A) {
+  extern __shared__ __align__(128) unsigned char stiff_smem[];
   using Tile = SurTileSmem<kFusedTiles>;
-  Tile *s = reinterpret_cast<Tile *>(fused_smem);
-  const long long ncells = (long long)A.g.n[0] * A.g.n[1] * A.g.n[2];
-  const long long step = (long long)gridDim.x * kFusedThreads;
+  Tile *s = reinterpret_cast<Tile *>(stiff_smem);
+  const long long cnt = (long long)*A.stiff_count;
+  if ((long long)blockIdx.x * kFusedThreads >= cnt) return;   // the whole CTA: no list entry for it
+  if constexpr (MODE == STIFF_NETWORK) sur_tile_setup<kFusedTiles>(A.W, s);
   const int lane = threadIdx.x & 31;
-  bool ready = false;   // the same on every thread (set under a block-wide condition)
   uint32_t phase = 0;
-  for (long long t0 = (long long)blockIdx.x * kFusedThreads; t0 < ncells; t0 += step) {
-    const long long t = t0 + threadIdx.x;
-    const bool valid = t < ncells;
-    const Cell32<false> c = source32_prep<false>(A, valid ? t : t0);
-    const bool stiff = valid && c.stiff;
-    float dp_cool = -(c.g1 * c.CooL * c.dts);
-    if (__syncthreads_or(stiff)) {
-      const float Tb = c.basef * c.nkbi;   // temperature the implicit solve starts from
-      const float Lb = fcool_ki(Tb, c.NN);
-      const float cc = c.dts * c.g1;
-      bool use = stiff;
-      float P;
-      if constexpr (MODE == STIFF_NETWORK) {
-        if (!ready) {
-          sur_tile_setup<kFusedTiles>(A.W, s);
-          ready = true;
-        }
-        const float rr = cc * fabsf(Lb) / c.basef;
-        const float x0 = log10f(c.NN), x1 = log10f(Tb), x2 = log10f(fmaxf(rr, 1e-30f));
-        const bool inbox = stiff && x0 >= -2.0f && x0 <= 5.0f && x1 >= -2.0f && x1 <= 1.30103f && x2 >= -3.0f &&
-                           x2 <= 3.0f;
-        float y0 = 0.0f, y1 = 0.0f;
-        const bool ok = sur_tile_forward<kFusedTiles>(s, inbox ? (x0 - SUR_C0) / SUR_S0 : 0.0f,
-                                                      inbox ? (x1 - SUR_C1) / SUR_S1 : 0.0f,
-                                                      inbox ? (x2 - SUR_C2) / SUR_S2 : 0.0f, phase, y0, y1);
-        if (!ok && threadIdx.x == 0) flag(A.err, ERRB_TC);
-        use = inbox && ok;
-        P = (Tb * exp10f(y0)) / c.nkbi;
-      } else {
-        P = Lb > 0.0f ? c.basef / (1.0f + cc * Lb / c.basef) : c.basef - cc * Lb;
-      }
-      const bool acc = use && polish_accept(A, c, P, &dp_cool);
-      const unsigned mu = __ballot_sync(0xffffffffu, use), ma = __ballot_sync(0xffffffffu, acc);
-      const unsigned mb = __ballot_sync(0xffffffffu, stiff && !acc);
-      if (lane == 0) {
-        if (ma) atomicAdd(A.sur_count, (unsigned long long)__popc(ma));
-        if (mu & ~ma) atomicAdd(A.fb_count, (unsigned long long)__popc(mu & ~ma));
-        if (mb) atomicAdd(A.imc_count, (unsigned long long)__popc(mb));
-      }
-      if (stiff && !acc) dp_cool = imc32_cell<false>(c) - c.basef;
+  for (long long e0 = (long long)blockIdx.x * kFusedThreads; e0 < cnt; e0 += (long long)gridDim.x * kFusedThreads) {
+    const long long e = e0 + threadIdx.x;
+    const bool on = e < cnt;
+    const Cell32<false> c = source32_prep<false>(A, A.stiff_list[on ? e : e0]);
+    const float Tb = c.basef * c.nkbi;   // temperature the implicit solve starts from
+    const float Lb = fcool_ki(Tb, c.NN);
+    const float cc = c.dts * c.g1;
+    bool use = on;
+    float P;
+    if constexpr (MODE == STIFF_NETWORK) {
+      const float rr = cc * fabsf(Lb) / c.basef;
+      const float x0 = log10f(c.NN), x1 = log10f(Tb), x2 = log10f(fmaxf(rr, 1e-30f));
+      const bool inbox = on && x0 >= -2.0f && x0 <= 5.0f && x1 >= -2.0f && x1 <= 1.30103f && x2 >= -3.0f &&
+                         x2 <= 3.0f;
+      float y0 = 0.0f, y1 = 0.0f;
+      const bool ok = sur_tile_forward<kFusedTiles>(s, inbox ? (x0 - SUR_C0) / SUR_S0 : 0.0f,
+                                                    inbox ? (x1 - SUR_C1) / SUR_S1 : 0.0f,
+                                                    inbox ? (x2 - SUR_C2) / SUR_S2 : 0.0f, phase, y0, y1);
+      if (!ok && threadIdx.x == 0) flag(A.err, ERRB_TC);
+      use = inbox && ok;
+      P = (Tb * exp10f(y0)) / c.nkbi;
+    } else {
+      P = Lb > 0.0f ? c.basef / (1.0f + cc * Lb / c.basef) : c.basef - cc * Lb;
     }
-    if (valid) source32_finish<false>(A, c, dp_cool);
+    float dp_cool = 0.0f;
+    const bool acc = use && polish_accept(A, c, P, &dp_cool);
+    const unsigned mu = __ballot_sync(0xffffffffu, use), ma = __ballot_sync(0xffffffffu, acc);
+    const unsigned mb = __ballot_sync(0xffffffffu, on && !acc);
+    if (lane == 0) {
+      if (ma) atomicAdd(A.sur_count, (unsigned long long)__popc(ma));
+      if (mu & ~ma) atomicAdd(A.fb_count, (unsigned long long)__popc(mu & ~ma));
+      if (mb) atomicAdd(A.imc_count, (unsigned long long)__popc(mb));
+    }
+    if (!on) continue;
+    if (!acc) dp_cool = imc32_cell<false>(c) - c.basef;
+    source32_finish<false>(A, c, dp_cool);
   }
-  if constexpr (MODE == STIFF_NETWORK) {
-    if (ready) sur_tile_teardown<kFusedTiles>(s, phase);
-  }
+  if constexpr (MODE == STIFF_NETWORK) sur_tile_teardown<kFusedTiles>(s, phase);
 }
 
 // dt for the chosen form, first of two kernels: an FP32 screen of every
@@ -325,11 +352,11 @@ __global__ void __launch_bounds__(kFusedThreads, 3) source32_fused_kernel(Source
 // (the CFL minimum stays FP64): this kernel computes the Courant limit
 // (:1912-1930) and the two thermal limits of Stblty (:2784-2822) of each
 // cell in FP32 together with an interval that surely holds the FP64 value,
-// [v (1 - eta), v (1 + eta)] with eta = 2^-10, far wider than the FP32
-// rounding of these products, sums and quotients of positive terms; the
-// cooling time divides by |Lambda|, a difference of cooling and heating, so
-// its interval widens |Lambda| by 2^-8 of the sum of the terms' magnitudes
-// (and is unbounded above where that covers 0).  The floor 2.5e-4 of the
+// [v (1 - eta), v (1 + eta)] (eta below, far wider than the FP32 rounding
+// of these products, sums and quotients of positive terms); the cooling
+// time divides by |Lambda|, a difference of cooling and heating, so its
+// interval widens |Lambda| by a fraction of the sum of the terms'
+// magnitudes (and is unbounded above where that covers 0).  The floor 2.5e-4 of the
 // cooling time is exact: a cell whose interval lies below it has the floor
 // as its FP64 value.  Each warp stores the lower ends of its three limits;
 // the block minima of the upper ends go to words[0..2] (non-negative floats
@@ -341,8 +368,15 @@ struct DtScreen {
   unsigned *words;    // [0..2] smallest upper ends (float bits), [3] a cooling time at the floor
   int nwarps;
 };
-constexpr float kDtEta = 1.0f / 1024.0f;
-constexpr float kDtEtaCool = 1.0f / 256.0f;
+// The FP32 rounding of these quantities stays below ~1e-6 relative (inputs
+// rounded once, IEEE quotients, the approximate square root): eta = 2^-14
+// is 60 times that.  The KI cooling terms carry the exponential's
+// argument error (|arg| x a few ulp, up to ~1e-5 where the term matters):
+// 2^-12 of their magnitude sum; the species function's powers and
+// logarithms: 2^-8.
+constexpr float kDtEta = 1.0f / 16384.0f;
+constexpr float kDtEtaCoolKI = 1.0f / 4096.0f;
+constexpr float kDtEtaCoolSpecies = 1.0f / 256.0f;
 
 __global__ void __launch_bounds__(256) dt32_screen_kernel(Grid g, Phys ph, Fields f, const float *sh2, DtScreen sc,
                                                           int *err) {
@@ -391,7 +425,8 @@ __global__ void __launch_bounds__(256) dt32_screen_kernel(Grid g, Phys ph, Field
       float CooL = (ph.ifchem == 2)
                        ? fcool_species<float>(Tn, cell_species<float>(f, a, [](double v) { return d2f(v); }), &mag)
                        : fcool_ki_mag(Tn, rho * (1.0f / 1.27f), mag);
-      const float ac = fabsf(CooL), e = kDtEtaCool * mag, num = 0.2f * p5;
+      const float ac = fabsf(CooL), num = 0.2f * p5;
+      const float e = (ph.ifchem == 2 ? kDtEtaCoolSpecies : kDtEtaCoolKI) * mag;
       const float tlo = __fdiv_rn(num, g1c * (ac + e)) * dn;
       const float thi = ac > e ? __fdiv_rn(num, g1c * (ac - e)) * up : INF;
       // the floor of the cooling time, bracketed in FP32
