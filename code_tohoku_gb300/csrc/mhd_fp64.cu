@@ -4,6 +4,7 @@
 // detmath.h transcendentals the GPU result is bit-identical to the CPU.
 // It also holds the precision-independent kernels (ghosts, CT face update,
 // source, dt, DISSIP, diagnostics).
+#include <algorithm>
 #define MHD_COMMON_KERNELS
 #include "mhd_sweep_impl.cuh"
 
@@ -104,7 +105,13 @@ cudaError_t dt_reduce(const Grid &g, const Phys &ph, const Fields &f, unsigned l
 cudaError_t dt_refine(const Grid &g, const Phys &ph, const Fields &f, const float *lo, const unsigned *words,
                       unsigned long long *out, cudaStream_t s) {
   long long n = (long long)g.n[0] * g.n[1] * g.n[2];
-  dt_refine_kernel<<<nblk(n, 256), 256, 0, s>>>(g, ph, f, lo, words, (int)((n + 31) / 32), out);
+  const int nwarps = (int)((n + 31) / 32);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // eight 256-thread blocks per SM at most, fewer for small grids
+  const unsigned blocks = (unsigned)std::min<long long>((nwarps + 7) / 8, 8LL * (sms > 0 ? sms : 1));
+  dt_refine_kernel<<<blocks, 256, 0, s>>>(g, ph, f, lo, words, nwarps, out);
   return cudaGetLastError();
 }
 

@@ -1347,28 +1347,39 @@ __global__ void dt_kernel(Grid g, Phys ph, Fields f, unsigned long long *out /* 
 // than some cell's, so the result is dt_kernel's bit for bit.  lo: [3][nwarps]
 // lower ends (c, tau, alpha); words[0..2]: smallest upper ends as float bits,
 // words[3]: some cooling time is at its floor, whose FP64 value the host adds.
+// A capped grid: each warp strides over the screen's warps (launching one
+// block per 256 cells spent ~0.2 ms at 256^3 scheduling blocks that find
+// nothing to do).
 __global__ void __launch_bounds__(256) dt_refine_kernel(Grid g, Phys ph, Fields f, const float *lo,
                                                         const unsigned *words, int nwarps,
                                                         unsigned long long *out /* [0]=tCFL [1]=tLMT */) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long w = t >> 5;
-  if (w >= nwarps) return;   // whole warps
-  bool cand = lo[w] <= __uint_as_float(words[0]);
-  if (ph.ifthrm == 2) {
-    cand = cand || lo[2 * nwarps + w] <= __uint_as_float(words[2]);
-    if (!words[3]) cand = cand || lo[nwarps + w] <= __uint_as_float(words[1]);
+  const float mc = __uint_as_float(words[0]), mt = __uint_as_float(words[1]), ma = __uint_as_float(words[2]);
+  const bool thermal = ph.ifthrm == 2, floored = words[3] != 0;
+  const long long ncells = (long long)g.n[0] * g.n[1] * g.n[2];
+  const int lane = threadIdx.x & 31;
+  const long long nw_grid = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned long long cb = ~0ull, sb = ~0ull;
+  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += nw_grid) {
+    bool cand = lo[w] <= mc;
+    if (thermal) {
+      cand = cand || lo[2 * (long long)nwarps + w] <= ma;
+      if (!floored) cand = cand || lo[(long long)nwarps + w] <= mt;
+    }
+    if (!cand) continue;       // the same for every lane of the warp
+    const long long t = 32 * w + lane;
+    double c_min = ph.tfinal, s_min = ph.tfinal;
+    if (t < ncells) cell_dt_limits(g, ph, f, t, c_min, s_min);
+    const unsigned long long c1 = dbits(c_min > 0.0 ? c_min : 0.0), s1 = dbits(s_min > 0.0 ? s_min : 0.0);
+    cb = c1 < cb ? c1 : cb;
+    sb = s1 < sb ? s1 : sb;
   }
-  if (!cand) return;         // the same for every lane of the warp
-  double c_min = ph.tfinal, s_min = ph.tfinal;
-  if (t < (long long)g.n[0] * g.n[1] * g.n[2]) cell_dt_limits(g, ph, f, t, c_min, s_min);
-  unsigned long long cb = dbits(c_min > 0.0 ? c_min : 0.0), sb = dbits(s_min > 0.0 ? s_min : 0.0);
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long c2 = __shfl_xor_sync(0xffffffffu, cb, o);
     unsigned long long s2 = __shfl_xor_sync(0xffffffffu, sb, o);
     cb = c2 < cb ? c2 : cb;
     sb = s2 < sb ? s2 : sb;
   }
-  if ((threadIdx.x & 31) == 0) {
+  if (lane == 0 && cb != ~0ull) {
     atomicMin(&out[0], cb);
     atomicMin(&out[1], sb);
   }
