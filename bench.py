@@ -70,6 +70,8 @@ def parse():
                     help="FP64 steps of the accuracy comparison (the chosen form runs to the same time)")
     ap.add_argument("--no-config2", action="store_true", help="skip the 128^3 turbulence sub-run")
     ap.add_argument("--no-config5", action="store_true", help="skip the 512^3 sub-run")
+    ap.add_argument("--stiff-only", action="store_true",
+                    help="train the surrogate and run only the stiff-cooling comparison (prints that object)")
     ap.add_argument("--sur-steps", type=int, default=2000)
     ap.add_argument("--sur-data", type=int, default=1 << 24)
     return ap.parse_args()
@@ -354,7 +356,111 @@ def main():
         hi = n_ - 1 if state.params.bc[1] == 1 else n_
         return float(a.max()), float(a[:, :, lo:hi].max())
 
+    def stiff_comparison():
+        # The stiff regime of KI cooling, where the learned part works: the same
+        # colliding flow at 30x the density (n = 30 cm^-3) and SOURCE(dt) with
+        # dt = 0.05 Myr, longer than the cooling time of most cells.  SOURCE only,
+        # from the same uploaded state each time; the FP64 form gives the
+        # reference pressure.
+        sst = problems.colliding_flows(args.n)
+        sst.U[0] *= 30.0
+        sst.species *= 30.0
+        sdt = 0.05
+        stiff = {"state": "colliding flow at 30x density", "dt": sdt}
+        p_ref = None
+        for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
+                                 ("fp32_exact", native.PREC_FP32, native.COOL_EXACT),
+                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE),
+                                 ("fp32_newton_no_network", native.PREC_FP32, native.COOL_NEWTON)):
+            gs = native.Mhd3D(sst.params, precision=prec, cooling=cool, device=dev)
+            gs.set_stream(stream.cuda_stream)
+            if cool == native.COOL_SURROGATE:
+                gs.surrogate_load(sur_params, 1e-3)
+            times = []
+            for _ in range(3):
+                gs.upload(sst)
+                gs.reset_counters()
+                barrier()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                gs.source(sdt)
+                b.record(stream)
+                barrier()
+                times.append(a.elapsed_time(b))
+            d = gs.diagnostics()
+            pp = gs.download(with_bcc=False)[0][4][2:-2, 2:-2, 2:-2]
+            if p_ref is None:
+                p_ref = pp
+            stiff[name] = {"ms_per_source": min(times), "bisection_cells": d["imc_cells"],
+                           "guess_accepted_cells": d["surrogate_cells"], "guess_rejected_cells": d["fallback_cells"],
+                           "l1_p_vs_fp64": float(np.abs(pp - p_ref).mean() / np.abs(p_ref).mean())}
+            del gs
+        stiff["surrogate_speedup_vs_fp32_exact"] = (stiff["fp32_exact"]["ms_per_source"] /
+                                                    stiff["fp32_surrogate"]["ms_per_source"])
+        stiff["surrogate_speedup_vs_newton_no_network"] = (stiff["fp32_newton_no_network"]["ms_per_source"] /
+                                                           stiff["fp32_surrogate"]["ms_per_source"])
+        for k in ("fp32_surrogate", "fp32_newton_no_network"):
+            r = stiff[k]
+            r["fallback_fraction"] = r["guess_rejected_cells"] / max(1, r["guess_rejected_cells"] + r["guess_accepted_cells"])
+
+        # The same solvers inside whole steps: the colliding flow at 3000x the
+        # density (n = 3000 cm^-3 at 6000 K cools in ~4e-4 Myr), where the
+        # reference's own time-step control leaves the cells stiff (the
+        # cooling-time limit 0.2 t_cool is floored at 2.5e-4 Myr, Stblty
+        # :2806).  At 30x the step's dt follows 0.2 t_cool and no cell is
+        # stiff; hence this density.  Steps 1..K from the uploaded state, each
+        # event-timed; FP64 runs the same steps for the error.
+        kst = 4
+        wst = problems.colliding_flows(args.n)
+        wst.U[0] *= 3000.0
+        wst.species *= 3000.0
+        wst.U[4] *= 3000.0          # the same 6000 K
+        steps_stiff = {"state": "colliding flow at 3000x density, 6000 K", "steps": kst}
+        u_ref = None
+        for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
+                                 ("fp32_exact", native.PREC_FP32, native.COOL_EXACT),
+                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE),
+                                 ("fp32_newton_no_network", native.PREC_FP32, native.COOL_NEWTON)):
+            gs = native.Mhd3D(wst.params, precision=prec, cooling=cool, device=dev)
+            gs.set_stream(stream.cuda_stream)
+            if cool == native.COOL_SURROGATE:
+                gs.surrogate_load(sur_params, 1e-3)
+            gs.upload(wst)
+            gs.reset_counters()
+            rec = {}
+            barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dts = []
+            gs.ifevo = 1
+            for _ in range(kst):
+                dts.append(step_timed(gs, rec, wst.params.dissip))
+            e1.record(stream)
+            barrier()
+            d = gs.diagnostics()
+            U = gs.download(with_bcc=False)[0]
+            c = (slice(2, -2),) * 3
+            if u_ref is None:
+                u_ref = (U[0][c].copy(), U[4][c].copy())
+            steps_stiff[name] = {"ms_per_step": e0.elapsed_time(e1) / kst, "phase_ms": phase_ms(rec), "dt": dts,
+                                 "bisection_cells": d["imc_cells"], "guess_accepted_cells": d["surrogate_cells"],
+                                 "guess_rejected_cells": d["fallback_cells"],
+                                 "l1_rho_vs_fp64": float(np.abs(U[0][c] - u_ref[0]).mean() / np.abs(u_ref[0]).mean()),
+                                 "l1_p_vs_fp64": float(np.abs(U[4][c] - u_ref[1]).mean() / np.abs(u_ref[1]).mean())}
+            del gs
+        steps_stiff["surrogate_speedup_vs_fp32_exact"] = (steps_stiff["fp32_exact"]["ms_per_step"] /
+                                                          steps_stiff["fp32_surrogate"]["ms_per_step"])
+        stiff["whole_steps"] = steps_stiff
+        return stiff
+
     hbm, which = peaks()
+    if args.stiff_only:
+        stiff = stiff_comparison()
+        if rank == 0:
+            print(json.dumps({"stiff_cooling_source": stiff, "n": args.n}), flush=True)
+        return
     # chosen form: FP32 reconstruction/flux + FP64 accumulation + surrogate
     g32, ms32, ph32, launches32, clocks = timed_run(native.PREC_FP32, native.COOL_SURROGATE)
     d32 = g32.diagnostics()
@@ -450,104 +556,8 @@ def main():
            "ms_per_step_median": e2e_s * 1e3, "ms_per_step_mean": float(np.mean(e2e_ms)),
            "samples_ms": [round(x, 2) for x in e2e_ms]}
 
-    # The stiff regime of KI cooling, where the learned part works: the same
-    # colliding flow at 30x the density (n = 30 cm^-3) and SOURCE(dt) with
-    # dt = 0.05 Myr, longer than the cooling time of most cells.  SOURCE only,
-    # from the same uploaded state each time; the FP64 form gives the
-    # reference pressure.
-    stiff = None
-    if not args.no_stiff:
-        sst = problems.colliding_flows(args.n)
-        sst.U[0] *= 30.0
-        sst.species *= 30.0
-        sdt = 0.05
-        stiff = {"state": "colliding flow at 30x density", "dt": sdt}
-        p_ref = None
-        for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
-                                 ("fp32_exact", native.PREC_FP32, native.COOL_EXACT),
-                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE),
-                                 ("fp32_newton_no_network", native.PREC_FP32, native.COOL_NEWTON)):
-            gs = native.Mhd3D(sst.params, precision=prec, cooling=cool, device=dev)
-            gs.set_stream(stream.cuda_stream)
-            if cool == native.COOL_SURROGATE:
-                gs.surrogate_load(sur_params, 1e-3)
-            times = []
-            for _ in range(3):
-                gs.upload(sst)
-                gs.reset_counters()
-                barrier()
-                a = torch.cuda.Event(enable_timing=True)
-                b = torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                gs.source(sdt)
-                b.record(stream)
-                barrier()
-                times.append(a.elapsed_time(b))
-            d = gs.diagnostics()
-            pp = gs.download(with_bcc=False)[0][4][2:-2, 2:-2, 2:-2]
-            if p_ref is None:
-                p_ref = pp
-            stiff[name] = {"ms_per_source": min(times), "bisection_cells": d["imc_cells"],
-                           "guess_accepted_cells": d["surrogate_cells"], "guess_rejected_cells": d["fallback_cells"],
-                           "l1_p_vs_fp64": float(np.abs(pp - p_ref).mean() / np.abs(p_ref).mean())}
-            del gs
-        stiff["surrogate_speedup_vs_fp32_exact"] = (stiff["fp32_exact"]["ms_per_source"] /
-                                                    stiff["fp32_surrogate"]["ms_per_source"])
-        stiff["surrogate_speedup_vs_newton_no_network"] = (stiff["fp32_newton_no_network"]["ms_per_source"] /
-                                                           stiff["fp32_surrogate"]["ms_per_source"])
-        for k in ("fp32_surrogate", "fp32_newton_no_network"):
-            r = stiff[k]
-            r["fallback_fraction"] = r["guess_rejected_cells"] / max(1, r["guess_rejected_cells"] + r["guess_accepted_cells"])
+    stiff = None if args.no_stiff else stiff_comparison()
 
-        # The same solvers inside whole steps: the colliding flow at 3000x the
-        # density (n = 3000 cm^-3 at 6000 K cools in ~4e-4 Myr), where the
-        # reference's own time-step control leaves the cells stiff (the
-        # cooling-time limit 0.2 t_cool is floored at 2.5e-4 Myr, Stblty
-        # :2806).  At 30x the step's dt follows 0.2 t_cool and no cell is
-        # stiff; hence this density.  Steps 1..K from the uploaded state, each
-        # event-timed; FP64 runs the same steps for the error.
-        kst = 4
-        wst = problems.colliding_flows(args.n)
-        wst.U[0] *= 3000.0
-        wst.species *= 3000.0
-        wst.U[4] *= 3000.0          # the same 6000 K
-        steps_stiff = {"state": "colliding flow at 3000x density, 6000 K", "steps": kst}
-        u_ref = None
-        for name, prec, cool in (("fp64", native.PREC_FP64, native.COOL_EXACT),
-                                 ("fp32_exact", native.PREC_FP32, native.COOL_EXACT),
-                                 ("fp32_surrogate", native.PREC_FP32, native.COOL_SURROGATE),
-                                 ("fp32_newton_no_network", native.PREC_FP32, native.COOL_NEWTON)):
-            gs = native.Mhd3D(wst.params, precision=prec, cooling=cool, device=dev)
-            gs.set_stream(stream.cuda_stream)
-            if cool == native.COOL_SURROGATE:
-                gs.surrogate_load(sur_params, 1e-3)
-            gs.upload(wst)
-            gs.reset_counters()
-            rec = {}
-            barrier()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            dts = []
-            gs.ifevo = 1
-            for _ in range(kst):
-                dts.append(step_timed(gs, rec, wst.params.dissip))
-            e1.record(stream)
-            barrier()
-            d = gs.diagnostics()
-            U = gs.download(with_bcc=False)[0]
-            c = (slice(2, -2),) * 3
-            if u_ref is None:
-                u_ref = (U[0][c].copy(), U[4][c].copy())
-            steps_stiff[name] = {"ms_per_step": e0.elapsed_time(e1) / kst, "phase_ms": phase_ms(rec), "dt": dts,
-                                 "bisection_cells": d["imc_cells"], "guess_accepted_cells": d["surrogate_cells"],
-                                 "guess_rejected_cells": d["fallback_cells"],
-                                 "l1_rho_vs_fp64": float(np.abs(U[0][c] - u_ref[0]).mean() / np.abs(u_ref[0]).mean()),
-                                 "l1_p_vs_fp64": float(np.abs(U[4][c] - u_ref[1]).mean() / np.abs(u_ref[1]).mean())}
-            del gs
-        steps_stiff["surrogate_speedup_vs_fp32_exact"] = (steps_stiff["fp32_exact"]["ms_per_step"] /
-                                                          steps_stiff["fp32_surrogate"]["ms_per_step"])
-        stiff["whole_steps"] = steps_stiff
 
     def drift(d0, d1, scale):
         """Mass and momentum change over a run; momentum relative to the sum
