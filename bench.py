@@ -70,6 +70,7 @@ def parse():
                     help="FP64 steps of the accuracy comparison (the chosen form runs to the same time)")
     ap.add_argument("--no-config2", action="store_true", help="skip the 128^3 turbulence sub-run")
     ap.add_argument("--no-config5", action="store_true", help="skip the 512^3 sub-run")
+    ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity timing")
     ap.add_argument("--stiff-only", action="store_true",
                     help="train the surrogate and run only the stiff-cooling comparison (prints that object)")
     ap.add_argument("--sur-steps", type=int, default=2000)
@@ -571,6 +572,18 @@ def main():
         dV = float(state.dx[2] * state.dy[2] * state.dz[2])
         return sum(float((state.U[0][c] * np.abs(state.U[q][c])).sum()) for q in (1, 2, 3)) * dV
 
+    # self-gravity (ifgrv = 2): the same chosen-form step with the potential
+    # solve and the two half kicks, against the step without them
+    grav = None
+    if not args.no_gravity:
+        sg = st.copy()
+        sg.params = st.params.replace(ifgrv=2)
+        gg, msg, phg, _, _ = timed_run(native.PREC_FP32, native.COOL_SURROGATE, state=sg, steps=5, warmup=args.warmup)
+        grav = {"workload": f"the headline problem with self-gravity, {args.n}^3", "steps": 5,
+                "ms_per_step_with_gravity": msg / 5, "ms_per_step_without": ms32 / args.steps,
+                "potential_solve": "radix-2 FFTs in y and z, a tridiagonal x solve per mode (FP64)"}
+        del gg
+
     # config 2: 128^3 decaying Mach-5 MHD turbulence, plain FP64, steps 1..100
     # at CFL 0.4 (the timed steps start from the initial state), and the
     # chosen form over the same steps; L1 at the FP64 run's final time
@@ -675,7 +688,7 @@ def main():
                             "note": "x boundaries are open (free): mass changes by the boundary flux, and the "
                                     "reference's face exchange rewrites face n+1, so only the cells next to a free "
                                     "x boundary carry a div B above round-off"},
-            "config2": config2, "config5": config5}
+            "config2": config2, "config5": config5, "self_gravity": grav}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)

@@ -10,6 +10,7 @@ into one shared library next to this file:
                     (--fmad=false: its FP64 labels match the CPU IMC bit for bit)
   csrc/mhd_noalloc.cu  the allocation-free time step
   csrc/mhd_peak.cu  the FP64 throughput measurement (the plain path's roofline)
+  csrc/mhd_gravity.cu  self-gravity: FFT + tridiagonal potential solve, the half kicks
   csrc/mhd_io.cpp   host code: the reference's output and restart files
 """
 import os
@@ -31,6 +32,7 @@ UNITS = {
     "mhd_surrogate.cu": ["--fmad=false"],
     "mhd_noalloc.cu": ["--fmad=false"],
     "mhd_peak.cu": [],
+    "mhd_gravity.cu": ["--fmad=false"],
     "mhd_io.cpp": [],
 }
 

@@ -55,6 +55,14 @@ struct mhd_handle {
   float *dtlo = nullptr;
   unsigned *dtwords = nullptr;
   float *dtf = nullptr;                  // BC=4 reservoir (device)
+  // self-gravity (ifgrv = 2): the potential, the complex work array, the
+  // Thomas scratch, the twiddles for ny and nz, and the grid scalars the
+  // solve and the kick read (from the last mhd_upload)
+  double *phi = nullptr;
+  void *gwork = nullptr;
+  double *gcp = nullptr;
+  void *gtw = nullptr;
+  double g_dx = 0.0, g_dy = 0.0, g_dz = 0.0, g_dx0 = 0.0, g_x0 = 0.0, g_lbox = 0.0;
   bool inflow_set = false;
   double *divv = nullptr;
   double *diag_part = nullptr;
@@ -160,6 +168,32 @@ int need_inflow(mhd_handle *h) {
   return MHD_OK;
 }
 
+// self-gravity (ifgrv = 2): GRAVTY mode 2 (the potential of the current
+// density) and mode 3 (a half kick of the velocities by its gradient)
+int gravity_potential(mhd_handle *h) {
+  GravityArgs a{};
+  a.g = h->g;
+  a.rho = h->f.U[0];
+  a.phi = h->phi;
+  a.w = static_cast<double2 *>(h->gwork);
+  a.cp = h->gcp;
+  a.tw_y = static_cast<const double2 *>(h->gtw);
+  a.tw_z = a.tw_y + (h->g.n[1] / 2 > 0 ? h->g.n[1] / 2 : 1) * 2;
+  a.dx = h->g_dx; a.dy = h->g_dy; a.dz = h->g_dz; a.x0 = h->g_x0; a.lbox = h->g_lbox;
+  CK(gravity_solve(a, h->stream));
+  h->launches += 9;    // ten kernels: the load, four transforms, the mode solve, the store, three ghost passes
+  return MHD_OK;
+}
+int gravity_half_kick(mhd_handle *h, double dt) {
+  CK(gravity_kick(h->g, h->f, h->phi, dt, h->g_dx0, h->stream));
+  return MHD_OK;
+}
+int gravity(mhd_handle *h, double dt, bool kick) {
+  TRY(gravity_potential(h));
+  if (kick) TRY(gravity_half_kick(h, dt));
+  return MHD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -178,6 +212,8 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   if (p->cooling != MHD_COOL_EXACT && p->precision != MHD_PREC_FP32) return MHD_ERR_ARG;
   if (p->ifchem != 0 && p->ifchem != 2) return MHD_ERR_ARG;
   if (p->ifrad != 0 && p->ifrad != 2) return MHD_ERR_ARG;
+  if (p->ifgrv != 0 && p->ifgrv != 2) return MHD_ERR_ARG;
+  if (p->ifgrv == 2 && !(gravity_size_ok(p->ny) && gravity_size_ok(p->nz))) return MHD_ERR_ARG;
   // the surrogate is trained on the KI cooling function only
   if (p->cooling != MHD_COOL_EXACT && p->ifchem == 2) return MHD_ERR_ARG;
   if (p->dissip && p->nx < 11) return MHD_ERR_ARG;
@@ -251,6 +287,23 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     }
     for (int q = 0; q < 10; q++) h->f.col[q] = h->colblock + (size_t)q * g.ncell;
   }
+  if (p->ifgrv == 2) {
+    const size_t nint = (size_t)g.n[0] * g.n[1] * g.n[2];
+    std::vector<double2> ty = gravity_twiddles(g.n[1]), tz = gravity_twiddles(g.n[2]);
+    bool okg = cudaMalloc(&h->phi, (size_t)g.ncell * sizeof(double)) == cudaSuccess &&
+               cudaMalloc(&h->gwork, nint * sizeof(double2)) == cudaSuccess &&
+               cudaMalloc(&h->gcp, nint * sizeof(double)) == cudaSuccess &&
+               cudaMalloc(&h->gtw, (ty.size() + tz.size()) * sizeof(double2)) == cudaSuccess &&
+               cudaMemcpy(h->gtw, ty.data(), ty.size() * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess &&
+               cudaMemcpy(static_cast<double2 *>(h->gtw) + ty.size(), tz.data(), tz.size() * sizeof(double2),
+                          cudaMemcpyHostToDevice) == cudaSuccess &&
+               cudaMemset(h->phi, 0, (size_t)g.ncell * sizeof(double)) == cudaSuccess;
+    if (!okg) {
+      cudaGetLastError();
+      mhd_destroy(h);
+      return MHD_ERR_CUDA;
+    }
+  }
   if (p->precision == MHD_PREC_FP32) {
     const size_t nf = 15;   // 14 FP32 arrays + the stiff-cell list of SOURCE
     size_t fbytes = nf * (size_t)g.ncell * sizeof(float);
@@ -313,6 +366,10 @@ int mhd_destroy(mhd_handle *h) {
   cudaFree(h->diag_part);
   cudaFree(h->dtred);
   cudaFree(h->dtlo);
+  cudaFree(h->phi);
+  cudaFree(h->gwork);
+  cudaFree(h->gcp);
+  cudaFree(h->gtw);
   cudaFree(h->err);
   cudaFree(h->sur_master);
   cudaFree(h->sur_net);
@@ -399,6 +456,13 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
   }
   CK(cell_b(h->g, h->f, h->stream));
   TRY(fill(h, {h->f.bcc[0], h->f.bcc[1], h->f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
+  if (h->p.ifgrv == 2) {
+    // GRAVTY(0,2) of INITIA (:481-484); index 2 of the coordinate arrays is
+    // cell 1, index 1 is x(0)
+    h->g_dx = dx[2]; h->g_dy = dy[2]; h->g_dz = dz[2]; h->g_dx0 = dx[1];
+    h->g_x0 = x[1]; h->g_lbox = x[g.n[0] + 1] - x[1];
+    TRY(gravity(h, 0.0, false));
+  }
   CKR(cudaStreamSynchronize(h->stream));
   h->uploaded = true;
   return MHD_OK;
@@ -411,6 +475,16 @@ int mhd_download_columns(mhd_handle *h, double *columns) {
   CKR(cudaSetDevice(h->p.device));
   CKR(cudaMemcpyAsync(columns, h->colblock, 10 * (size_t)h->g.ncell * sizeof(double), cudaMemcpyDeviceToHost,
                       h->stream));
+  CKR(cudaStreamSynchronize(h->stream));
+  return check_err(h);
+}
+
+int mhd_download_potential(mhd_handle *h, double *phi) {
+  if (!h || !phi) return MHD_ERR_ARG;
+  if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
+  if (h->p.ifgrv != 2) return fail(h, MHD_ERR_STATE, "the handle has no potential (ifgrv != 2)");
+  CKR(cudaSetDevice(h->p.device));
+  CKR(cudaMemcpyAsync(phi, h->phi, (size_t)h->g.ncell * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CKR(cudaStreamSynchronize(h->stream));
   return check_err(h);
 }
@@ -651,11 +725,13 @@ int mhd_advance(mhd_handle *h, double dt) {
   if (!h) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
+  if (h->p.ifgrv == 2) TRY(gravity_half_kick(h, dt));   // EVOLVE :607
   TRY(mhd_source(h, 0.5 * dt));
   for (int s = 0; s < 3; s++) TRY(mhd_sweep(h, orders[h->ifevo - 1][s], dt));
   h->ifevo = h->ifevo % 6 + 1;
   TRY(mhd_ct(h, dt));
   TRY(mhd_source(h, 0.5 * dt));
+  if (h->p.ifgrv == 2) TRY(gravity(h, dt, true));        // :653
   if (h->p.dissip) TRY(mhd_dissip(h));
   h->time = h->time + dt;
   h->steps++;
@@ -687,6 +763,7 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, 
   const size_t nc = (size_t)h->g.ncell, nb = nc * sizeof(double);
   Fields &f = h->f;
   static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
+  if (h->p.ifgrv == 2) TRY(gravity_half_kick(h, d));   // EVOLVE :607
   TRY(mhd_source(h, 0.5 * d));
   if (late_species) CKR(cudaStreamWaitEvent(h->stream, h->ev_io[2], 0));
   for (int q = 0; q < 3; q++) TRY(mhd_sweep(h, orders[h->ifevo - 1][q], d));
@@ -710,6 +787,7 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, 
   for (int q = 5; q < 8; q++)
     CKR(cudaMemcpyAsync(U_out + q * nc, f.U[q], nb, cudaMemcpyDeviceToHost, h->io_stream));
   TRY(source_impl(h, 0.5 * d, early));
+  if (h->p.ifgrv == 2) TRY(gravity(h, d, true));        // :653
   if (h->p.dissip) TRY(mhd_dissip(h));
   h->time = h->time + d;
   h->steps++;

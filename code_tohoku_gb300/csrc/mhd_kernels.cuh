@@ -1347,9 +1347,11 @@ __global__ void dt_kernel(Grid g, Phys ph, Fields f, unsigned long long *out /* 
 // than some cell's, so the result is dt_kernel's bit for bit.  lo: [3][nwarps]
 // lower ends (c, tau, alpha); words[0..2]: smallest upper ends as float bits,
 // words[3]: some cooling time is at its floor, whose FP64 value the host adds.
-// A capped grid: each warp strides over the screen's warps (launching one
-// block per 256 cells spent ~0.2 ms at 256^3 scheduling blocks that find
-// nothing to do).
+// A capped grid: each lane of a warp checks one of the screen's warps
+// (coalesced, independent loads of the three lower ends), the warp ballots
+// the candidates and recomputes their cells together; at 256^3 a thread per
+// screened cell, or a warp walking the screen's warps one at a time, spent
+// 0.2-0.3 ms on the checks alone.
 __global__ void __launch_bounds__(256) dt_refine_kernel(Grid g, Phys ph, Fields f, const float *lo,
                                                         const unsigned *words, int nwarps,
                                                         unsigned long long *out /* [0]=tCFL [1]=tLMT */) {
@@ -1359,19 +1361,25 @@ __global__ void __launch_bounds__(256) dt_refine_kernel(Grid g, Phys ph, Fields 
   const int lane = threadIdx.x & 31;
   const long long nw_grid = ((long long)gridDim.x * blockDim.x) >> 5;
   unsigned long long cb = ~0ull, sb = ~0ull;
-  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwarps; w += nw_grid) {
-    bool cand = lo[w] <= mc;
-    if (thermal) {
-      cand = cand || lo[2 * (long long)nwarps + w] <= ma;
-      if (!floored) cand = cand || lo[(long long)nwarps + w] <= mt;
+  const long long first = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+  for (long long wb = first; wb < nwarps; wb += 32 * nw_grid) {
+    const long long w = wb + lane;
+    bool cand = false;
+    if (w < nwarps) {
+      const float l0 = lo[w], l1 = lo[(long long)nwarps + w], l2 = lo[2 * (long long)nwarps + w];
+      cand = l0 <= mc || (thermal && (l2 <= ma || (!floored && l1 <= mt)));
     }
-    if (!cand) continue;       // the same for every lane of the warp
-    const long long t = 32 * w + lane;
-    double c_min = ph.tfinal, s_min = ph.tfinal;
-    if (t < ncells) cell_dt_limits(g, ph, f, t, c_min, s_min);
-    const unsigned long long c1 = dbits(c_min > 0.0 ? c_min : 0.0), s1 = dbits(s_min > 0.0 ? s_min : 0.0);
-    cb = c1 < cb ? c1 : cb;
-    sb = s1 < sb ? s1 : sb;
+    unsigned m = __ballot_sync(0xffffffffu, cand);
+    while (m) {                // the same on every lane
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const long long t = 32 * (wb + b) + lane;
+      double c_min = ph.tfinal, s_min = ph.tfinal;
+      if (t < ncells) cell_dt_limits(g, ph, f, t, c_min, s_min);
+      const unsigned long long c1 = dbits(c_min > 0.0 ? c_min : 0.0), s1 = dbits(s_min > 0.0 ? s_min : 0.0);
+      cb = c1 < cb ? c1 : cb;
+      sb = s1 < sb ? s1 : sb;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long c2 = __shfl_xor_sync(0xffffffffu, cb, o);

@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "mhd_kernels.cuh"
 #include "mhd_ct32.cuh"
 #include "mhd_source32.cuh"
@@ -69,5 +71,21 @@ cudaError_t dt_refine(const Grid &g, const Phys &ph, const Fields &f, const floa
 cudaError_t divv(const Grid &g, const Fields &f, double *d, cudaStream_t s);
 cudaError_t dissip(const Grid &g, const Fields &f, const double *d, int e, cudaStream_t s);
 cudaError_t diag(const Grid &g, const Phys &ph, const Fields &f, double *part, int *nblocks, cudaStream_t s);
+
+// self-gravity (mhd_gravity.cu): the potential of rho on the grid, and the
+// half kick of the velocities by its gradient
+struct GravityArgs {
+  Grid g;
+  const double *rho;
+  double *phi;                       // padded layout of U
+  double2 *w;                        // nx ny nz complex work
+  double *cp;                        // nx ny nz doubles of Thomas scratch
+  const double2 *tw_y, *tw_z;        // twiddles (gravity_twiddles) for ny and nz
+  double dx, dy, dz, x0, lbox;       // dx(1), dy(1), dz(1), x(0), x(nx) - x(0)
+};
+bool gravity_size_ok(int n);          // a power of two up to 1024
+std::vector<double2> gravity_twiddles(int n);
+cudaError_t gravity_solve(const GravityArgs &a, cudaStream_t s);
+cudaError_t gravity_kick(const Grid &g, const Fields &f, const double *phi, double dt, double dx0, cudaStream_t s);
 
 }  // namespace mhd

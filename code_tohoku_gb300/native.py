@@ -24,7 +24,7 @@ COOL_EXACT, COOL_SURROGATE, COOL_NEWTON = 0, 1, 2
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_timestep", "mhd_source",
            "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_step_host", "mhd_evolve",
-           "mhd_download_columns", "mhd_get_time",
+           "mhd_download_columns", "mhd_download_potential", "mhd_get_time",
            "mhd_set_time", "mhd_set_inflow", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
            "mhd_kernel_launches", "mhd_reset_counters", "mhd_surrogate_nparams", "mhd_surrogate_load",
            "mhd_surrogate_train", "mhd_surrogate_label", "mhd_surrogate_eval", "mhd_surrogate_grad",
@@ -44,7 +44,8 @@ class _Params(ctypes.Structure):
                 ("pmin", ctypes.c_double), ("pmax", ctypes.c_double), ("rmin", ctypes.c_double),
                 ("kb", ctypes.c_double), ("kcond", ctypes.c_double),
                 ("ifthrm", ctypes.c_int), ("dissip", ctypes.c_int), ("precision", ctypes.c_int),
-                ("cooling", ctypes.c_int), ("device", ctypes.c_int), ("ifchem", ctypes.c_int), ("ifrad", ctypes.c_int)]
+                ("cooling", ctypes.c_int), ("device", ctypes.c_int), ("ifchem", ctypes.c_int), ("ifrad", ctypes.c_int),
+                ("ifgrv", ctypes.c_int)]
 
 
 class _Diag(ctypes.Structure):
@@ -91,6 +92,7 @@ def load(build_if_missing=True):
         "mhd_upload": [H, _P, _P, _P, _P, _P, _P, _P, _P],
         "mhd_download": [H, _P, _P, _P],
         "mhd_download_columns": [H, _P],
+        "mhd_download_potential": [H, _P],
         "mhd_timestep": [H, _P, ctypes.POINTER(ctypes.c_int)],
         "mhd_source": [H, ctypes.c_double],
         "mhd_sweep": [H, ctypes.c_int, ctypes.c_double],
@@ -223,6 +225,7 @@ def params_struct(p: MhdParams, precision=PREC_FP64, cooling=COOL_EXACT, device=
     s.precision, s.cooling, s.device = precision, cooling, device
     s.ifchem = getattr(p, "ifchem", 0)
     s.ifrad = getattr(p, "ifrad", 0)
+    s.ifgrv = getattr(p, "ifgrv", 0)
     return s
 
 
@@ -299,6 +302,12 @@ class Mhd3D:
         """SHIELD's ten column arrays (ifrad = 2), padded layout."""
         out = np.zeros((10,) + self.shape)
         self._ck(self.L.mhd_download_columns(self.h, _ptr(out)))
+        return out
+
+    def potential(self):
+        """The gravitational potential (ifgrv = 2), padded layout."""
+        out = np.zeros(self.shape)
+        self._ck(self.L.mhd_download_potential(self.h, _ptr(out)))
         return out
 
     def step_host(self, U_in, species_in, U_out, species_out, tsave=1e30):

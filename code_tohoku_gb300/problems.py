@@ -58,6 +58,7 @@ class MhdParams:
     dissip: int = 1
     ifchem: int = 0     # 2: chemistry network + species cooling (the shipped deck's); 0: KI cooling
     ifrad: int = 0      # 2: SHIELD column densities (x sides); 0: columns 0 (the shipped deck's)
+    ifgrv: int = 0      # 2: self-gravity (periodic y, z; isolated x); 0: off (the shipped deck's)
 
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)

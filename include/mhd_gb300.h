@@ -80,6 +80,12 @@ typedef struct mhd_params {
   int ifrad;                   /* 2: SHIELD column densities from both x
                                   sides (:2924-3036) for the species cooling
                                   and the rates; 0: columns 0 (the deck's) */
+  int ifgrv;                   /* 2: self-gravity (GRAVTY, selfG_MPIfull8.f90):
+                                  grad^2 Phi = 4 pi G rho, periodic y and z,
+                                  isolated x, half kicks before the first and
+                                  after the second SOURCE; needs ny and nz
+                                  powers of two up to 1024 and uniform cells.
+                                  0: off (the shipped deck's)               */
 } mhd_params;
 
 /* Inflow boundary data (BC code 4 on an x side): the values a ghost cell on
@@ -124,6 +130,9 @@ int mhd_download(mhd_handle *h, double *U, double *species, double *bcc);
  * NCO(2), tCII(1), tCII(2) (the module arrays of :30, side 1 = column from
  * x = 0, side 2 = from the far end). */
 int mhd_download_columns(mhd_handle *h, double *columns);
+/* The gravitational potential Phi (ifgrv = 2) in the layout of one block of
+ * U, ghosts included (the module array Phi of :37, written by SAVEU). */
+int mhd_download_potential(mhd_handle *h, double *phi);
 
 /* Couran + Stblty + min (EVOLVE:569-599 for the whole grid).  *dt is
  * min(tfinal, CFL*tCFL, tLMT); *st is 1 (FastSpd) or 2 (Conduct).  Both

@@ -18,6 +18,7 @@
 // expressions follow the Fortran line by line; build with -ffp-contract=off.
 // exp/log10/10**x come from detmath.h, shared with the GPU kernels.
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -73,6 +74,7 @@ struct Params {
                       //    (SOURCE :2576-2776, Fcool :2825-2880); 0: KI cooling
   int dissip;         // 1: DISSIP edge damping (MCF3DSGincfca3.f90:3143-3173)
   int ifrad;          // 2: SHIELD column densities (:2924-3036); 0: columns stay 0
+  int ifgrv;          // 2: self-gravity (GRAVTY, selfG_MPIfull8.f90); 0: off
   int nspecies;       // 8 (all species carried)
 };
 
@@ -117,6 +119,7 @@ struct Mhd3D {
     for (int c = 1; c <= 3; c++) { Bcc[c].assign(ncell, 0.0); Vfc[c].assign(ncell, 0.0); EMF[c].assign(ncell, 0.0); }
     for (int c = 1; c <= 2; c++) Blg[c].assign(ncell, 0.0);
     dnc.assign(ncell, 0.0); xlag.assign(ncell, 0.0); dxlagM.assign(ncell, 0.0);
+    Phi.assign(ncell, 0.0);
     for (int d = 0; d < 3; d++) { xc[d].assign(Nd(d) + 4, 0.0); dxc[d].assign(Nd(d) + 4, 0.0); }
     // MCF3DSGincfca3.f90:178-179
     ndmin[SH] = p.rmin * 0.91; ndmin[SP] = 1e-20; ndmin[SH2] = 1e-20; ndmin[SHE] = p.rmin * 0.09;
@@ -1338,13 +1341,157 @@ struct Mhd3D {
   }
 
   // one in20 iteration of EVOLVE after dt is known (:606-656)
+  // ---------------------------------------------------------- self-gravity
+  // GRAVTY (3DMHD-CfCA/selfG_MPIfull8.f90) solves grad^2 Phi = 4 pi G rho
+  // (crhs = U(:,:,:,1) G4pi, :166) periodic in y and z and isolated in x:
+  // the potential on the two x faces comes from the density's y-z Fourier
+  // modes through the Green's function of d^2/dx^2 - kap^2, with kap^2 the
+  // eigenvalue of the discrete y-z Laplacian, 4 sin^2(pi l/Ny)/dy^2 +
+  // 4 sin^2(pi m/Nz)/dz^2 (PB :1133-1200):
+  //   Phi_face(kap) = -G4pi dx / (2 kap) sum_i rho_i exp(-kap d_i),
+  //   Phi_face(0)   = +G4pi dx / 2 sum_i rho_i d_i  (d_i: cell centre to the face)
+  // and the interior is solved with the faces as Dirichlet values.  The
+  // reference relaxes it by multigrid on node-centred grids split over the
+  // MPI ranks (mglin, relaxMPI); here every mode's x line is solved
+  // exactly: Fourier transforms in y and z (a plain DFT in this
+  // restatement), then the tridiagonal system of the second-order x
+  // Laplacian minus kap^2 with the face values through the ghost
+  // reflection Phi_0 = 2 Phi_face - Phi_1.  After the solve the x ghosts
+  // copy the edge cells (grad = 0, GRAVTY :70-75) and y, z wrap.
+  std::vector<double> Phi;
+  static constexpr double kG = 1.11142e-4, kG4pi = 12.56637 * 1.11142e-4;   // MCF3DSGincfca3.f90:35
+
+  static void dft_lines(std::vector<std::complex<double>> &w, int n, size_t stride, size_t nlines,
+                        size_t line_step_a, size_t na, size_t line_step_b, int sign) {
+    std::vector<std::complex<double>> tmp(n), tw(n);
+    for (int q = 0; q < n; q++) {
+      const double ang = sign * 2.0 * M_PI * (double)q / (double)n;
+      tw[q] = std::complex<double>(std::cos(ang), std::sin(ang));
+    }
+    for (size_t L = 0; L < nlines; L++) {
+      const size_t base = (L % na) * line_step_a + (L / na) * line_step_b;
+      for (int m = 0; m < n; m++) {
+        std::complex<double> acc(0.0, 0.0);
+        for (int j = 0; j < n; j++) acc += w[base + (size_t)j * stride] * tw[((size_t)j * m) % n];
+        tmp[m] = acc;
+      }
+      for (int m = 0; m < n; m++) w[base + (size_t)m * stride] = tmp[m];
+    }
+  }
+
+  void gravity_solve() {
+    const int nx = Nx, ny = Ny, nz = Nz;
+    const double dx = dxc[0][2], dy = dxc[1][2], dz = dxc[2][2];   // dx(1), dy(1), dz(1)
+    const double x0 = xc[0][1];                                      // x(0): the left face
+    const double lbox = xc[0][nx + 1] - x0;
+    std::vector<std::complex<double>> w((size_t)nx * ny * nz);
+    auto W = [&](int i, int j, int k) -> std::complex<double> & { return w[(size_t)i + (size_t)nx * (j + (size_t)ny * k)]; };
+    for (int k = 0; k < nz; k++)
+      for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) W(i, j, k) = U[1][id(i + 1, j + 1, k + 1)];
+    // y lines (stride nx) for every (i, k), then z lines (stride nx ny) for every (i, j)
+    dft_lines(w, ny, (size_t)nx, (size_t)nx * nz, 1, (size_t)nx, (size_t)nx * ny, -1);
+    dft_lines(w, nz, (size_t)nx * ny, (size_t)nx * ny, 1, (size_t)nx * ny, 0, -1);
+    std::vector<double> cp(nx);
+    std::vector<std::complex<double>> rhs(nx);
+    for (int m = 0; m < nz; m++)
+      for (int l = 0; l < ny; l++) {
+        const double sy = std::sin(M_PI * l / ny), sz2 = std::sin(M_PI * m / nz);
+        const double kap2 = 4.0 * sy * sy / (dy * dy) + 4.0 * sz2 * sz2 / (dz * dz);
+        const double kap = std::sqrt(kap2);
+        std::complex<double> bl(0.0, 0.0), br(0.0, 0.0);
+        for (int i = 0; i < nx; i++) {
+          const double xcen = 0.5 * (xc[0][i + 1] + xc[0][i + 2]);   // centre of cell i+1
+          const double d1 = xcen - x0, d2 = lbox - d1;
+          const std::complex<double> r = W(i, l, m);
+          if (l == 0 && m == 0) {
+            bl += r * (0.5 * kG4pi * dx * d1);
+            br += r * (0.5 * kG4pi * dx * d2);
+          } else {
+            bl += r * (-0.5 * kG4pi * dx * std::exp(-kap * d1) / kap);
+            br += r * (-0.5 * kG4pi * dx * std::exp(-kap * d2) / kap);
+          }
+        }
+        // (Phi_{i-1} - 2 Phi_i + Phi_{i+1}) / dx^2 - kap^2 Phi_i = G4pi rho_i,
+        // Phi_0 = 2 bl - Phi_1, Phi_{n+1} = 2 br - Phi_n (Thomas algorithm)
+        const double a = 1.0 / (dx * dx), b0 = -2.0 / (dx * dx) - kap2, be = -3.0 / (dx * dx) - kap2;
+        for (int i = 0; i < nx; i++) rhs[i] = W(i, l, m) * kG4pi;
+        rhs[0] -= 2.0 * a * bl;
+        rhs[nx - 1] -= 2.0 * a * br;
+        double diag = (nx == 1) ? (-4.0 / (dx * dx) - kap2) : be;
+        double c = a / diag;
+        std::complex<double> dprev = rhs[0] / diag;
+        cp[0] = c;
+        rhs[0] = dprev;
+        for (int i = 1; i < nx; i++) {
+          const double bi = (i == nx - 1) ? be : b0;
+          const double den = bi - a * cp[i - 1];
+          cp[i] = a / den;
+          rhs[i] = (rhs[i] - a * rhs[i - 1]) / den;
+        }
+        for (int i = nx - 2; i >= 0; i--) rhs[i] -= cp[i] * rhs[i + 1];
+        for (int i = 0; i < nx; i++) W(i, l, m) = rhs[i];
+      }
+    dft_lines(w, nz, (size_t)nx * ny, (size_t)nx * ny, 1, (size_t)nx * ny, 0, +1);
+    dft_lines(w, ny, (size_t)nx, (size_t)nx * nz, 1, (size_t)nx, (size_t)nx * ny, +1);
+    const double scale = 1.0 / ((double)ny * (double)nz);
+    for (int k = 0; k < nz; k++)
+      for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) Phi[id(i + 1, j + 1, k + 1)] = W(i, j, k).real() * scale;
+    gravity_ghosts();
+  }
+  // x: grad = 0 copies of the edge cells (GRAVTY :70-75); y, z periodic
+  void gravity_ghosts() {
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny; j++) {
+        Phi[id(0, j, k)] = Phi[id(1, j, k)];
+        Phi[id(-1, j, k)] = Phi[id(1, j, k)];
+        Phi[id(Nx + 1, j, k)] = Phi[id(Nx, j, k)];
+        Phi[id(Nx + 2, j, k)] = Phi[id(Nx, j, k)];
+      }
+    for (int k = 1; k <= Nz; k++)
+      for (int j = -1; j <= Ny + 2; j++) {
+        if (j >= 1 && j <= Ny) continue;
+        const int js = j < 1 ? j + Ny : j - Ny;
+        for (int i = -1; i <= Nx + 2; i++) Phi[id(i, j, k)] = Phi[id(i, js, k)];
+      }
+    for (int k = -1; k <= Nz + 2; k++) {
+      if (k >= 1 && k <= Nz) continue;
+      const int ks = k < 1 ? k + Nz : k - Nz;
+      for (int j = -1; j <= Ny + 2; j++)
+        for (int i = -1; i <= Nx + 2; i++) Phi[id(i, j, k)] = Phi[id(i, j, ks)];
+    }
+  }
+  // GRAVTY mode 3 (:90-97): half a kick of the velocities by the fourth-order
+  // gradient of Phi, with dx(0) in every direction
+  void gravity_kick(double dt) {
+    const double dxi = 1.0 / (12.0 * dxc[0][1]);
+    const size_t sy_ = (size_t)sx, sz_ = (size_t)sx * sy;
+    for (int k = 1; k <= Nz; k++)
+      for (int j = 1; j <= Ny; j++)
+        for (int i = 1; i <= Nx; i++) {
+          const size_t a = id(i, j, k);
+          const double *F = Phi.data();
+          U[2][a] = U[2][a] - dt * (-F[a + 2] + 8.0 * F[a + 1] - 8.0 * F[a - 1] + F[a - 2]) * dxi * 0.5;
+          U[3][a] = U[3][a] - dt * (-F[a + 2 * sy_] + 8.0 * F[a + sy_] - 8.0 * F[a - sy_] + F[a - 2 * sy_]) * dxi * 0.5;
+          U[4][a] = U[4][a] - dt * (-F[a + 2 * sz_] + 8.0 * F[a + sz_] - 8.0 * F[a - sz_] + F[a - 2 * sz_]) * dxi * 0.5;
+        }
+  }
+
+  // EVOLVE :606-656: with ifgrv = 2 a half kick before the first SOURCE, and
+  // after the second SOURCE a new Phi and the other half kick
   void advance(double dt) {
+    if (P.ifgrv == 2) gravity_kick(dt);
     SOURCE(0.5 * dt);
     static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
     for (int s = 0; s < 3; s++) MHD(orders[ifEVO - 1][s], dt);
     ifEVO = ifEVO % 6 + 1;
     CT(dt);
     SOURCE(0.5 * dt);
+    if (P.ifgrv == 2) {
+      gravity_solve();
+      gravity_kick(dt);
+    }
     if (P.dissip) DISSIP();
     time = time + dt;
   }
@@ -1354,7 +1501,8 @@ struct Mhd3D {
 
 extern "C" {
 
-// params (doubles): nx,ny,nz, CFL,facdep,tfinal, bc[6], pmin,pmax,rmin, kb,Kcond, ifthrm, dissip, ifchem, ifrad
+// params (doubles): nx,ny,nz, CFL,facdep,tfinal, bc[6], pmin,pmax,rmin, kb,Kcond, ifthrm, dissip, ifchem, ifrad,
+// ifgrv
 void *o3d_create(const double *p) {
   Params P{};
   P.nx = (int)p[0]; P.ny = (int)p[1]; P.nz = (int)p[2];
@@ -1365,6 +1513,7 @@ void *o3d_create(const double *p) {
   P.ifthrm = (int)p[17]; P.dissip = (int)p[18];
   P.ifchem = (int)p[19];
   P.ifrad = (int)p[20];
+  P.ifgrv = (int)p[21];
   P.nspecies = 8;
   Mhd3D *m = new Mhd3D();
   m->init(P);
@@ -1388,7 +1537,15 @@ void o3d_upload(void *h, const double *U, const double *sp, const double *coords
   m->init_chem_totals();   // nde, ndtot and the columns (:471-477)
   if (m->P.ifrad == 2)
     for (int l = 0; l < 20; l++) m->SHIELD();   // :479
+  if (m->P.ifgrv == 2) m->gravity_solve();      // :481-484
 }
+
+// Phi in the padded layout of U
+void o3d_potential(void *h, double *out) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  memcpy(out, m->Phi.data(), m->ncell * sizeof(double));
+}
+void o3d_gravity_solve(void *h) { static_cast<Mhd3D *>(h)->gravity_solve(); }
 
 void o3d_columns(void *h, double *out) {
   Mhd3D *m = static_cast<Mhd3D *>(h);

@@ -61,6 +61,8 @@ def lib():
         L.o3d_destroy.argtypes = [ctypes.c_void_p]
         L.o3d_set_inflow.argtypes = [ctypes.c_void_p, _P, ctypes.c_void_p, ctypes.c_double]
         L.o3d_columns.argtypes = [ctypes.c_void_p, _P]
+        L.o3d_potential.argtypes = [ctypes.c_void_p, _P]
+        L.o3d_gravity_solve.argtypes = [ctypes.c_void_p]
         L.o3d_ki_label.restype = ctypes.c_double
         L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
@@ -108,7 +110,8 @@ class Oracle3D:
     def __init__(self, params):
         p = params
         v = [p.nx, p.ny, p.nz, p.cfl, p.facdep, p.tfinal, *p.bc, p.pmin, p.pmax, p.rmin,
-             p.kb, p.kcond, p.ifthrm, p.dissip, getattr(p, "ifchem", 0), getattr(p, "ifrad", 0)]
+             p.kb, p.kcond, p.ifthrm, p.dissip, getattr(p, "ifchem", 0), getattr(p, "ifrad", 0),
+             getattr(p, "ifgrv", 0)]
         self.params = p
         self.shape = (p.nz + 4, p.ny + 4, p.nx + 4)
         self.h = lib().o3d_create(_ptr(np.array(v, dtype=np.float64)))
@@ -140,6 +143,15 @@ class Oracle3D:
         out = np.zeros((10,) + self.shape)
         lib().o3d_columns(self.h, _ptr(out))
         return out
+
+    def potential(self):
+        """Phi (self-gravity, ifgrv = 2) in the padded layout."""
+        out = np.zeros(self.shape)
+        lib().o3d_potential(self.h, _ptr(out))
+        return out
+
+    def gravity_solve(self):
+        lib().o3d_gravity_solve(self.h)
 
     def sweep(self, d, dt):
         lib().o3d_sweep(self.h, d, dt)
