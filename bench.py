@@ -52,7 +52,9 @@ B_ALG_STEP = 552.0      # algorithmic bytes per zone-update of the whole step
 B_ALG_SWEEP = 104.0     # per sweep: read rho, v3, p, face-B3 (64) + write rho, v3, p (40)
 # algorithmic bytes per zone of each phase of the step (they add up to B_ALG_STEP)
 B_ALG_PHASE = {"timestep": 64.0, "source_1": 48.0, "sweep_x": 104.0, "sweep_y": 104.0, "sweep_z": 104.0,
-               "ct": 80.0, "source_2": 48.0, "dissip": 0.0}
+               "ct": 80.0, "source_2": 48.0, "dissip": 0.0,
+               # self-gravity (not part of the 552 B/zone step): read rho, write Phi; read Phi, v + write v
+               "gravity_potential": 16.0, "gravity_kick_1": 56.0, "gravity_kick_2": 56.0}
 SWEEP_NAMES = ("sweep_x", "sweep_y", "sweep_z")
 
 
@@ -287,6 +289,9 @@ def main():
             rec.setdefault(name, []).append((e0, e1))
             return r
         dt, _ = phase("timestep", g.timestep)
+        grav = getattr(g.params, "ifgrv", 0) == 2
+        if grav:
+            phase("gravity_kick_1", g.gravity, dt, 3)            # EVOLVE :607
         phase("source_1", g.source, 0.5 * dt)
         order = ((0, 1, 2), (1, 2, 0), (2, 0, 1), (0, 2, 1), (1, 0, 2), (2, 1, 0))[g.ifevo - 1]
         for d in order:
@@ -294,6 +299,9 @@ def main():
         g.ifevo = g.ifevo % 6 + 1
         phase("ct", g.ct, dt)
         phase("source_2", g.source, 0.5 * dt)
+        if grav:
+            phase("gravity_potential", g.gravity, dt, 2)         # :653
+            phase("gravity_kick_2", g.gravity, dt, 3)
         if dissip:
             phase("dissip", g.dissip)
         g.set_time(g.time + dt, g.ifevo)
@@ -581,6 +589,7 @@ def main():
         gg, msg, phg, _, _ = timed_run(native.PREC_FP32, native.COOL_SURROGATE, state=sg, steps=5, warmup=args.warmup)
         grav = {"workload": f"the headline problem with self-gravity, {args.n}^3", "steps": 5,
                 "ms_per_step_with_gravity": msg / 5, "ms_per_step_without": ms32 / args.steps,
+                "phase_ms": {k: v for k, v in phg.items() if k.startswith("gravity")},
                 "potential_solve": "radix-2 FFTs in y and z, a tridiagonal x solve per mode (FP64)"}
         del gg
 

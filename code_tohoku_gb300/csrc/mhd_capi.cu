@@ -721,6 +721,14 @@ int mhd_dissip(mhd_handle *h) {
   return MHD_OK;
 }
 
+int mhd_gravity(mhd_handle *h, double dt, int mode) {
+  if (!h || (mode != 2 && mode != 3)) return MHD_ERR_ARG;
+  if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
+  if (h->p.ifgrv != 2) return fail(h, MHD_ERR_STATE, "the handle has no self-gravity (ifgrv != 2)");
+  CKR(cudaSetDevice(h->p.device));
+  return mode == 2 ? gravity_potential(h) : gravity_half_kick(h, dt);
+}
+
 int mhd_advance(mhd_handle *h, double dt) {
   if (!h) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");

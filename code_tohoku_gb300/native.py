@@ -23,7 +23,7 @@ COOL_EXACT, COOL_SURROGATE, COOL_NEWTON = 0, 1, 2
 
 # every symbol the header declares (checked by the CPU test suite)
 EXPORTS = ("mhd_create", "mhd_destroy", "mhd_upload", "mhd_download", "mhd_timestep", "mhd_source",
-           "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_advance", "mhd_step", "mhd_step_host", "mhd_evolve",
+           "mhd_sweep", "mhd_ct", "mhd_dissip", "mhd_gravity", "mhd_advance", "mhd_step", "mhd_step_host", "mhd_evolve",
            "mhd_download_columns", "mhd_download_potential", "mhd_get_time",
            "mhd_set_time", "mhd_set_inflow", "mhd_diagnostics", "mhd_synchronize", "mhd_set_stream", "mhd_last_error",
            "mhd_kernel_launches", "mhd_reset_counters", "mhd_surrogate_nparams", "mhd_surrogate_load",
@@ -98,6 +98,7 @@ def load(build_if_missing=True):
         "mhd_sweep": [H, ctypes.c_int, ctypes.c_double],
         "mhd_ct": [H, ctypes.c_double],
         "mhd_dissip": [H],
+        "mhd_gravity": [H, ctypes.c_double, ctypes.c_int],
         "mhd_advance": [H, ctypes.c_double],
         "mhd_step": [H, ctypes.c_double, _P, ctypes.POINTER(ctypes.c_int)],
         "mhd_step_host": [H, _P, _P, _P, _P, ctypes.c_double, _P, ctypes.POINTER(ctypes.c_int)],
@@ -288,6 +289,10 @@ class Mhd3D:
 
     def dissip(self):
         self._ck(self.L.mhd_dissip(self.h))
+
+    def gravity(self, dt, mode):
+        """GRAVTY(dt, mode): 2 the potential, 3 the half kick (ifgrv = 2)."""
+        self._ck(self.L.mhd_gravity(self.h, dt, mode))
 
     def advance(self, dt):
         self._ck(self.L.mhd_advance(self.h, dt))

@@ -143,6 +143,12 @@ int mhd_source(mhd_handle *h, double dt);             /* SOURCE(dt)        */
 int mhd_sweep(mhd_handle *h, int dir, double dt);     /* dir 0=x,1=y,2=z   */
 int mhd_ct(mhd_handle *h, double dt);
 int mhd_dissip(mhd_handle *h);
+/* GRAVTY(dt, mode) of selfG_MPIfull8.f90:1-100 for a handle with ifgrv = 2:
+ * mode 2 solves the potential of the current density, mode 3 gives the
+ * half kick of the velocities by its fourth-order gradient (:90-97).
+ * mhd_advance / mhd_step call both where EVOLVE does (:607, :653); a driver
+ * that calls the step's parts one by one calls this itself. */
+int mhd_gravity(mhd_handle *h, double dt, int mode);
 /* SOURCE(dt/2), three sweeps in the order ifEVO (1..6, :611-634), CT,
  * SOURCE(dt/2), DISSIP, time += dt.  Advances ifEVO like the reference. */
 int mhd_advance(mhd_handle *h, double dt);

@@ -99,3 +99,30 @@ def test_step_host_with_gravity_equals_upload_step_download():
     Ub, Sb, _ = b.download(with_bcc=False)
     assert np.array_equal(Uout, Ub) and np.array_equal(Sout, Sb)
     assert np.array_equal(a.potential(), b.potential())
+
+
+def test_gravity_entry_point_parts_equal_advance():
+    """A driver calling the step's parts one by one, with mhd_gravity where
+    EVOLVE calls GRAVTY (:607, :653), gets mhd_advance's result bit for bit."""
+    st = blob_state(16, 16, 16, seed=4)
+    a = native.Mhd3D(st.params)
+    a.upload(st)
+    b = native.Mhd3D(st.params)
+    b.upload(st)
+    for k in range(3):
+        dt, _ = a.timestep()
+        a.advance(dt)
+        b.set_time(b.time, k + 1)
+        b.gravity(dt, 3)
+        b.source(0.5 * dt)
+        for d in ((0, 1, 2), (1, 2, 0), (2, 0, 1))[k]:
+            b.sweep(d, dt)
+        b.ct(dt)
+        b.source(0.5 * dt)
+        b.gravity(dt, 2)
+        b.gravity(dt, 3)
+        b.set_time(b.time + dt, k + 2)
+    Ua, Sa, _ = a.download(with_bcc=False)
+    Ub, Sb, _ = b.download(with_bcc=False)
+    assert np.array_equal(Ua, Ub) and np.array_equal(Sa, Sb)
+    assert np.array_equal(a.potential(), b.potential())
