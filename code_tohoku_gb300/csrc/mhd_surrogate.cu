@@ -3,9 +3,9 @@
 //   sur_label_kernel  labels from the plain integrator (FP64 IMC bisection,
 //                     the same device code as the FP64 SOURCE)
 //   sur_pack_kernel   FP32 master parameters -> BF16 packed SurNet
-//   sur_grad_kernel   forward + backward on BF16 tensor-core tiles
-//                     (mma.sync m16n8k16, FP32 accumulate), gradients of
-//                     the mean squared error summed into an FP32 vector
+//   sur_grad_kernel   forward + backward on tcgen05 tensor-core tiles (BF16
+//                     operands, FP32 accumulators in tensor memory), gradients
+//                     of the mean squared error summed into an FP32 vector
 //   sur_adam_kernel   Adam update of the FP32 master parameters
 //   sur_eval_kernel   batch inference (tcgen05 tiles: the fused SOURCE's network code)
 // and the extern "C" entry points that expose them.
@@ -119,195 +119,259 @@ __global__ void __launch_bounds__(kFusedThreads) sur_eval_kernel(const SurNet *n
 // learns the log of the first head's error).
 constexpr float kConfWeight = 0.1f;
 
-// Forward + backward of one batch.  A CTA of 4 warps works on tiles of 64
-// samples (16 per warp).  Per warp: FP32 first layer, BF16 tensor-core
-// second and output layers, output gradients, dh2 = dy W3 (CUDA cores),
-// dz2 = dh2 SiLU'(z2), dh1 = dz2 W2 (tensor cores), dz1 = dh1 SiLU'(z1).
-// Per CTA: dW2 = dz2^T h1 over the 64 samples on tensor cores (each warp
-// owns 16 rows of dW2); the small gradients (W1, b1, b2, W3, b3) are
-// reduced with shuffles and shared-memory atomics.  Gradients are summed
+// Forward + backward of one batch on the fifth-generation tensor cores.  A
+// CTA of 128 threads takes tiles of 128 samples (thread r = sample row r),
+// one CTA per SM striding over the batch's tiles.  Per tile:
+//   layer 1 on the CUDA cores in FP32: h1 = bf16(SiLU(z1));
+//   Z2 = h1 W2^T                       tcgen05 (M 128, N 64, K 64)
+//   h2 = bf16(SiLU(Z2 + b2)),  Y = h2 W3^T   (N 16, the 2 outputs padded)
+//   output gradients d = (d0, d1) of the loss per sample (CUDA cores),
+//   dz2 = (d W3) SiLU'(z2) in FP32, rounded to BF16 for the products;
+//   dh1 = dz2 W2                       tcgen05 (B = W2^T, K-major)
+//   and, accumulated in tensor memory over all the CTA's tiles:
+//   [dW2 | gb2]  = dz2^T [h1 | 1]      (M 64 padded to 128, N 80, K 128)
+//   [gW3 | gb3]^T = [h2 | 1]^T d      (M 65 padded to 128, N 16, K 128)
+//   [gW1 | gb1]  = dz1^T [x | 1]       (dz1 = dh1 SiLU'(z1); N 16, K 128)
+// with the BF16 rounding points of oracle/surrogate_ref.py.  The
+// transposed operands are written transposed into shared memory by the
+// threads; the ones columns and zero rows are set once.  Gradients are summed
 // over the batch (divided by the batch size) into g (FP32).
-__global__ void __launch_bounds__(128) sur_grad_kernel(const SurNet *net, const float *x, const float *y,
-                                                       long long n, float inv_batch, float *gout, float *loss) {
-  __shared__ __nv_bfloat16 s_h1[64][64 + 8];   // [sample][feature]
-  __shared__ __nv_bfloat16 s_dz2[64][64 + 8];
-  __shared__ float s_g[SUR_NPARAM];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  for (int q = threadIdx.x; q < SUR_NPARAM; q += blockDim.x) s_g[q] = 0.0f;
-  float accW2[8][4];
-#pragma unroll
-  for (int nt = 0; nt < 8; nt++) accW2[nt][0] = accW2[nt][1] = accW2[nt][2] = accW2[nt][3] = 0.0f;
-  float lsum = 0.0f;
-  __syncthreads();
-  long long ntile = (n + 63) / 64;
-  for (long long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-    long long s0 = tile * 64 + warp * 16;
-    // lanes 0..15 bring one sample each (normalised inputs)
-    long long sr = s0 + (lane & 15);
-    bool ok = lane < 16 && sr < n;
-    float n0 = ok ? (x[3 * sr] - SUR_C0) / SUR_S0 : 0.0f;
-    float n1 = ok ? (x[3 * sr + 1] - SUR_C1) / SUR_S1 : 0.0f;
-    float n2 = ok ? (x[3 * sr + 2] - SUR_C2) / SUR_S2 : 0.0f;
-    // forward
-    float z1[8][4];
-    layer1_fp32(net, n0, n1, n2, 0, z1);
-    uint32_t a1[4][4];
-    act_frags(z1, a1);
-    float z2[8][4];
-    layer64<4>(net->W2, net->b2, a1, z2);
-    uint32_t a2[4][4];
-    act_frags(z2, a2);
-    float yo[4];
-    layer_out(net, a2, yo);
-    // output gradients for rows g and g+8 (held by the t == 0 lanes)
-    float d0g = 0, d1g = 0, d0h = 0, d1h = 0;
-    if (t == 0) {
-      long long ra = s0 + g, rb = s0 + g + 8;
-      if (ra < n) {
-        float e = yo[0] - y[ra];
-        float tc = log10f(fabsf(e) + 1e-4f);
-        d0g = 2.0f * e * inv_batch;
-        d1g = kConfWeight * 2.0f * (yo[1] - tc) * inv_batch;
-        lsum += e * e;
-      }
-      if (rb < n) {
-        float e = yo[2] - y[rb];
-        float tc = log10f(fabsf(e) + 1e-4f);
-        d0h = 2.0f * e * inv_batch;
-        d1h = kConfWeight * 2.0f * (yo[3] - tc) * inv_batch;
-        lsum += e * e;
-      }
-    }
-    d0g = __shfl_sync(0xffffffffu, d0g, g * 4);
-    d1g = __shfl_sync(0xffffffffu, d1g, g * 4);
-    d0h = __shfl_sync(0xffffffffu, d0h, g * 4);
-    d1h = __shfl_sync(0xffffffffu, d1h, g * 4);
-    // b3, W3 gradients; dh2 and dz2
-    float dz2[8][4];
-    float gb3a = (t == 0) ? d0g + d0h : 0.0f, gb3b = (t == 0) ? d1g + d1h : 0.0f;
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        int k = nt * 8 + 2 * t + q;
-        float hg = silu(z2[nt][q]), hh = silu(z2[nt][2 + q]);
-        // the BF16-rounded activations the forward used
-        hg = bf16_round(hg);
-        hh = bf16_round(hh);
-        float w30 = __bfloat162float(net->W3[k]), w31 = __bfloat162float(net->W3[64 + k]);
-        float gw0 = d0g * hg + d0h * hh, gw1 = d1g * hg + d1h * hh;
-        for (int o = 4; o < 32; o <<= 1) {
-          gw0 += __shfl_xor_sync(0xffffffffu, gw0, o);
-          gw1 += __shfl_xor_sync(0xffffffffu, gw1, o);
-        }
-        if (g == 0) {
-          atomicAdd(&s_g[SUR_OW3 + k], gw0);
-          atomicAdd(&s_g[SUR_OW3 + 64 + k], gw1);
-        }
-        dz2[nt][q] = (d0g * w30 + d1g * w31) * dsilu(z2[nt][q]);
-        dz2[nt][2 + q] = (d0h * w30 + d1h * w31) * dsilu(z2[nt][2 + q]);
-      }
-    }
-    for (int o = 4; o < 32; o <<= 1) {
-      gb3a += __shfl_xor_sync(0xffffffffu, gb3a, o);
-      gb3b += __shfl_xor_sync(0xffffffffu, gb3b, o);
-    }
-    if (lane == 0) {
-      atomicAdd(&s_g[SUR_OB3], gb3a);
-      atomicAdd(&s_g[SUR_OB3 + 1], gb3b);
-    }
-    // b2 gradient; stage dz2 and h1 (BF16) for the dW2 product
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        int k = nt * 8 + 2 * t + q;
-        float gb = dz2[nt][q] + dz2[nt][2 + q];
-        for (int o = 4; o < 32; o <<= 1) gb += __shfl_xor_sync(0xffffffffu, gb, o);
-        if (g == 0) atomicAdd(&s_g[SUR_OB2 + k], gb);
-        s_dz2[warp * 16 + g][k] = __float2bfloat16_rn(dz2[nt][q]);
-        s_dz2[warp * 16 + g + 8][k] = __float2bfloat16_rn(dz2[nt][2 + q]);
-        s_h1[warp * 16 + g][k] = __float2bfloat16_rn(silu(z1[nt][q]));
-        s_h1[warp * 16 + g + 8][k] = __float2bfloat16_rn(silu(z1[nt][2 + q]));
-      }
-    }
-    // dh1 = dz2 W2 on tensor cores (B operand from W2T rows)
-    uint32_t adz[4][4];
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) {
-      adz[kt][0] = pack_bf16(dz2[2 * kt][0], dz2[2 * kt][1]);
-      adz[kt][1] = pack_bf16(dz2[2 * kt][2], dz2[2 * kt][3]);
-      adz[kt][2] = pack_bf16(dz2[2 * kt + 1][0], dz2[2 * kt + 1][1]);
-      adz[kt][3] = pack_bf16(dz2[2 * kt + 1][2], dz2[2 * kt + 1][3]);
-    }
-    float dh1[8][4];
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-      dh1[nt][0] = dh1[nt][1] = dh1[nt][2] = dh1[nt][3] = 0.0f;
-      const __nv_bfloat16 *row = net->W2T + (nt * 8 + g) * 64;
-#pragma unroll
-      for (int kt = 0; kt < 4; kt++) mma_bf16(dh1[nt], adz[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
-    }
-    // dz1, b1 and W1 gradients (W1 against the FP32 inputs)
-    float xa0 = __shfl_sync(0xffffffffu, n0, g), xa1 = __shfl_sync(0xffffffffu, n1, g),
-          xa2 = __shfl_sync(0xffffffffu, n2, g);
-    float xb0 = __shfl_sync(0xffffffffu, n0, g + 8), xb1 = __shfl_sync(0xffffffffu, n1, g + 8),
-          xb2 = __shfl_sync(0xffffffffu, n2, g + 8);
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        int k = nt * 8 + 2 * t + q;
-        float ga = dh1[nt][q] * dsilu(z1[nt][q]), gb = dh1[nt][2 + q] * dsilu(z1[nt][2 + q]);
-        float gbias = ga + gb, gw0 = ga * xa0 + gb * xb0, gw1 = ga * xa1 + gb * xb1, gw2 = ga * xa2 + gb * xb2;
-        for (int o = 4; o < 32; o <<= 1) {
-          gbias += __shfl_xor_sync(0xffffffffu, gbias, o);
-          gw0 += __shfl_xor_sync(0xffffffffu, gw0, o);
-          gw1 += __shfl_xor_sync(0xffffffffu, gw1, o);
-          gw2 += __shfl_xor_sync(0xffffffffu, gw2, o);
-        }
-        if (g == 0) {
-          atomicAdd(&s_g[SUR_OB1 + k], gbias);
-          atomicAdd(&s_g[SUR_OW1 + 3 * k], gw0);
-          atomicAdd(&s_g[SUR_OW1 + 3 * k + 1], gw1);
-          atomicAdd(&s_g[SUR_OW1 + 3 * k + 2], gw2);
-        }
-      }
-    }
-    __syncthreads();
-    // dW2[n][k] += sum_s dz2[s][n] h1[s][k]; warp w owns rows n = 16w..16w+15
-#pragma unroll
-    for (int ks = 0; ks < 4; ks++) {
-      int sa = ks * 16 + 2 * t;
-      uint32_t a[4];
-      int nr = warp * 16 + g;
-      a[0] = (uint32_t)__bfloat16_as_ushort(s_dz2[sa][nr]) | ((uint32_t)__bfloat16_as_ushort(s_dz2[sa + 1][nr]) << 16);
-      a[1] = (uint32_t)__bfloat16_as_ushort(s_dz2[sa][nr + 8]) | ((uint32_t)__bfloat16_as_ushort(s_dz2[sa + 1][nr + 8]) << 16);
-      a[2] = (uint32_t)__bfloat16_as_ushort(s_dz2[sa + 8][nr]) | ((uint32_t)__bfloat16_as_ushort(s_dz2[sa + 9][nr]) << 16);
-      a[3] = (uint32_t)__bfloat16_as_ushort(s_dz2[sa + 8][nr + 8]) | ((uint32_t)__bfloat16_as_ushort(s_dz2[sa + 9][nr + 8]) << 16);
-#pragma unroll
-      for (int nt = 0; nt < 8; nt++) {
-        int kc = nt * 8 + g;
-        uint32_t b0 = (uint32_t)__bfloat16_as_ushort(s_h1[sa][kc]) | ((uint32_t)__bfloat16_as_ushort(s_h1[sa + 1][kc]) << 16);
-        uint32_t b1 = (uint32_t)__bfloat16_as_ushort(s_h1[sa + 8][kc]) | ((uint32_t)__bfloat16_as_ushort(s_h1[sa + 9][kc]) << 16);
-        mma_bf16(accW2[nt], a, b0, b1);
-      }
-    }
-    __syncthreads();
+struct SurGradSmem {
+  __nv_bfloat16 W2[64 * 64];       // B of Z2: [out][in], K-major
+  __nv_bfloat16 W2T[64 * 64];      // B of dh1: [in][out], K-major
+  __nv_bfloat16 W3[16 * 64];       // B of Y: [out padded to 16][in]
+  __nv_bfloat16 A[128 * 64];       // h1, then h2, then dz2: [sample][feature]
+  __nv_bfloat16 dz2T[128 * 128];   // [feature n (64, rest 0)][sample]: A of dW2, then dz1^T, A of gW1
+  __nv_bfloat16 h2T[128 * 128];    // [feature k (64), row 64 ones, rest 0][sample]: A of gW3
+  __nv_bfloat16 h1T[80 * 128];     // [feature k (64), row 64 ones, rest 0][sample]: B of dW2
+  __nv_bfloat16 dT[16 * 128];      // [d0, d1, rest 0][sample]: B of gW3
+  __nv_bfloat16 xT[16 * 128];      // [x0, x1, x2, 1, rest 0][sample]: B of gW1
+  float4 w1[64];                   // (w0, w1, w2, b1)
+  float b2[64], b3[2], w3[2][64];  // BF16-rounded W3 for dh2 on the CUDA cores
+  uint64_t bar;
+  uint32_t tmem;
+  int broken;
+};
+// TMEM columns: Z2 0-63, Y 64-79, dh1 80-143, [dW2|gb2] 144-223, [gW3|gb3] 224-239, [gW1|gb1] 240-255
+constexpr uint32_t kGZ2 = 0, kGY = 64, kGDH1 = 80, kGDW2 = 144, kGW3 = 224, kGW1 = 240, kGCols = 256;
+
+__device__ __forceinline__ void gstore(__nv_bfloat16 *buf, int row, int col, int K, float v) {
+  *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(buf) + tc::kmajor_off(row, col, K)) =
+      __float2bfloat16_rn(v);
+}
+__device__ __forceinline__ void gstore8(__nv_bfloat16 *buf, int row, int col8, int K, const float (&v)[8]) {
+  const uint4 q = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                             pack_bf16(v[6], v[7]));
+  *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(buf) + tc::kmajor_off(row, col8, K)) = q;
+}
+// one thread issues nk K-steps of 16 (A: K-major with K = 16 nk... columns)
+__device__ __forceinline__ void gmma(uint32_t d, const __nv_bfloat16 *Am, int KA, const __nv_bfloat16 *Bm, int KB,
+                                     int N, int nk, bool acc_first) {
+  const uint32_t idesc = tc::idesc_bf16_f32(128, N), ab = tc::smem_u32(Am), bb = tc::smem_u32(Bm);
+  for (int kk = 0; kk < nk; kk++)
+    tc::mma_bf16(d, tc::smem_desc(ab + 256 * kk, 128, 16 * KA), tc::smem_desc(bb + 256 * kk, 128, 16 * KB), idesc,
+                 acc_first || kk > 0);
+}
+// the commit of the MMAs issued so far and the CTA-wide wait for it; false
+// on every thread when the wait timed out
+__device__ __forceinline__ bool gsync(SurGradSmem *s, uint32_t &phase, bool issued) {
+  if (threadIdx.x == 0 && issued) tc::mma_commit(&s->bar);
+  const bool ok = !s->broken && tc::mbar_wait(&s->bar, phase);
+  if (!__syncthreads_and(ok)) {
+    if (threadIdx.x == 0) s->broken = 1;
+    return false;
   }
-  // flush: dW2 fragment -> shared, then everything -> global
-#pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-    int r0 = warp * 16 + g, c0 = nt * 8 + 2 * t;
-    s_g[SUR_OW2 + r0 * 64 + c0] += accW2[nt][0];
-    s_g[SUR_OW2 + r0 * 64 + c0 + 1] += accW2[nt][1];
-    s_g[SUR_OW2 + (r0 + 8) * 64 + c0] += accW2[nt][2];
-    s_g[SUR_OW2 + (r0 + 8) * 64 + c0 + 1] += accW2[nt][3];
-  }
-  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-  if (lane == 0) atomicAdd(loss, lsum);
+  phase ^= 1u;
+  tc::fence_after_sync();
+  return true;
+}
+__device__ __forceinline__ void gbarrier() {
+  tc::fence_async_smem();
+  tc::fence_before_sync();
   __syncthreads();
-  for (int q = threadIdx.x; q < SUR_NPARAM; q += blockDim.x) atomicAdd(&gout[q], s_g[q]);
+  tc::fence_after_sync();
+}
+
+__global__ void __launch_bounds__(128, 1) sur_grad_kernel(const SurNet *net, const float *x, const float *y,
+                                                          long long n, float inv_batch, float *gout, float *loss,
+                                                          int *err) {
+  extern __shared__ __align__(128) unsigned char grad_smem[];
+  SurGradSmem *s = reinterpret_cast<SurGradSmem *>(grad_smem);
+  const int r = threadIdx.x, w = r >> 5;
+  // set-up: weights in the operand layouts, the constant rows, TMEM
+  for (int q = r; q < 64 * 64; q += 128) {
+    const int o = q >> 6, i = q & 63;
+    *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(s->W2) + tc::kmajor_off(o, i, 64)) = net->W2[q];
+    *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(s->W2T) + tc::kmajor_off(i, o, 64)) = net->W2[q];
+  }
+  for (int q = r; q < 16 * 64; q += 128) {
+    const int o = q >> 6, i = q & 63;
+    *reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(s->W3) + tc::kmajor_off(o, i, 64)) =
+        o < 2 ? net->W3[q] : __float2bfloat16_rn(0.0f);
+  }
+  for (int q = r; q < 64; q += 128) {
+    const __nv_bfloat16 *wv = net->W1 + q * 16;
+    s->w1[q] = make_float4(__bfloat162float(wv[0]), __bfloat162float(wv[1]), __bfloat162float(wv[2]), net->b1[q]);
+    s->b2[q] = net->b2[q];
+    s->w3[0][q] = __bfloat162float(net->W3[q]);
+    s->w3[1][q] = __bfloat162float(net->W3[64 + q]);
+  }
+  if (r < 2) s->b3[r] = net->b3[r];
+  // column r (sample r) of the transposed operands: zero rows, the ones rows
+  for (int row = 64; row < 128; row++) {
+    gstore(s->dz2T, row, r, 128, 0.0f);
+    gstore(s->h2T, row, r, 128, row == 64 ? 1.0f : 0.0f);
+  }
+  for (int row = 64; row < 80; row++) gstore(s->h1T, row, r, 128, row == 64 ? 1.0f : 0.0f);
+  for (int row = 2; row < 16; row++) gstore(s->dT, row, r, 128, 0.0f);
+  for (int row = 3; row < 16; row++) gstore(s->xT, row, r, 128, row == 3 ? 1.0f : 0.0f);
+  if (r == 0) {
+    tc::mbar_init(&s->bar, 1);
+    s->broken = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (r < 32) tc::tmem_alloc(&s->tmem, kGCols);
+  gbarrier();
+  const uint32_t tm = s->tmem, lane_off = (uint32_t)(w * 32) << 16;
+  uint32_t phase = 0;
+  bool first = true, ok = true;
+  float lacc = 0.0f;
+  const long long ntile = (n + 127) / 128;
+  for (long long tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+    const long long smp = tile * 128 + r;
+    const bool act = smp < n;
+    const float n0 = act ? (x[3 * smp] - SUR_C0) / SUR_S0 : 0.0f;
+    const float n1 = act ? (x[3 * smp + 1] - SUR_C1) / SUR_S1 : 0.0f;
+    const float n2 = act ? (x[3 * smp + 2] - SUR_C2) / SUR_S2 : 0.0f;
+    // layer 1 (FP32), h1 into A and, transposed, into h1T
+    for (int kc = 0; kc < 8; kc++) {
+      float hv[8];
+      for (int q = 0; q < 8; q++) {
+        const float4 c = s->w1[8 * kc + q];
+        hv[q] = bf16_round(silu(c.w + c.x * n0 + c.y * n1 + c.z * n2));
+        gstore(s->h1T, 8 * kc + q, r, 128, act ? hv[q] : 0.0f);
+      }
+      gstore8(s->A, r, 8 * kc, 64, hv);
+    }
+    gstore(s->xT, 0, r, 128, n0);
+    gstore(s->xT, 1, r, 128, n1);
+    gstore(s->xT, 2, r, 128, n2);
+    gbarrier();
+    if (r == 0) gmma(tm + kGZ2, s->A, 64, s->W2, 64, 64, 4, false);
+    if (!(ok = gsync(s, phase, true))) break;
+    // h2 = bf16(SiLU(Z2 + b2)) into A and h2T
+    for (int cc = 0; cc < 4; cc++) {
+      float v[16];
+      tc::tmem_ld16(tm + lane_off + kGZ2 + 16 * cc, v);
+      tc::tmem_wait_ld();
+      for (int hf = 0; hf < 2; hf++) {
+        float hv[8];
+        for (int q = 0; q < 8; q++) {
+          const int k = 16 * cc + 8 * hf + q;
+          hv[q] = bf16_round(silu(v[8 * hf + q] + s->b2[k]));
+          gstore(s->h2T, k, r, 128, act ? hv[q] : 0.0f);
+        }
+        gstore8(s->A, r, 16 * cc + 8 * hf, 64, hv);
+      }
+    }
+    gbarrier();
+    if (r == 0) gmma(tm + kGY, s->A, 64, s->W3, 64, 16, 4, false);
+    if (!(ok = gsync(s, phase, true))) break;
+    float o0, o1;
+    tc::tmem_ld2(tm + lane_off + kGY, o0, o1);
+    tc::tmem_wait_ld();
+    o0 += s->b3[0];
+    o1 += s->b3[1];
+    float d0 = 0.0f, d1 = 0.0f;
+    if (act) {
+      const float e = o0 - y[smp];
+      const float tcf = log10f(fabsf(e) + 1e-4f);
+      d0 = 2.0f * e * inv_batch;
+      d1 = kConfWeight * 2.0f * (o1 - tcf) * inv_batch;
+      lacc += e * e;
+    }
+    gstore(s->dT, 0, r, 128, d0);
+    gstore(s->dT, 1, r, 128, d1);
+    // dz2 = (d W3) SiLU'(Z2 + b2): into A (K-major) and dz2T
+    for (int cc = 0; cc < 4; cc++) {
+      float v[16];
+      tc::tmem_ld16(tm + lane_off + kGZ2 + 16 * cc, v);
+      tc::tmem_wait_ld();
+      for (int hf = 0; hf < 2; hf++) {
+        float dv[8];
+        for (int q = 0; q < 8; q++) {
+          const int k = 16 * cc + 8 * hf + q;
+          dv[q] = (d0 * s->w3[0][k] + d1 * s->w3[1][k]) * dsilu(v[8 * hf + q] + s->b2[k]);
+          gstore(s->dz2T, k, r, 128, dv[q]);
+        }
+        gstore8(s->A, r, 16 * cc + 8 * hf, 64, dv);
+      }
+    }
+    gbarrier();
+    if (r == 0) {
+      gmma(tm + kGDH1, s->A, 64, s->W2T, 64, 64, 4, false);
+      gmma(tm + kGDW2, s->dz2T, 128, s->h1T, 128, 80, 8, !first);
+      gmma(tm + kGW3, s->h2T, 128, s->dT, 128, 16, 8, !first);
+    }
+    if (!(ok = gsync(s, phase, true))) break;
+    // dz1 = dh1 SiLU'(z1) into dz2T (its products are done), then [gW1 | gb1]
+    for (int cc = 0; cc < 4; cc++) {
+      float v[16];
+      tc::tmem_ld16(tm + lane_off + kGDH1 + 16 * cc, v);
+      tc::tmem_wait_ld();
+      for (int q = 0; q < 16; q++) {
+        const int k = 16 * cc + q;
+        const float4 c = s->w1[k];
+        const float z1 = c.w + c.x * n0 + c.y * n1 + c.z * n2;
+        gstore(s->dz2T, k, r, 128, act ? v[q] * dsilu(z1) : 0.0f);
+      }
+    }
+    gbarrier();
+    if (r == 0) gmma(tm + kGW1, s->dz2T, 128, s->xT, 128, 16, 8, !first);
+    if (!(ok = gsync(s, phase, true))) break;
+    first = false;
+  }
+  // the accumulators out: lane n of [dW2 | gb2] and [gW1 | gb1] (n < 64), lane
+  // k of [gW3 | gb3] (k <= 64); every warp takes part in the loads
+  if (ok && !first) {
+    float v[16];
+    for (int cc = 0; cc < 5; cc++) {
+      tc::tmem_ld16(tm + lane_off + kGDW2 + 16 * cc, v);
+      tc::tmem_wait_ld();
+      if (r < 64)
+        for (int q = 0; q < 16; q++) {
+          const int k = 16 * cc + q;
+          if (k < 64) atomicAdd(&gout[SUR_OW2 + r * 64 + k], v[q]);
+          else if (k == 64) atomicAdd(&gout[SUR_OB2 + r], v[q]);
+        }
+    }
+    tc::tmem_ld16(tm + lane_off + kGW3, v);
+    tc::tmem_wait_ld();
+    if (r < 64) {
+      atomicAdd(&gout[SUR_OW3 + r], v[0]);
+      atomicAdd(&gout[SUR_OW3 + 64 + r], v[1]);
+    } else if (r == 64) {
+      atomicAdd(&gout[SUR_OB3], v[0]);
+      atomicAdd(&gout[SUR_OB3 + 1], v[1]);
+    }
+    tc::tmem_ld16(tm + lane_off + kGW1, v);
+    tc::tmem_wait_ld();
+    if (r < 64) {
+      for (int c = 0; c < 3; c++) atomicAdd(&gout[SUR_OW1 + 3 * r + c], v[c]);
+      atomicAdd(&gout[SUR_OB1 + r], v[3]);
+    }
+  }
+  if (!ok && r == 0) atomicOr(err, ERRB_TC);
+  for (int o = 16; o > 0; o >>= 1) lacc += __shfl_xor_sync(0xffffffffu, lacc, o);
+  if ((r & 31) == 0) atomicAdd(loss, lacc);
+  // TMEM free once nothing of this CTA is in flight (a timed-out wait: one more bounded wait)
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (s->broken && r == 0) tc::mbar_wait(&s->bar, phase);
+  __syncthreads();
+  if (r < 32) tc::tmem_free(tm, kGCols);
+  if (r == 0) tc::mbar_inval(&s->bar);
 }
 
 __global__ void sur_adam_kernel(float *m, float *mom1, float *mom2, float *grad, float lr, float b1, float b2,
@@ -321,6 +385,22 @@ __global__ void sur_adam_kernel(float *m, float *mom1, float *mom2, float *grad,
   mom2[q] = v;
   m[q] -= lr * (a / c1) / (sqrtf(v / c2) + eps);
   grad[q] = 0.0f;
+}
+
+// one 128-thread CTA per SM (the kernel's 131 KB of operands), striding
+// over the batch's 128-sample tiles
+cudaError_t sur_grad_launch(const SurNet *net, const float *x, const float *y, long long n, float *g, float *loss,
+                            int *err, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int smem = (int)sizeof(SurGradSmem);
+  cudaError_t e = cudaFuncSetAttribute(sur_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const long long tiles = (n + 127) / 128;
+  const unsigned grid = (unsigned)(tiles < (long long)sms ? tiles : (long long)sms);
+  sur_grad_kernel<<<grid, 128, smem, st>>>(net, x, y, n, 1.0f / (float)n, g, loss, err);
+  return cudaGetLastError();
 }
 
 cudaError_t surrogate_pack(const float *master, SurNet *net, cudaStream_t s) {
@@ -417,7 +497,7 @@ int mhd_surrogate_grad(const float *params, const float *x, const float *y, long
   if (!params || !x || !y || !grad || n <= 0) return MHD_ERR_ARG;
   int r = sur_device(device);
   if (r) return r;
-  DevBuf dm, dnet, dx, dy, dg, dl;
+  DevBuf dm, dnet, dx, dy, dg, dl, derr;
   SCK(cudaMalloc(&dm.p, SUR_NPARAM * sizeof(float)));
   SCK(cudaMalloc(&dnet.p, sizeof(SurNet)));
   SCK(cudaMalloc(&dx.p, n * 3 * sizeof(float)));
@@ -430,9 +510,13 @@ int mhd_surrogate_grad(const float *params, const float *x, const float *y, long
   SCK(cudaMemset(dg.p, 0, SUR_NPARAM * sizeof(float)));
   SCK(cudaMemset(dl.p, 0, sizeof(float)));
   sur_pack_kernel<<<16, 256>>>(dm.as<float>(), dnet.as<SurNet>());
-  sur_grad_kernel<<<nb(n, 64) < 608 ? nb(n, 64) : 608, 128>>>(dnet.as<SurNet>(), dx.as<float>(), dy.as<float>(), n,
-                                                              1.0f / (float)n, dg.as<float>(), dl.as<float>());
-  SCK(cudaGetLastError());
+  SCK(cudaMalloc(&derr.p, sizeof(int)));
+  SCK(cudaMemset(derr.p, 0, sizeof(int)));
+  SCK(sur_grad_launch(dnet.as<SurNet>(), dx.as<float>(), dy.as<float>(), n, dg.as<float>(), dl.as<float>(),
+                      derr.as<int>(), nullptr));
+  int e = 0;
+  SCK(cudaMemcpy(&e, derr.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return MHD_ERR_CUDA;
   SCK(cudaMemcpy(grad, dg.p, SUR_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
   if (loss) {
     SCK(cudaMemcpy(loss, dl.p, sizeof(float), cudaMemcpyDeviceToHost));
@@ -450,7 +534,9 @@ int mhd_surrogate_train(float *params, long long n_data, int batch, int steps, f
   if (!params || n_data < batch || batch < 64 || steps < 0) return MHD_ERR_ARG;
   int r = sur_device(device);
   if (r) return r;
-  DevBuf dm, m1, m2, dg, dnet, dx, dy, dl;
+  DevBuf dm, m1, m2, dg, dnet, dx, dy, dl, derr;
+  SCK(cudaMalloc(&derr.p, sizeof(int)));
+  SCK(cudaMemset(derr.p, 0, sizeof(int)));
   SCK(cudaMalloc(&dm.p, SUR_NPARAM * sizeof(float)));
   SCK(cudaMalloc(&m1.p, SUR_NPARAM * sizeof(float)));
   SCK(cudaMalloc(&m2.p, SUR_NPARAM * sizeof(float)));
@@ -468,13 +554,12 @@ int mhd_surrogate_train(float *params, long long n_data, int batch, int steps, f
   SCK(cudaGetLastError());
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   long long nbatch = n_data / batch;
-  unsigned grid = nb(batch, 64) < 1216 ? nb(batch, 64) : 1216;
   double c1 = 1.0, c2 = 1.0;
   for (int s = 0; s < steps; s++) {
     long long off = (long long)(s % nbatch) * batch;
     sur_pack_kernel<<<16, 256>>>(dm.as<float>(), dnet.as<SurNet>());
-    sur_grad_kernel<<<grid, 128>>>(dnet.as<SurNet>(), dx.as<float>() + 3 * off, dy.as<float>() + off, batch,
-                                   1.0f / (float)batch, dg.as<float>(), dl.as<float>() + s);
+    SCK(sur_grad_launch(dnet.as<SurNet>(), dx.as<float>() + 3 * off, dy.as<float>() + off, batch, dg.as<float>(),
+                        dl.as<float>() + s, derr.as<int>(), nullptr));
     c1 *= b1;
     c2 *= b2;
     sur_adam_kernel<<<nb(SUR_NPARAM, 256), 256>>>(dm.as<float>(), m1.as<float>(), m2.as<float>(), dg.as<float>(), lr,
@@ -482,6 +567,9 @@ int mhd_surrogate_train(float *params, long long n_data, int batch, int steps, f
   }
   SCK(cudaGetLastError());
   SCK(cudaDeviceSynchronize());
+  int e = 0;
+  SCK(cudaMemcpy(&e, derr.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return MHD_ERR_CUDA;
   SCK(cudaMemcpy(params, dm.p, SUR_NPARAM * sizeof(float), cudaMemcpyDeviceToHost));
   if (history && steps > 0) {
     std::vector<float> h(steps);

@@ -6,8 +6,11 @@ kernels' gradients.
 Rounding points (mirroring code_tohoku_gb300/csrc/mhd_surrogate_net.cuh and
 mhd_surrogate.cu): inputs normalised in FP32; W1 rounded to BF16, first
 layer in FP32; hidden activations h1 = bf16(SiLU(z1)), h2 = bf16(SiLU(z2));
-W2, W3 rounded to BF16; dz2 rounded to BF16 where it enters the tensor-core
-products dW2 = dz2^T h1 and dh1 = dz2 W2.
+W2, W3 rounded to BF16; every gradient product runs on the tensor cores with
+BF16 operands: dz2 where it enters dW2 = dz2^T h1, gb2 = sum dz2 and
+dh1 = dz2 W2; the output gradients d where they enter gW3 = d^T h2 and
+gb3 = sum d; dz1 and the normalised inputs where they enter gW1 = dz1^T x
+and gb1 = sum dz1.
 """
 import numpy as np
 
@@ -81,16 +84,18 @@ def grad(p, X, Y):
     e = f["y"][:, 0] - np.asarray(Y, np.float64)
     tc = np.log10(np.abs(e) + 1e-4)
     d = np.stack([2 * e / B, CONF_WEIGHT * 2 * (f["y"][:, 1] - tc) / B], axis=1)
-    gW3 = d.T @ f["h2"]
-    gb3 = d.sum(0)
+    db = bf16(d.astype(np.float32)).astype(np.float64)
+    gW3 = db.T @ f["h2"]
+    gb3 = db.sum(0)
     dh2 = d @ bf16(W3).astype(np.float64)
     dz2 = dh2 * dsilu(f["z2"])
-    gb2 = dz2.sum(0)
     dz2b = bf16(dz2.astype(np.float32)).astype(np.float64)
+    gb2 = dz2b.sum(0)
     gW2 = dz2b.T @ f["h1"]
     dh1 = dz2b @ bf16(W2).astype(np.float64)
     dz1 = dh1 * dsilu(f["z1"])
-    gb1 = dz1.sum(0)
-    gW1 = dz1.T @ f["n"]
+    dz1b = bf16(dz1.astype(np.float32)).astype(np.float64)
+    gb1 = dz1b.sum(0)
+    gW1 = dz1b.T @ bf16(f["n"].astype(np.float32)).astype(np.float64)
     g = np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gW3.ravel(), gb3])
     return g, float(np.mean(e * e))
