@@ -71,10 +71,7 @@ __global__ void sur_pack_kernel(const float *m, SurNet *net) {
     net->W1[t] = __float2bfloat16_rn(k < 3 ? m[SUR_OW1 + o * 3 + k] : 0.0f);
   }
   if (t < 64 * 64) {
-    int o = t / 64, k = t % 64;
-    __nv_bfloat16 w = __float2bfloat16_rn(m[SUR_OW2 + t]);
-    net->W2[t] = w;
-    net->W2T[k * 64 + o] = w;
+    net->W2[t] = __float2bfloat16_rn(m[SUR_OW2 + t]);
   }
   if (t < 8 * 64) {
     int o = t / 64, k = t % 64;

@@ -8,14 +8,11 @@
 //   x2 = log10(dt/t_cool),  t_cool = P/((gamma-1)|Lambda|)
 // and the network maps (x0,x1,x2) -> (log10(T_new/T), c), where c is a
 // learned estimate of log10 of its own error.  Layers 3->64->64->2 with SiLU;
-// operands are BF16 (mma.sync m16n8k16, FP32 accumulate), biases FP32.
-//
-// Fragment layouts follow the PTX ISA for mma.m16n8k16 with .bf16: lane
-// l = 4g + t holds A rows g and g+8, columns 2t,2t+1 (and +8); B column g,
-// rows 2t,2t+1 (and +8); the accumulator rows g, g+8, columns 2t, 2t+1.
-// The accumulator of one layer is repacked in registers as the A operand
-// of the next, so a warp evaluates 16 samples per tile without shared
-// memory.
+// the 64-wide layers run on the fifth-generation tensor cores (tcgen05.mma
+// kind::f16, BF16 operands in shared memory, FP32 accumulators in tensor
+// memory), layer 1 and the biases in FP32 on the CUDA cores.  Inference
+// (below) and the training gradients (mhd_surrogate.cu) use the same
+// operand layout and rounding points.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -40,7 +37,6 @@ constexpr float SUR_C2 = 0.0f, SUR_S2 = 3.0f;
 struct SurNet {
   __nv_bfloat16 W1[64 * 16];    // [out][in padded to 16]
   __nv_bfloat16 W2[64 * 64];    // [out][in]
-  __nv_bfloat16 W2T[64 * 64];   // [in][out]   (backward: dh1 = dz2 W2)
   __nv_bfloat16 W3[8 * 64];     // [out padded to 8][in]
   float b1[64], b2[64], b3[8];
 };
@@ -50,145 +46,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<uint32_t *>(&v);
 }
 __device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
 __device__ __forceinline__ float silu(float z) { return z * sigm(z); }
 __device__ __forceinline__ float dsilu(float z) {
   float s = sigm(z);
   return s * (1.0f + z * (1.0f - s));
-}
-
-// First layer on the CUDA cores in FP32 (3 inputs are too few for a
-// tensor-core tile, and BF16 inputs would quantise log T to 0.3%): the
-// weights are the BF16-rounded values, the products and sums FP32.  Each
-// lane computes the entries it owns in the accumulator layout (rows g, g+8;
-// columns 8nt+2t, 8nt+2t+1), so the result feeds act_frags directly.
-__device__ __forceinline__ void layer1_fp32(const SurNet *net, float n0, float n1, float n2, int rowbase,
-                                            float (&z)[8][4]) {
-  int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  float a0 = __shfl_sync(0xffffffffu, n0, rowbase + g), a1 = __shfl_sync(0xffffffffu, n1, rowbase + g),
-        a2 = __shfl_sync(0xffffffffu, n2, rowbase + g);
-  float c0 = __shfl_sync(0xffffffffu, n0, rowbase + g + 8), c1 = __shfl_sync(0xffffffffu, n1, rowbase + g + 8),
-        c2 = __shfl_sync(0xffffffffu, n2, rowbase + g + 8);
-#pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-      int n = nt * 8 + 2 * t + q;
-      const __nv_bfloat16 *w = net->W1 + n * 16;
-      float w0 = __bfloat162float(w[0]), w1 = __bfloat162float(w[1]), w2 = __bfloat162float(w[2]);
-      float b = net->b1[n];
-      z[nt][q] = b + w0 * a0 + w1 * a1 + w2 * a2;
-      z[nt][2 + q] = b + w0 * c0 + w1 * c1 + w2 * c2;
-    }
-  }
-}
-
-// z = A W^T + b for a 64-wide layer; W is [64][K] bf16 with K = 16*nk
-template <int NK>
-__device__ __forceinline__ void layer64(const __nv_bfloat16 *W, const float *b, const uint32_t (&a)[NK][4],
-                                        float (&z)[8][4]) {
-  int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-    float b0 = b[nt * 8 + 2 * t], b1 = b[nt * 8 + 2 * t + 1];
-    z[nt][0] = b0; z[nt][1] = b1; z[nt][2] = b0; z[nt][3] = b1;
-    const __nv_bfloat16 *row = W + (nt * 8 + g) * (16 * NK);
-#pragma unroll
-    for (int kt = 0; kt < NK; kt++) mma_bf16(z[nt], a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
-  }
-}
-
-// accumulator (16 x 64) -> four A fragments of the next layer after SiLU
-__device__ __forceinline__ void act_frags(const float (&z)[8][4], uint32_t (&a)[4][4]) {
-#pragma unroll
-  for (int kt = 0; kt < 4; kt++) {
-    a[kt][0] = pack_bf16(silu(z[2 * kt][0]), silu(z[2 * kt][1]));
-    a[kt][1] = pack_bf16(silu(z[2 * kt][2]), silu(z[2 * kt][3]));
-    a[kt][2] = pack_bf16(silu(z[2 * kt + 1][0]), silu(z[2 * kt + 1][1]));
-    a[kt][3] = pack_bf16(silu(z[2 * kt + 1][2]), silu(z[2 * kt + 1][3]));
-  }
-}
-
-// output layer: y (16 x 8, columns 0,1 used) = A W3^T + b3
-__device__ __forceinline__ void layer_out(const SurNet *net, const uint32_t (&a)[4][4], float (&y)[4]) {
-  int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  float b0 = net->b3[2 * t], b1 = net->b3[2 * t + 1];
-  y[0] = b0; y[1] = b1; y[2] = b0; y[3] = b1;
-  const __nv_bfloat16 *row = net->W3 + g * 64;
-#pragma unroll
-  for (int kt = 0; kt < 4; kt++) mma_bf16(y, a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
-}
-
-// forward pass of the 16 samples whose inputs sit in lanes rowbase..rowbase+15;
-// returns (out0, out1) for the sample of lanes rowbase+r in that lane.
-__device__ __forceinline__ void net_forward16(const SurNet *net, float n0, float n1, float n2, int rowbase,
-                                              float &o0, float &o1) {
-  float z1[8][4];
-  layer1_fp32(net, n0, n1, n2, rowbase, z1);
-  uint32_t a1[4][4];
-  act_frags(z1, a1);
-  float z2[8][4];
-  layer64<4>(net->W2, net->b2, a1, z2);
-  uint32_t a2[4][4];
-  act_frags(z2, a2);
-  float y[4];
-  layer_out(net, a2, y);
-  // row r of the tile: r < 8 at lane 4r (y0,y1), r >= 8 at lane 4(r-8) (y2,y3)
-  int lane = threadIdx.x & 31;
-  int r = lane - rowbase;
-  int src = ((r & 7) << 2);
-  float v0 = __shfl_sync(0xffffffffu, y[0], src), v1 = __shfl_sync(0xffffffffu, y[1], src);
-  float v2 = __shfl_sync(0xffffffffu, y[2], src), v3 = __shfl_sync(0xffffffffu, y[3], src);
-  o0 = (r < 8) ? v0 : v2;
-  o1 = (r < 8) ? v1 : v3;
-}
-
-// ---------------------------------------------------------------------
-// Inference inside the solver (source32_stiff_kernel): the weights of one
-// block in shared memory, staged once per block, instead of per-lane loads
-// from global memory for every tile; W2 and W3 rows padded from 64 to 72
-// BF16 so that the eight rows a B fragment load touches fall in distinct
-// banks.  The activation is SiLU(z) = s + s tanh(s), s = z/2, evaluated on
-// BF16 pairs with the hardware tanh approximation (one MUFU operation for
-// two activations instead of two for one); the activations are BF16
-// operands of the next layer in any case, and the solver checks every
-// answer by its implicit residual.
-constexpr int SUR_LD = 72;   // padded row length of W2 / W3 in shared memory
-
-struct SurNetSmem {
-  float4 w1[64];                      // (w0, w1, w2, b1) of hidden unit n
-  float b2[64], b3[8];
-  __nv_bfloat16 W2[64 * SUR_LD];      // [out][in]
-  __nv_bfloat16 W3[8 * SUR_LD];       // [out padded to 8][in]
-};
-
-// all threads of the block call; a barrier follows inside
-__device__ __forceinline__ void sur_stage(const SurNet *net, SurNetSmem *s) {
-  for (int q = threadIdx.x; q < 64; q += blockDim.x) {
-    const __nv_bfloat16 *w = net->W1 + q * 16;
-    s->w1[q] = make_float4(__bfloat162float(w[0]), __bfloat162float(w[1]), __bfloat162float(w[2]), net->b1[q]);
-    s->b2[q] = net->b2[q];
-  }
-  for (int q = threadIdx.x; q < 8; q += blockDim.x) s->b3[q] = net->b3[q];
-  for (int q = threadIdx.x; q < 64 * 32; q += blockDim.x) {   // 32-bit words of W2
-    const int r = q >> 5, c = (q & 31) * 2;
-    *reinterpret_cast<uint32_t *>(&s->W2[r * SUR_LD + c]) = ld32(net->W2 + r * 64 + c);
-  }
-  for (int q = threadIdx.x; q < 8 * 32; q += blockDim.x) {
-    const int r = q >> 5, c = (q & 31) * 2;
-    *reinterpret_cast<uint32_t *>(&s->W3[r * SUR_LD + c]) = ld32(net->W3 + r * 64 + c);
-  }
-  __syncthreads();
 }
 
 // SiLU of two accumulator entries, packed as the BF16 pair of the next A
@@ -202,95 +65,6 @@ __device__ __forceinline__ uint32_t silu2_bf16(float z0, float z1) {
   return r;
 }
 
-__device__ __forceinline__ void act_frags_fast(const float (&z)[8][4], uint32_t (&a)[4][4]) {
-#pragma unroll
-  for (int kt = 0; kt < 4; kt++) {
-    a[kt][0] = silu2_bf16(z[2 * kt][0], z[2 * kt][1]);
-    a[kt][1] = silu2_bf16(z[2 * kt][2], z[2 * kt][3]);
-    a[kt][2] = silu2_bf16(z[2 * kt + 1][0], z[2 * kt + 1][1]);
-    a[kt][3] = silu2_bf16(z[2 * kt + 1][2], z[2 * kt + 1][3]);
-  }
-}
-
-__device__ __forceinline__ void net_forward16_smem(const SurNetSmem *s, float n0, float n1, float n2, int rowbase,
-                                                   float &o0, float &o1) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  // layer 1 on the CUDA cores in FP32 (accumulator layout, as layer1_fp32)
-  const float a0 = __shfl_sync(0xffffffffu, n0, rowbase + g), a1 = __shfl_sync(0xffffffffu, n1, rowbase + g),
-              a2 = __shfl_sync(0xffffffffu, n2, rowbase + g);
-  const float c0 = __shfl_sync(0xffffffffu, n0, rowbase + g + 8), c1 = __shfl_sync(0xffffffffu, n1, rowbase + g + 8),
-              c2 = __shfl_sync(0xffffffffu, n2, rowbase + g + 8);
-  float z[8][4];
-#pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-      const float4 w = s->w1[nt * 8 + 2 * t + q];
-      z[nt][q] = w.w + w.x * a0 + w.y * a1 + w.z * a2;
-      z[nt][2 + q] = w.w + w.x * c0 + w.y * c1 + w.z * c2;
-    }
-  }
-  uint32_t a[4][4];
-  act_frags_fast(z, a);
-  // layer 2 on the tensor cores
-#pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-    const float b0 = s->b2[nt * 8 + 2 * t], b1 = s->b2[nt * 8 + 2 * t + 1];
-    z[nt][0] = b0; z[nt][1] = b1; z[nt][2] = b0; z[nt][3] = b1;
-    const __nv_bfloat16 *row = s->W2 + (nt * 8 + g) * SUR_LD;
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) mma_bf16(z[nt], a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
-  }
-  act_frags_fast(z, a);
-  // output layer
-  float y[4];
-  {
-    const float b0 = s->b3[2 * t], b1 = s->b3[2 * t + 1];
-    y[0] = b0; y[1] = b1; y[2] = b0; y[3] = b1;
-    const __nv_bfloat16 *row = s->W3 + g * SUR_LD;
-#pragma unroll
-    for (int kt = 0; kt < 4; kt++) mma_bf16(y, a[kt], ld32(row + kt * 16 + 2 * t), ld32(row + kt * 16 + 8 + 2 * t));
-  }
-  const int r = lane - rowbase;
-  const int src = ((r & 7) << 2);
-  const float v0 = __shfl_sync(0xffffffffu, y[0], src), v1 = __shfl_sync(0xffffffffu, y[1], src);
-  const float v2 = __shfl_sync(0xffffffffu, y[2], src), v3 = __shfl_sync(0xffffffffu, y[3], src);
-  o0 = (r < 8) ? v0 : v2;
-  o1 = (r < 8) ? v1 : v3;
-}
-
-// whole-warp inference from the staged weights (all 32 lanes call)
-__device__ __forceinline__ float surrogate_warp_smem(const SurNetSmem *s, float x0, float x1, float x2, bool active,
-                                                     float *conf) {
-  const float n0 = active ? (x0 - SUR_C0) / SUR_S0 : 0.0f;
-  const float n1 = active ? (x1 - SUR_C1) / SUR_S1 : 0.0f;
-  const float n2 = active ? (x2 - SUR_C2) / SUR_S2 : 0.0f;
-  float o0a = 0.0f, o1a = 0.0f, o0b = 0.0f, o1b = 0.0f;
-  const unsigned any = __ballot_sync(0xffffffffu, active);
-  if (any & 0x0000ffffu) net_forward16_smem(s, n0, n1, n2, 0, o0a, o1a);
-  if (any & 0xffff0000u) net_forward16_smem(s, n0, n1, n2, 16, o0b, o1b);
-  const int lane = threadIdx.x & 31;
-  *conf = lane < 16 ? o1a : o1b;
-  return lane < 16 ? o0a : o0b;
-}
-
-// Whole-warp inference: every lane brings one sample (all 32 lanes must
-// call).  Returns log10(T_new/T) and writes the confidence estimate.
-__device__ __forceinline__ float surrogate_warp(const SurNet *net, float x0, float x1, float x2, bool active,
-                                                float *conf) {
-  float n0 = active ? (x0 - SUR_C0) / SUR_S0 : 0.0f;
-  float n1 = active ? (x1 - SUR_C1) / SUR_S1 : 0.0f;
-  float n2 = active ? (x2 - SUR_C2) / SUR_S2 : 0.0f;
-  float o0a, o1a, o0b, o1b;
-  unsigned any = __ballot_sync(0xffffffffu, active);
-  o0a = o1a = o0b = o1b = 0.0f;
-  if (any & 0x0000ffffu) net_forward16(net, n0, n1, n2, 0, o0a, o1a);
-  if (any & 0xffff0000u) net_forward16(net, n0, n1, n2, 16, o0b, o1b);
-  int lane = threadIdx.x & 31;
-  *conf = lane < 16 ? o1a : o1b;
-  return lane < 16 ? o0a : o0b;
-}
-
 // ---------------------------------------------------------------------
 // Inference on the fifth-generation tensor cores (tcgen05), for SOURCE's
 // stiff cells: a CTA of 128 * NT threads holds NT tiles of 128 cells, one
@@ -301,8 +75,7 @@ __device__ __forceinline__ float surrogate_warp(const SurNet *net, float x0, flo
 // output layer (N padded to 16) as tcgen05.mma with the FP32 accumulators
 // in tensor memory (64 columns per tile, reused by the output layer);
 // every thread reads its row back with tcgen05.ld, adds the bias and applies
-// SiLU for the next layer.  SiLU(z) = s + s tanh(s), s = z/2, on BF16 pairs
-// as in net_forward16_smem.
+// SiLU for the next layer: silu2_bf16 above.
 
 template <int NT>
 struct SurTileSmem {
