@@ -41,6 +41,10 @@ struct Mhd1D {
   double CFL = 0.49, facdep = 1.0, tfinal = 40.0;
   int BCx1 = 1, BCx2 = 1, iflag = 0, ifthrm = 2;
   int brio_wu = 0;   // 1DMHDwCC3bw.f90: gamma=2 in RHS sound speed + Couran, SOURCE off
+  // RHS's RIEMAN iterations: 5 in the 1D codes (1DMHDwCC3.f90, itrn = 5);
+  // the 3D code unrolls 4 (MCF3DSGincfca3.f90:1500-1546, its loop
+  // commented out), which a test sets here to compare the two schemes
+  int itrn = 5;
 
   // state
   int Ncell = 0, nd = 0;
@@ -210,7 +214,7 @@ struct Mhd1D {
               (3.0 * (ndHm + ndpm + ndHem + ndHepm) + 5.0 * ndH2m);
       gammi1 = gamma - 1.0; gammi2 = gamma - 2.0; gammi3 = gamma - 3.0;
       gampl1 = gamma + 1.0; gampl2 = gamma + 2.0; gampl3 = gamma + 3.0;
-      RIEMAN(QL1, QL2, QL3, QL4, QR1, QR2, QR3, QR4, Pa[i + 1], VA(i), 5);
+      RIEMAN(QL1, QL2, QL3, QL4, QR1, QR2, QR3, QR4, Pa[i + 1], VA(i), itrn);
     }
     for (int i = 0; i <= Ncell; i++) {
       dm[i + 1] = DX(i) * U(i, 1);
@@ -468,14 +472,20 @@ struct Mhd1D {
     }
   }
 
-  // one in20 iteration of EVOLVE (1DMHDwCC3.f90:254-277); returns dt
-  double step() {
+  // one in20 iteration of EVOLVE (1DMHDwCC3.f90:254-277); returns dt.
+  // dt_given > 0 replaces the Couran/Stblty limit (a test drives this code
+  // with the 3D code's steps, whose Stblty differs)
+  double step(double dt_given = -1.0) {
     double dt = tfinal;
-    double tLMT = Couran();
-    dt = fmin2(dt, CFL * tLMT);
-    if (ifthrm == 2) {
-      tLMT = Stblty();
-      dt = fmin2(dt, 0.2 * tLMT);
+    if (dt_given > 0.0) {
+      dt = dt_given;
+    } else {
+      double tLMT = Couran();
+      dt = fmin2(dt, CFL * tLMT);
+      if (ifthrm == 2) {
+        tLMT = Stblty();
+        dt = fmin2(dt, 0.2 * tLMT);
+      }
     }
     if (time + dt > tfinal) dt = tfinal - time;
     if (!brio_wu) SOURCE(dt * 0.5);
@@ -529,6 +539,8 @@ void *o1d_create(const double *d) {
 int o1d_ncell(void *h) { return static_cast<Mhd1D *>(h)->Ncell; }
 double o1d_time(void *h) { return static_cast<Mhd1D *>(h)->time; }
 double o1d_step(void *h) { return static_cast<Mhd1D *>(h)->step(); }
+void o1d_set_riemann_iterations(void *h, int n) { static_cast<Mhd1D *>(h)->itrn = n; }
+double o1d_step_dt(void *h, double dt) { return static_cast<Mhd1D *>(h)->step(dt); }
 
 // Runs nsteps iterations and records the cooling.dat row after each:
 // time, U(512,1)/1.27, U(512,5)*1.52/1.38*100, U(510,7)  (1DMHDwCC3.f90:277)

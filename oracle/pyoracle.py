@@ -40,6 +40,10 @@ def lib():
         L.o1d_time.argtypes = [ctypes.c_void_p]
         L.o1d_step.restype = ctypes.c_double
         L.o1d_step.argtypes = [ctypes.c_void_p]
+        L.o1d_step_dt.restype = ctypes.c_double
+        L.o1d_step_dt.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.o1d_set_riemann_iterations.restype = None
+        L.o1d_set_riemann_iterations.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.o1d_run_trace.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
         L.o1d_state.argtypes = [ctypes.c_void_p, _P]
         L.o1d_destroy.argtypes = [ctypes.c_void_p]
@@ -88,6 +92,14 @@ class Oracle1D:
 
     def step(self):
         return lib().o1d_step(self.h)
+
+    def step_dt(self, dt):
+        """One step of the given length instead of the Couran/Stblty one."""
+        return lib().o1d_step_dt(self.h, float(dt))
+
+    def set_riemann_iterations(self, n):
+        """RHS's RIEMAN iteration count (5 in the 1D codes, 4 in the 3D one)."""
+        lib().o1d_set_riemann_iterations(self.h, int(n))
 
     @property
     def time(self):
