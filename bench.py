@@ -590,7 +590,7 @@ def main():
         grav = {"workload": f"the headline problem with self-gravity, {args.n}^3", "steps": 5,
                 "ms_per_step_with_gravity": msg / 5, "ms_per_step_without": ms32 / args.steps,
                 "phase_ms": {k: v for k, v in phg.items() if k.startswith("gravity")},
-                "potential_solve": "radix-2 FFTs in y and z, a tridiagonal x solve per mode (FP64)"}
+                "potential_solve": "radix-4 FFTs in y (two real z rows per complex transform) and z over the half spectrum, a tridiagonal x solve per mode from tabulated coefficients (FP64)"}
         del gg
 
     # config 2: 128^3 decaying Mach-5 MHD turbulence, plain FP64, steps 1..100

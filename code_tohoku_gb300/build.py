@@ -32,7 +32,7 @@ UNITS = {
     "mhd_surrogate.cu": ["--fmad=false"],
     "mhd_noalloc.cu": ["--fmad=false"],
     "mhd_peak.cu": [],
-    "mhd_gravity.cu": ["--fmad=false"],
+    "mhd_gravity.cu": [],
     "mhd_io.cpp": [],
 }
 

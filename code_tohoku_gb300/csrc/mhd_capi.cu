@@ -59,8 +59,9 @@ struct mhd_handle {
   // Thomas scratch, the twiddles for ny and nz, and the grid scalars the
   // solve and the kick read (from the last mhd_upload)
   double *phi = nullptr;
-  void *gwork = nullptr;
-  double *gcp = nullptr;
+  void *gwork = nullptr;                  // the half spectrum
+  double *gtab = nullptr;                 // the grid's tables (built at the first solve after an upload)
+  bool gtab_ready = false;
   void *gtw = nullptr;
   double g_dx = 0.0, g_dy = 0.0, g_dz = 0.0, g_dx0 = 0.0, g_x0 = 0.0, g_lbox = 0.0;
   bool inflow_set = false;
@@ -175,13 +176,19 @@ int gravity_potential(mhd_handle *h) {
   a.g = h->g;
   a.rho = h->f.U[0];
   a.phi = h->phi;
-  a.w = static_cast<double2 *>(h->gwork);
-  a.cp = h->gcp;
+  a.S = static_cast<double2 *>(h->gwork);
+  a.tab = h->gtab;
   a.tw_y = static_cast<const double2 *>(h->gtw);
   a.tw_z = a.tw_y + (h->g.n[1] / 2 > 0 ? h->g.n[1] / 2 : 1) * 2;
   a.dx = h->g_dx; a.dy = h->g_dy; a.dz = h->g_dz; a.x0 = h->g_x0; a.lbox = h->g_lbox;
+  if (!h->gtab_ready) {
+    CK(gravity_tables(a, h->stream));
+    h->launches += 1;
+    h->gtab_ready = true;
+  }
   CK(gravity_solve(a, h->stream));
-  h->launches += 9;    // ten kernels: the load, four transforms, the mode solve, the store, three ghost passes
+  // the y transform, z transform, mode solve, inverse z, inverse y, three ghost passes
+  h->launches += (h->g.n[2] > 1) ? 8 : 6;
   return MHD_OK;
 }
 int gravity_half_kick(mhd_handle *h, double dt) {
@@ -288,11 +295,11 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
     for (int q = 0; q < 10; q++) h->f.col[q] = h->colblock + (size_t)q * g.ncell;
   }
   if (p->ifgrv == 2) {
-    const size_t nint = (size_t)g.n[0] * g.n[1] * g.n[2];
+    const size_t nspec = gravity_spectrum_size(g);
     std::vector<double2> ty = gravity_twiddles(g.n[1]), tz = gravity_twiddles(g.n[2]);
     bool okg = cudaMalloc(&h->phi, (size_t)g.ncell * sizeof(double)) == cudaSuccess &&
-               cudaMalloc(&h->gwork, nint * sizeof(double2)) == cudaSuccess &&
-               cudaMalloc(&h->gcp, nint * sizeof(double)) == cudaSuccess &&
+               cudaMalloc(&h->gwork, nspec * sizeof(double2)) == cudaSuccess &&
+               cudaMalloc(&h->gtab, 4 * nspec * sizeof(double)) == cudaSuccess &&
                cudaMalloc(&h->gtw, (ty.size() + tz.size()) * sizeof(double2)) == cudaSuccess &&
                cudaMemcpy(h->gtw, ty.data(), ty.size() * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess &&
                cudaMemcpy(static_cast<double2 *>(h->gtw) + ty.size(), tz.data(), tz.size() * sizeof(double2),
@@ -368,7 +375,7 @@ int mhd_destroy(mhd_handle *h) {
   cudaFree(h->dtlo);
   cudaFree(h->phi);
   cudaFree(h->gwork);
-  cudaFree(h->gcp);
+  cudaFree(h->gtab);
   cudaFree(h->gtw);
   cudaFree(h->err);
   cudaFree(h->sur_master);
@@ -461,6 +468,7 @@ int mhd_upload(mhd_handle *h, const double *U, const double *species, const doub
     // cell 1, index 1 is x(0)
     h->g_dx = dx[2]; h->g_dy = dy[2]; h->g_dz = dz[2]; h->g_dx0 = dx[1];
     h->g_x0 = x[1]; h->g_lbox = x[g.n[0] + 1] - x[1];
+    h->gtab_ready = false;   // new coordinates: new tables
     TRY(gravity(h, 0.0, false));
   }
   CKR(cudaStreamSynchronize(h->stream));

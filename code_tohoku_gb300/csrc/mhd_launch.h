@@ -78,13 +78,15 @@ struct GravityArgs {
   Grid g;
   const double *rho;
   double *phi;                       // padded layout of U
-  double2 *w;                        // nx ny nz complex work
-  double *cp;                        // nx ny nz doubles of Thomas scratch
+  double2 *S;                        // the half spectrum, gravity_spectrum_size complex values
+  double *tab;                       // the grid's tables: 4 gravity_spectrum_size doubles
   const double2 *tw_y, *tw_z;        // twiddles (gravity_twiddles) for ny and nz
   double dx, dy, dz, x0, lbox;       // dx(1), dy(1), dz(1), x(0), x(nx) - x(0)
 };
 bool gravity_size_ok(int n);          // a power of two up to 1024
+size_t gravity_spectrum_size(const Grid &g);   // nx nz (ny/2 + 1)
 std::vector<double2> gravity_twiddles(int n);
+cudaError_t gravity_tables(const GravityArgs &a, cudaStream_t s);   // once per grid
 cudaError_t gravity_solve(const GravityArgs &a, cudaStream_t s);
 cudaError_t gravity_kick(const Grid &g, const Fields &f, const double *phi, double dt, double dx0, cudaStream_t s);
 
