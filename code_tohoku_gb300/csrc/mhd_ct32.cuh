@@ -194,6 +194,116 @@ __global__ void __launch_bounds__(128) emf32_kernel(CT32Args A) {
   A.emf[E][p0] = 0.25f * (v1a * B2a - v2a * B1a) * (dncv * dsqinv);
 }
 
+// Packed FP32 pairs for emf32x2_kernel: Blackwell's paired FP32 add, multiply
+// and fused multiply-add (one instruction for both lanes).
+__device__ __forceinline__ float2 p2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pabs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+
+// vlim_w of two quantities (lanes) that share the widths and the switch
+__device__ __forceinline__ float2 vlim_w2(float2 qm, float2 q0, float2 qp, const LimW &w) {
+  if (w.s > 0.0f) {
+    const float2 dp = pmul(psub(qp, q0), p2(w.rp, w.rp)), dm = pmul(psub(q0, qm), p2(w.rm, w.rm));
+    const float2 pr = pmul(dp, dm);
+    return p2(pr.x > 0.0f ? copysignf(fminf(fabsf(dp.x), fabsf(dm.x)), dp.x) : 0.0f,
+              pr.y > 0.0f ? copysignf(fminf(fabsf(dp.y), fabsf(dm.y)), dp.y) : 0.0f);
+  }
+  const float2 delp = psub(qp, q0), delm = psub(q0, qm);
+  const float2 eps = p2(1e-10f, 1e-10f);
+  const float2 num = pfma(pmul(p2(2.0f, 2.0f), delp), delm, eps);
+  const float2 den = pfma(delp, delp, pfma(delm, delm, eps));
+  const float2 fl = p2(fmaxf(0.0f, __fdividef(num.x, den.x)), fmaxf(0.0f, __fdividef(num.y, den.y)));
+  return pmul(pmul(fl, psub(qp, qm)), p2(w.ra, w.ra));
+}
+
+// emf32_kernel with the two characteristic combinations of every candidate
+// in the two lanes of packed FP32 pairs: lane x the (+, -) pair (C1p, C2m),
+// lane y the (-, +) pair (C1m, C2p), which do the same arithmetic on their
+// own inputs; the slopes of V and B along a direction share their widths
+// and switch, so they form a pair too.  32-bit cell offsets (the padded grid
+// has fewer than 2^31 cells).
+template <int E>
+__global__ void __launch_bounds__(128) emf32x2_kernel(CT32Args A) {
+  const Grid &g = A.g;
+  constexpr int da = E, db = (E + 1) % 3, dc = (E + 2) % 3;
+  int ext[3];
+  ext[da] = g.n[da] + 1; ext[db] = g.n[db] + 1; ext[dc] = g.n[dc];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)ext[0] * ext[1] * ext[2]) return;
+  int c3[3];
+  split3(t, ext[0], ext[1], c3[0], c3[1], c3[2]);
+  c3[0] += 1; c3[1] += 1; c3[2] += 1;
+  const int aa = c3[da], bb = c3[db];
+  const int p0 = (int)gidx(g, c3[0], c3[1], c3[2]);
+  const int sa = (int)g.st[da], sb = (int)g.st[db];
+  const float *rn = A.rn, *sw = A.sw;
+  const float dncv = 0.25f * (rn[p0] + rn[p0 - sa] + rn[p0 - sb] + rn[p0 - sa - sb]);
+  const float dsqinv = rsqrtf(dncv);
+  const float facm = A.facm, dt = A.dt;
+  const float *Vx = A.vf[da], *Vy = A.vf[db], *Bxf = A.bf[da], *Byf = A.bf[db];
+  const float *dxe = g.dxf[da], *dye = g.dxf[db];
+  const float dxm = dxe[aa], dx0 = dxe[aa + 1], dym = dye[bb], dy0 = dye[bb + 1];
+  const float2 sq = p2(dsqinv, -dsqinv), fm = p2(facm, facm);
+  // (v + b s, v - b s) and ((q_v + q_b s) facm, (q_v - q_b s) facm), s = 1/sqrt(rho)
+  auto chars = [&](const float *V, const float *B, int p, int sd, const float *dxx, int pos, float2 &a, float2 &d) {
+    const LimW w = lim_w(dxx[pos], dxx[pos + 1], dxx[pos + 2], sw[p]);
+    const float2 q = vlim_w2(p2(V[p - sd], B[p - sd]), p2(V[p], B[p]), p2(V[p + sd], B[p + sd]), w);
+    const float v = V[p], b = B[p];
+    a = pfma(p2(b, b), sq, p2(v, v));
+    d = pmul(pfma(p2(q.y, q.y), sq, p2(q.x, q.x)), fm);
+  };
+  float2 a1L, d1L, a1R, d1R, a2L, d2L, a2R, d2R;
+  chars(Vx, Bxf, p0 - sb, sb, dye, bb - 1, a1L, d1L);   // (a, b-1): (a1p, a1m), (da1p, da1m)
+  chars(Vx, Bxf, p0, sb, dye, bb, a1R, d1R);            // (a, b)
+  chars(Vy, Byf, p0 - sa, sa, dxe, aa - 1, a2L, d2L);   // (a-1, b): (a2p, a2m), (da2p, da2m)
+  chars(Vy, Byf, p0, sa, dxe, aa, a2R, d2R);            // (a, b)
+  auto swp = [](float2 v) { return make_float2(v.y, v.x); };
+  const float2 mdt = p2(-dt, -dt), mdt2 = p2(-dt * dt, -dt * dt), one = p2(1.0f, 1.0f);
+  auto cand = [&](float2 a1, float2 d1, float2 a2, float2 d2, float dyv, float dxv, float2 &C1, float2 &C2) {
+    const float2 A1 = pfma(d1, p2(dyv, dyv), a1), A2 = pfma(d2, p2(dxv, dxv), a2);
+    const float2 den = pfma(pmul(d1, d2), mdt2, one);
+    const float2 r = p2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+    C1 = pmul(pfma(pmul(d1, A2), mdt, A1), r);
+    C2 = pmul(pfma(pmul(d2, A1), mdt, A2), r);
+  };
+  // the second-side quantities enter as (a2m, a2p): the lanes swapped
+  float2 C1LL, C2LL, C1RL, C2RL, C1LR, C2LR, C1RR, C2RR;
+  cand(a1L, d1L, swp(a2L), swp(d2L), dym, dxm, C1LL, C2LL);     // S1 = +1, S2 = +1
+  cand(a1R, d1R, swp(a2L), swp(d2L), -dy0, dxm, C1RL, C2RL);    // S1 = -1, S2 = +1
+  cand(a1L, d1L, swp(a2R), swp(d2R), dym, -dx0, C1LR, C2LR);    // S1 = +1, S2 = -1
+  cand(a1R, d1R, swp(a2R), swp(d2R), -dy0, -dx0, C1RR, C2RR);   // S1 = -1, S2 = -1
+  const bool w11 = C1LL.x > 0.0f && C2LL.x > 0.0f, w12 = C1LL.y > 0.0f && C2LL.y > 0.0f;
+  const bool w21 = C1RL.x > 0.0f && C2RL.x < 0.0f, w22 = C1RL.y > 0.0f && C2RL.y < 0.0f;
+  const bool w31 = C1LR.x < 0.0f && C2LR.x > 0.0f, w32 = C1LR.y < 0.0f && C2LR.y > 0.0f;
+  const bool w41 = C1RR.x < 0.0f && C2RR.x < 0.0f, w42 = C1RR.y < 0.0f && C2RR.y < 0.0f;
+  // weight w + (1e13-1) * int(0.51 w1 + 0.51 w2): the boost is w1 AND w2
+  const float big = 1.e13f - 1.0f;
+  auto Wp = [&](bool x, bool y) {
+    const float b = (x && y) ? big : 0.0f;
+    return p2((x ? 1.0f : 0.0f) + b, (y ? 1.0f : 0.0f) + b);
+  };
+  float2 n1 = p2(0.0f, 0.0f), e1 = n1, n2 = n1, e2 = n1;
+  auto acc = [&](float2 W, float2 C1, float2 C2) {
+    const float2 u = pmul(W, pabs(C2)), v = pmul(W, pabs(C1));
+    e1 = padd(e1, u);
+    n1 = pfma(u, C1, n1);
+    e2 = padd(e2, v);
+    n2 = pfma(v, C2, n2);
+  };
+  acc(Wp(w11, w12), C1LL, C2LL);
+  acc(Wp(w21, w22), C1RL, C2RL);
+  acc(Wp(w31, w32), C1LR, C2LR);
+  acc(Wp(w41, w42), C1RR, C2RR);
+  const bool anyx = w11 || w21 || w31 || w41, anyy = w12 || w22 || w32 || w42;
+  const float C1p = anyx ? __fdividef(n1.x, e1.x) : 0.0f, C2m = anyx ? __fdividef(n2.x, e2.x) : 0.0f;
+  const float C1m = anyy ? __fdividef(n1.y, e1.y) : 0.0f, C2p = anyy ? __fdividef(n2.y, e2.y) : 0.0f;
+  const float v1a = C1p + C1m, v2a = C2p + C2m, B1a = C1p - C1m, B2a = C2p - C2m;
+  A.emf[E][p0] = 0.25f * (v1a * B2a - v2a * B1a) * (dncv * dsqinv);
+}
+
 // dt/dx(i) of every coordinate of the three axes (concatenated), once per
 // CT: face_b32 reads them instead of forming three FP64 products per cell
 // on the narrow FP64 pipe (the same products, so the update is unchanged)

@@ -63,6 +63,13 @@ constexpr int kSweepLongStride = MHD_SWEEP_LONG_STRIDE;
 #define MHD_SWEEP_Z_THREADS 1024
 #endif
 constexpr int kSweepZThreads = MHD_SWEEP_Z_THREADS;
+#ifndef MHD_EMF_PACKED
+#define MHD_EMF_PACKED 0
+#endif
+#ifndef MHD_SWEEP_Z_PENCILS
+#define MHD_SWEEP_Z_PENCILS 8
+#endif
+constexpr int kSweepZPencils = MHD_SWEEP_Z_PENCILS;
 
 template <int DIR, int P, int LS, int NT, int MINB>
 static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
@@ -95,8 +102,8 @@ static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
   // within a page or two, is faster with four: 2.41 against 2.52, and the x
   // sweep with four rows and two CTAs: 2.16 against 2.58)
   if constexpr (DIR == 2) {
-    if (L <= kSweepFixedStride && sweep32_smem_bytes(a.g.n[DIR], 8, kSweepFixedStride) <= 226 * 1024)
-      return launch32<DIR, 8, kSweepFixedStride, kSweepZThreads, 1>(a, s);
+    if (L <= kSweepFixedStride && sweep32_smem_bytes(a.g.n[DIR], kSweepZPencils, kSweepFixedStride) <= 226 * 1024)
+      return launch32<DIR, kSweepZPencils, kSweepFixedStride, kSweepZThreads, 1>(a, s);
   }
   if (MHD_SWEEP_MAX_PENCILS >= 4 && nb % 4 == 0 && L <= kSweepFixedStride &&
       sweep32_smem_bytes(a.g.n[DIR], 4, kSweepFixedStride) <= kSweepSmemPerCta)
@@ -162,7 +169,11 @@ static cudaError_t emf32_e(const CT32Args &a, cudaStream_t s) {
   const Grid &g = a.g;
   constexpr int da = E, db = (E + 1) % 3, dc = (E + 2) % 3;
   long long n = (long long)(g.n[da] + 1) * (g.n[db] + 1) * g.n[dc];
+#if MHD_EMF_PACKED
+  emf32x2_kernel<E><<<blocks_for(n, 128), 128, 0, s>>>(a);
+#else
   emf32_kernel<E><<<blocks_for(n, 128), 128, 0, s>>>(a);
+#endif
   return cudaGetLastError();
 }
 

@@ -143,3 +143,4 @@ def test_network_gain_over_the_same_solver_without_it(trained):
         assert d["surrogate_cells"] >= 0.9 * n_stiff, (name, d)
     assert max(l1.values()) < 1e-3, l1
     assert 10.0 * l1["surrogate"] < l1["newton"], l1
+
