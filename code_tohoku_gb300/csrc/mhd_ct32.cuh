@@ -8,8 +8,8 @@
 //   ct_prep32         one pass over the padded grid after those exchanges:
 //                     FP32 copies of the face velocities, face B, rho and
 //                     VLIMIT's T switch, so the EMF kernels load only FP32
-//   emf32<E>          CC(2) + CCT for the edges along E, thread per edge,
-//                     FP32 loads, FP32 arithmetic, FP32 EMF
+//   emf32x2<E>        CC(2) + CCT for the edges along E, thread per edge,
+//                     FP32 loads, FP32 arithmetic in packed pairs, FP32 EMF
 //   face_b32          CC(3): B_face += dt/dy (E(j+1)-E(j)) - ..., the EMF
 //                     differences taken in FP64 from the FP32 values, so the
 //                     discrete div B of the update cancels to FP64 round-off
@@ -85,117 +85,8 @@ __global__ void __launch_bounds__(256) ct_prep32_kernel(long long ncell, Fields 
   }
 }
 
-// CC(2) + CCT for the edge direction E (0: Ez on x/y, 1: Ex on y/z,
-// 2: Ey on z/x): the arithmetic of emf_kernel (:2140-2157, :2186-2445) in
-// FP32 on FP32 inputs.
-template <int E>
-__global__ void __launch_bounds__(128) emf32_kernel(CT32Args A) {
-  const Grid &g = A.g;
-  constexpr int da = E, db = (E + 1) % 3, dc = (E + 2) % 3;
-  // edges: n+1 positions along da and db, n along dc; the thread index
-  // runs fastest along x whatever E is, so neighbouring threads load
-  // neighbouring words
-  int ext[3];
-  ext[da] = g.n[da] + 1; ext[db] = g.n[db] + 1; ext[dc] = g.n[dc];
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)ext[0] * ext[1] * ext[2]) return;
-  int c3[3];
-  split3(t, ext[0], ext[1], c3[0], c3[1], c3[2]);
-  c3[0] += 1; c3[1] += 1; c3[2] += 1;
-  const int aa = c3[da], bb = c3[db];
-  long long p0 = gidx(g, c3[0], c3[1], c3[2]);
-  const long long sa = g.st[da], sb = g.st[db];
-  const float *rn = A.rn, *sw = A.sw;
-  const float dncv = 0.25f * (rn[p0] + rn[p0 - sa] + rn[p0 - sb] + rn[p0 - sa - sb]);
-  const float *Vx = A.vf[da], *Vy = A.vf[db];
-  const float *Bxf = A.bf[da], *Byf = A.bf[db];
-  const float dsqinv = rsqrtf(dncv);
-  const float facm = A.facm, dt = A.dt;
-  const float *dxe = g.dxf[da], *dye = g.dxf[db];
-  const float dxm = dxe[aa], dx0 = dxe[aa + 1], dym = dye[bb], dy0 = dye[bb + 1];
-  // VLIMIT of two face arrays along direction d at cell c (T switch of cell
-  // c): the same widths and switch, so the divisors are formed once
-  auto slopes = [&](const float *q, const float *r, long long c, long long sd, const float *dxx, int pos,
-                    float &sq, float &sr) {
-    const LimW w = lim_w(dxx[pos], dxx[pos + 1], dxx[pos + 2], sw[c]);
-    sq = vlim_w(q[c - sd], q[c], q[c + sd], w);
-    sr = vlim_w(r[c - sd], r[c], r[c + sd], w);
-  };
-  auto load1 = [&](long long p, int bpos, float &a1p, float &a1m, float &da1p, float &da1m) {
-    float v = Vx[p], b = Bxf[p];
-    float q1, q3;
-    slopes(Vx, Bxf, p, sb, dye, bpos, q1, q3);
-    a1p = v + b * dsqinv;
-    da1p = (q1 + q3 * dsqinv) * facm;
-    a1m = v - b * dsqinv;
-    da1m = (q1 - q3 * dsqinv) * facm;
-  };
-  auto load2 = [&](long long p, int apos, float &a2m, float &a2p, float &da2m, float &da2p) {
-    float v = Vy[p], b = Byf[p];
-    float q2, q4;
-    slopes(Vy, Byf, p, sa, dxe, apos, q2, q4);
-    a2m = v - b * dsqinv;
-    da2m = (q2 - q4 * dsqinv) * facm;
-    a2p = v + b * dsqinv;
-    da2p = (q2 + q4 * dsqinv) * facm;
-  };
-  float a1pL, a1mL, da1pL, da1mL, a1pR, a1mR, da1pR, da1mR;
-  float a2mL, a2pL, da2mL, da2pL, a2mR, a2pR, da2mR, da2pR;
-  load1(p0 - sb, bb - 1, a1pL, a1mL, da1pL, da1mL);   // (a, b-1)
-  load1(p0, bb, a1pR, a1mR, da1pR, da1mR);            // (a, b)
-  load2(p0 - sa, aa - 1, a2mL, a2pL, da2mL, da2pL);   // (a-1, b)
-  load2(p0, aa, a2mR, a2pR, da2mR, da2pR);            // (a, b)
-
-  auto cand = [&](float a1p, float da1p, float a1m, float da1m, float a2m, float da2m, float a2p, float da2p,
-                  float dyv, float dxv, float S1, float S2, float &C1p, float &C2m, float &C1m, float &C2p) {
-    float r1 = __fdividef(1.0f, 1.0f - da1p * da2m * dt * dt);
-    float r2 = __fdividef(1.0f, 1.0f - da1m * da2p * dt * dt);
-    C1p = (a1p + da1p * dyv * S1 - da1p * (a2m + da2m * dxv * S2) * dt) * r1;
-    C2m = (a2m + da2m * dxv * S2 - da2m * (a1p + da1p * dyv * S1) * dt) * r1;
-    C1m = (a1m + da1m * dyv * S1 - da1m * (a2p + da2p * dxv * S2) * dt) * r2;
-    C2p = (a2p + da2p * dxv * S2 - da2p * (a1m + da1m * dyv * S1) * dt) * r2;
-  };
-  float C1pLL, C2mLL, C1mLL, C2pLL, C1pRL, C2mRL, C1mRL, C2pRL;
-  float C1pLR, C2mLR, C1mLR, C2pLR, C1pRR, C2mRR, C1mRR, C2pRR;
-  cand(a1pL, da1pL, a1mL, da1mL, a2mL, da2mL, a2pL, da2pL, dym, dxm, 1.0f, 1.0f, C1pLL, C2mLL, C1mLL, C2pLL);
-  cand(a1pR, da1pR, a1mR, da1mR, a2mL, da2mL, a2pL, da2pL, dy0, dxm, -1.0f, 1.0f, C1pRL, C2mRL, C1mRL, C2pRL);
-  cand(a1pL, da1pL, a1mL, da1mL, a2mR, da2mR, a2pR, da2pR, dym, dx0, 1.0f, -1.0f, C1pLR, C2mLR, C1mLR, C2pLR);
-  cand(a1pR, da1pR, a1mR, da1mR, a2mR, da2mR, a2pR, da2pR, dy0, dx0, -1.0f, -1.0f, C1pRR, C2mRR, C1mRR, C2pRR);
-
-  const bool w11 = C1pLL > 0.0f && C2mLL > 0.0f, w12 = C1mLL > 0.0f && C2pLL > 0.0f;
-  const bool w21 = C1pRL > 0.0f && C2mRL < 0.0f, w22 = C1mRL > 0.0f && C2pRL < 0.0f;
-  const bool w31 = C1pLR < 0.0f && C2mLR > 0.0f, w32 = C1mLR < 0.0f && C2pLR > 0.0f;
-  const bool w41 = C1pRR < 0.0f && C2mRR < 0.0f, w42 = C1mRR < 0.0f && C2pRR < 0.0f;
-  // weight w + (1e13-1) * int(0.51 w1 + 0.51 w2): the boost is w1 AND w2
-  const float big = 1.e13f - 1.0f;
-  auto W = [&](bool w, bool x1, bool x2) { return (w ? 1.0f : 0.0f) + ((x1 && x2) ? big : 0.0f); };
-  float W11 = W(w11, w11, w12), W12 = W(w12, w11, w12);
-  float W21 = W(w21, w21, w22), W22 = W(w22, w21, w22);
-  float W31 = W(w31, w31, w32), W32 = W(w32, w31, w32);
-  float W41 = W(w41, w41, w42), W42 = W(w42, w41, w42);
-  float C1p = 0.0f, C2m = 0.0f, C1m = 0.0f, C2p = 0.0f;
-  if (w11 || w21 || w31 || w41) {
-    C1p = __fdividef(W11 * fabsf(C2mLL) * C1pLL + W21 * fabsf(C2mRL) * C1pRL + W31 * fabsf(C2mLR) * C1pLR +
-                         W41 * fabsf(C2mRR) * C1pRR,
-                     W11 * fabsf(C2mLL) + W21 * fabsf(C2mRL) + W31 * fabsf(C2mLR) + W41 * fabsf(C2mRR));
-    C2m = __fdividef(W11 * fabsf(C1pLL) * C2mLL + W21 * fabsf(C1pRL) * C2mRL + W31 * fabsf(C1pLR) * C2mLR +
-                         W41 * fabsf(C1pRR) * C2mRR,
-                     W11 * fabsf(C1pLL) + W21 * fabsf(C1pRL) + W31 * fabsf(C1pLR) + W41 * fabsf(C1pRR));
-  }
-  if (w12 || w22 || w32 || w42) {
-    C1m = __fdividef(W12 * fabsf(C2pLL) * C1mLL + W22 * fabsf(C2pRL) * C1mRL + W32 * fabsf(C2pLR) * C1mLR +
-                         W42 * fabsf(C2pRR) * C1mRR,
-                     W12 * fabsf(C2pLL) + W22 * fabsf(C2pRL) + W32 * fabsf(C2pLR) + W42 * fabsf(C2pRR));
-    C2p = __fdividef(W12 * fabsf(C1mLL) * C2pLL + W22 * fabsf(C1mRL) * C2pRL + W32 * fabsf(C1mLR) * C2pLR +
-                         W42 * fabsf(C1mRR) * C2pRR,
-                     W12 * fabsf(C1mLL) + W22 * fabsf(C1mRL) + W32 * fabsf(C1mLR) + W42 * fabsf(C1mRR));
-  }
-  float v1a = C1p + C1m, v2a = C2p + C2m, B1a = C1p - C1m, B2a = C2p - C2m;
-  A.emf[E][p0] = 0.25f * (v1a * B2a - v2a * B1a) * (dncv * dsqinv);
-}
-
-// Packed FP32 pairs for emf32x2_kernel: Blackwell's paired FP32 add, multiply
-// and fused multiply-add (one instruction for both lanes).
+// Packed FP32 pairs: Blackwell's paired FP32 add, multiply and fused
+// multiply-add (one instruction for both lanes).
 __device__ __forceinline__ float2 p2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 psub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
@@ -219,7 +110,9 @@ __device__ __forceinline__ float2 vlim_w2(float2 qm, float2 q0, float2 qp, const
   return pmul(pmul(fl, psub(qp, qm)), p2(w.ra, w.ra));
 }
 
-// emf32_kernel with the two characteristic combinations of every candidate
+// CC(2) + CCT for the edge direction E (0: Ez on x/y, 1: Ex on y/z, 2: Ey on
+// z/x): the arithmetic of emf_kernel (:2140-2157, :2186-2445) in FP32 on
+// FP32 inputs, with the two characteristic combinations of every candidate
 // in the two lanes of packed FP32 pairs: lane x the (+, -) pair (C1p, C2m),
 // lane y the (-, +) pair (C1m, C2p), which do the same arithmetic on their
 // own inputs; the slopes of V and B along a direction share their widths

@@ -242,7 +242,11 @@ __global__ void grav_table_kernel(Grid g, double *tab, double dx, double dy, dou
 
 // One thread per mode: the face values, the forward elimination (the
 // right-hand side overwrites the line) and the back substitution; the
-// mode's value at x cell i is S[i nmh + mode].
+// mode's value at x cell i is S[i nmh + mode].  There are only ny/2+1 times
+// nz modes (about seven warps per SM at 256^3), so each pass loads a batch
+// of kGB x cells before it uses any: one memory wait per batch instead of
+// one per cell.
+constexpr int kGB = 8;
 __global__ void grav_modes_kernel(Grid g, double2 *S, const double *tab, double dx) {
   const int nx = g.n[0], nyh = g.n[1] / 2 + 1;
   const long long nmh = (long long)nyh * g.n[2];
@@ -250,32 +254,71 @@ __global__ void grav_modes_kernel(Grid g, double2 *S, const double *tab, double 
   if (t >= nmh) return;
   const size_t N = (size_t)nx * nmh;
   const double *f1 = tab, *f2 = tab + N, *cc = tab + 2 * N, *iv = tab + 3 * N;
+  double2 *Sm = S + t;   // Sm[i nmh]: the mode at x cell i
   double2 bl = make_double2(0.0, 0.0), br = make_double2(0.0, 0.0);
-  for (int i = 0; i < nx; i++) {
-    const size_t o = (size_t)i * nmh + t;
-    const double2 r = S[o];
-    const double w1 = f1[o], w2 = f2[o];
-    bl = make_double2(bl.x + r.x * w1, bl.y + r.y * w1);
-    br = make_double2(br.x + r.x * w2, br.y + r.y * w2);
+  for (int i0 = 0; i0 < nx; i0 += kGB) {
+    double2 r[kGB];
+    double w1[kGB], w2[kGB];
+#pragma unroll
+    for (int u = 0; u < kGB; u++) {
+      if (i0 + u < nx) {
+        const size_t o = (size_t)(i0 + u) * nmh + t;
+        r[u] = Sm[(size_t)(i0 + u) * nmh];
+        w1[u] = f1[o];
+        w2[u] = f2[o];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kGB; u++) {
+      if (i0 + u < nx) {
+        bl = make_double2(bl.x + r[u].x * w1[u], bl.y + r[u].y * w1[u]);
+        br = make_double2(br.x + r[u].x * w2[u], br.y + r[u].y * w2[u]);
+      }
+    }
   }
   const double a = 1.0 / (dx * dx);
   double2 d = make_double2(0.0, 0.0);
-  for (int i = 0; i < nx; i++) {
-    const size_t o = (size_t)i * nmh + t;
-    const double2 r = S[o];
-    double2 ri = make_double2(r.x * kG4pi, r.y * kG4pi);
-    if (i == 0) ri = make_double2(ri.x - 2.0 * a * bl.x, ri.y - 2.0 * a * bl.y);
-    if (i == nx - 1) ri = make_double2(ri.x - 2.0 * a * br.x, ri.y - 2.0 * a * br.y);
-    const double inv = iv[o];
-    d = make_double2((ri.x - a * d.x) * inv, (ri.y - a * d.y) * inv);
-    S[o] = d;
+  for (int i0 = 0; i0 < nx; i0 += kGB) {
+    double2 r[kGB];
+    double inv[kGB];
+#pragma unroll
+    for (int u = 0; u < kGB; u++) {
+      if (i0 + u < nx) {
+        r[u] = Sm[(size_t)(i0 + u) * nmh];
+        inv[u] = iv[(size_t)(i0 + u) * nmh + t];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kGB; u++) {
+      const int i = i0 + u;
+      if (i < nx) {
+        double2 ri = make_double2(r[u].x * kG4pi, r[u].y * kG4pi);
+        if (i == 0) ri = make_double2(ri.x - 2.0 * a * bl.x, ri.y - 2.0 * a * bl.y);
+        if (i == nx - 1) ri = make_double2(ri.x - 2.0 * a * br.x, ri.y - 2.0 * a * br.y);
+        d = make_double2((ri.x - a * d.x) * inv[u], (ri.y - a * d.y) * inv[u]);
+        Sm[(size_t)i * nmh] = d;
+      }
+    }
   }
-  for (int i = nx - 2; i >= 0; i--) {
-    const size_t o = (size_t)i * nmh + t;
-    const double2 cur = S[o];
-    const double c = cc[o];
-    d = make_double2(cur.x - c * d.x, cur.y - c * d.y);
-    S[o] = d;
+  // back substitution, x cells nx-2 down to 0, in batches from the top
+  for (int i1 = nx - 2; i1 >= 0; i1 -= kGB) {
+    double2 r[kGB];
+    double c[kGB];
+#pragma unroll
+    for (int u = 0; u < kGB; u++) {
+      if (i1 - u >= 0) {
+        r[u] = Sm[(size_t)(i1 - u) * nmh];
+        c[u] = cc[(size_t)(i1 - u) * nmh + t];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kGB; u++) {
+      const int i = i1 - u;
+      if (i >= 0) {
+        d = make_double2(r[u].x - c[u] * d.x, r[u].y - c[u] * d.y);
+        Sm[(size_t)i * nmh] = d;
+      }
+    }
   }
 }
 
