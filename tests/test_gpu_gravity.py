@@ -53,6 +53,23 @@ def test_potential_matches_the_oracle(shape):
     assert np.abs(pg[full] - po[full]).max() <= 1e-12 * np.abs(po).max()
 
 
+def test_potential_after_a_new_upload_with_other_coordinates():
+    """The Green's weights and elimination coefficients are tabulated from
+    the grid: a second upload with another box size must rebuild them."""
+    st1 = blob_state(16, 16, 16, seed=2)
+    g = native.Mhd3D(st1.params)
+    g.upload(st1)
+    g.potential()
+    st2, _, _, _ = state(16, 16, 16, 37.0, lambda x, y, z: 1.0 + 0.5 * np.cos(2 * np.pi * y / 37.0) * np.exp(-((x - 12.0) / 5.0) ** 2) + 0 * z)
+    st2.U[4][...] = 51.8 * st2.U[0] / 1.27
+    st2.species[0][...] = st2.U[0] / 1.27
+    g.upload(st2)
+    o = Oracle3D(st2.params)
+    o.upload(st2)
+    pg, po = g.potential(), o.potential()
+    assert np.abs(pg - po).max() <= 1e-12 * np.abs(po).max()
+
+
 def test_uniform_slab_on_the_gpu():
     rho0, H, xc = 2.0 / G4PI / 90.0, 10.0, 50.0
     st, cx, _, _ = state(80, 4, 4, 100.0, lambda x, y, z: np.where(np.abs(x - xc) <= H, rho0, 0.0) + 0 * y * z)
