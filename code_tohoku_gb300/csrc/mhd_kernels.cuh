@@ -1040,6 +1040,16 @@ __global__ void face_b_kernel(Grid g, Fields f, const double *Ez, const double *
 }
 
 // CC(4): cell-centred B (:2171-2177)
+// 0.5 x, bit for bit the FP64 product: for a normal x whose half is normal
+// the exponent field drops by one (an integer subtraction, off GB300's
+// narrow FP64 pipe); zeros, subnormals, Inf and NaN take the multiply.
+__device__ __forceinline__ double half_exact(double x) {
+  const int hi = __double2hiint(x);
+  const int e = (hi >> 20) & 0x7ff;
+  if (e > 1 && e < 0x7ff) return __hiloint2double(hi - 0x00100000, __double2loint(x));
+  return 0.5 * x;
+}
+
 __global__ void cell_b_kernel(Grid g, Fields f) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int nx = g.n[0], ny = g.n[1], nz = g.n[2];
@@ -1048,9 +1058,9 @@ __global__ void cell_b_kernel(Grid g, Fields f) {
   split3(t, nx, ny, i, j, k);
   i += 1; j += 1; k += 1;
   long long a = gidx(g, i, j, k);
-  f.bcc[0][a] = 0.5 * (f.U[5][a] + f.U[5][a + 1]);
-  f.bcc[1][a] = 0.5 * (f.U[6][a] + f.U[6][a + g.st[1]]);
-  f.bcc[2][a] = 0.5 * (f.U[7][a] + f.U[7][a + g.st[2]]);
+  f.bcc[0][a] = half_exact(f.U[5][a] + f.U[5][a + 1]);
+  f.bcc[1][a] = half_exact(f.U[6][a] + f.U[6][a + g.st[1]]);
+  f.bcc[2][a] = half_exact(f.U[7][a] + f.U[7][a + g.st[2]]);
 }
 
 #endif  // MHD_COMMON_KERNELS
