@@ -671,6 +671,15 @@ def main():
             "traffic": tr * n3 if tr else None, "kernel": "sweep32_kernel (fused RHS+MOC+REMAP, FP32 recon/flux + FP64 accumulation)",
             "peak_source": f"{which} (MEASURED_PEAKS.json hbm_gbs)" if which == "measured" else which,
             "algorithmic_bytes_per_zone": B_ALG_SWEEP}
+    if tr:
+        # the bytes the kernel really moves (the species too), over the same time
+        roof["traffic_gbs"] = tr * n3 / (sweep_ms * 1e-3) / 1e9
+        roof["traffic_frac"] = roof["traffic_gbs"] / hbm
+    issue = profile_value("sweep_fp32_traffic.txt", "sweep_fp32_issue_active_pct")
+    if issue:
+        roof["limiter"] = {"issue_active_pct": issue,
+                           "fp64_pipe_pct": profile_value("sweep_fp32_traffic.txt", "sweep_fp32_fp64_pipe_pct"),
+                           "source": "ncu --set full of the three sweep launches at 128^3 (profiles/)"}
     line = {"metric": "zone-updates/s, 256^3 MHD+KI cool: FP32+surrogate vs plain FP64 at stated L1 err",
             "value": value, "unit": "zone-updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True,
