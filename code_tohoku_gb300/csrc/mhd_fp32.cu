@@ -133,10 +133,12 @@ int dt_screen_warps(const Grid &g) {
 cudaError_t dt_screen_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, float *lo,
                            unsigned *words, int *err, cudaStream_t s) {
   long long n = (long long)g.n[0] * g.n[1] * g.n[2];
-  // a thread per cell: with a capped grid of 4864 blocks (~13 cells per
-  // thread, 50x fewer atomics) the 256^3 kernel took 385 us against 333-358
+  // two cells per thread (a capped grid of 4864 blocks, ~13 cells per
+  // thread and 50x fewer atomics, took 385 us at 256^3 against 333-358 for
+  // one cell per thread)
   DtScreen sc{lo, words, dt_screen_warps(g)};
-  dt32_screen_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g, ph, f, sh2, sc, err);
+  dt32_screen_kernel<<<(unsigned)((n + kDtScreenCells - 1) / kDtScreenCells), kDtScreenThreads, 0, s>>>(g, ph, f,
+                                                                                                      sh2, sc, err);
   return cudaGetLastError();
 }
 

@@ -378,39 +378,69 @@ constexpr float kDtEta = 1.0f / 16384.0f;
 constexpr float kDtEtaCoolKI = 1.0f / 4096.0f;
 constexpr float kDtEtaCoolSpecies = 1.0f / 256.0f;
 
-__global__ void __launch_bounds__(256) dt32_screen_kernel(Grid g, Phys ph, Fields f, const float *sh2, DtScreen sc,
-                                                          int *err) {
+// Two cells per thread, 256 apart (block-strided, so every warp access
+// stays coalesced), the loads of both issued before either is used: the
+// screen moves ~72 bytes a cell and one cell per thread left it waiting on
+// memory.  The per-warp lower ends stay per 32 consecutive cells (the unit
+// the refine kernel walks).
+constexpr int kDtScreenThreads = 256, kDtScreenCells = 2 * kDtScreenThreads;
+__global__ void __launch_bounds__(kDtScreenThreads) dt32_screen_kernel(Grid g, Phys ph, Fields f, const float *sh2,
+                                                                       DtScreen sc, int *err) {
   const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   const long long ncells = (long long)nx * ny * nz;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long base = (long long)blockIdx.x * kDtScreenCells + threadIdx.x;
   const float INF = __int_as_float(0x7f800000);
   const float dn = 1.0f - kDtEta, up = 1.0f + kDtEta;
-  float lo[3] = {INF, INF, INF}, hi[3] = {INF, INF, INF};   // c, tau, alpha
+  // the inputs of both cells first: rho, v1..v3, p, Bcc1..3 (and S, H2)
+  double raw[2][8];
+  float sr[2][2];
+  int ijk[2][3];
+  long long aa[2];
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const long long t = base + u * kDtScreenThreads;
+    aa[u] = -1;
+    if (t < ncells) {
+      split3(t, nx, ny, ijk[u][0], ijk[u][1], ijk[u][2]);
+      ijk[u][0] += 1; ijk[u][1] += 1; ijk[u][2] += 1;
+      const long long a = gidx(g, ijk[u][0], ijk[u][1], ijk[u][2]);
+      aa[u] = a;
+      raw[u][0] = __ldg(f.U[0] + a); raw[u][1] = __ldg(f.U[1] + a); raw[u][2] = __ldg(f.U[2] + a);
+      raw[u][3] = __ldg(f.U[3] + a); raw[u][4] = __ldg(f.U[4] + a);
+      raw[u][5] = __ldg(f.bcc[0] + a); raw[u][6] = __ldg(f.bcc[1] + a); raw[u][7] = __ldg(f.bcc[2] + a);
+      if (sh2) {
+        sr[u][0] = __ldg(sh2 + a);
+        sr[u][1] = __ldg(sh2 + g.ncell + a);
+      }
+    }
+  }
+  float lo[2][3], hi[3] = {INF, INF, INF};   // c, tau, alpha
   bool floored = false;
-  if (t < ncells) {
-    int i, j, k;
-    split3(t, nx, ny, i, j, k);
-    i += 1; j += 1; k += 1;
-    long long a = gidx(g, i, j, k);
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    lo[u][0] = lo[u][1] = lo[u][2] = INF;
+    if (aa[u] < 0) continue;
+    const long long a = aa[u];
+    const int i = ijk[u][0], j = ijk[u][1], k = ijk[u][2];
     // S = H+p+He+He+ and H2: SOURCE's floats when current (the same sums)
     float S, H2;
     if (sh2) {
-      S = sh2[a];
-      H2 = sh2[g.ncell + a];
+      S = sr[u][0];
+      H2 = sr[u][1];
     } else {
       S = d2f(f.sp[0][a]) + d2f(f.sp[1][a]) + d2f(f.sp[3][a]) + d2f(f.sp[4][a]);
       H2 = d2f(f.sp[2][a]);
     }
     float rg = __fdiv_rn(1.0f, 3.0f * S + 5.0f * H2);
     float gam = (5.0f * S + 7.0f * H2) * rg;
-    float bx = d2f(f.bcc[0][a]), by = d2f(f.bcc[1][a]), bz = d2f(f.bcc[2][a]);
-    float rho = d2f(f.U[0][a]), p5 = d2f(f.U[4][a]);
+    float bx = d2f(raw[u][5]), by = d2f(raw[u][6]), bz = d2f(raw[u][7]);
+    float rho = d2f(raw[u][0]), p5 = d2f(raw[u][4]);
     float cs = sqrtf(__fdiv_rn(gam * p5 + bx * bx + by * by + bz * bz, rho));
     float dxi = g.dxf[0][i + 1], dyj = g.dxf[1][j + 1], dzk = g.dxf[2][k + 1];
-    float c = fminf(fminf(__fdiv_rn(dxi, cs + fabsf(d2f(f.U[1][a]))), __fdiv_rn(dyj, cs + fabsf(d2f(f.U[2][a])))),
-                    __fdiv_rn(dzk, cs + fabsf(d2f(f.U[3][a]))));
-    lo[0] = c * dn;
-    hi[0] = c * up;
+    float c = fminf(fminf(__fdiv_rn(dxi, cs + fabsf(d2f(raw[u][1]))), __fdiv_rn(dyj, cs + fabsf(d2f(raw[u][2])))),
+                    __fdiv_rn(dzk, cs + fabsf(d2f(raw[u][3]))));
+    lo[u][0] = c * dn;
+    hi[0] = fminf(hi[0], c * up);
     bool bad = !(c > 0.0f);
     if (ph.ifthrm == 2) {
       float Nn = S + H2;
@@ -419,8 +449,8 @@ __global__ void __launch_bounds__(256) dt32_screen_kernel(Grid g, Phys ph, Field
       float dl = fminf(fminf(dxi, dyj), dzk);
       float g1c = (2.0f * S + 2.0f * H2) * rg;
       float alpha = __fdiv_rn(0.4f * Nn * kb, g1c * d2f(ph.kcond) * sqrtf(fminf(Tn, 15.0f))) * (dl * dl);
-      lo[2] = alpha * dn;
-      hi[2] = alpha * up;
+      lo[u][2] = alpha * dn;
+      hi[2] = fminf(hi[2], alpha * up);
       float mag;
       float CooL = (ph.ifchem == 2)
                        ? fcool_species<float>(Tn, cell_species<float>(f, a, [](double v) { return d2f(v); }), &mag)
@@ -431,10 +461,10 @@ __global__ void __launch_bounds__(256) dt32_screen_kernel(Grid g, Phys ph, Field
       const float thi = ac > e ? __fdiv_rn(num, g1c * (ac - e)) * up : INF;
       // the floor of the cooling time, bracketed in FP32
       const float flo = 2.5e-4f * (1.0f - 1e-6f), fhi = 2.5e-4f * (1.0f + 1e-6f);
-      floored = thi <= flo;
-      lo[1] = fmaxf(tlo, flo);
-      hi[1] = fmaxf(thi, fhi);
-      bad = bad || !(alpha > 0.0f) || !(lo[1] > 0.0f);
+      floored = floored || thi <= flo;
+      lo[u][1] = fmaxf(tlo, flo);
+      hi[1] = fminf(hi[1], fmaxf(thi, fhi));
+      bad = bad || !(alpha > 0.0f) || !(lo[u][1] > 0.0f);
     }
     if (bad) flag(err, ERRB_DT);
   }
@@ -442,18 +472,24 @@ __global__ void __launch_bounds__(256) dt32_screen_kernel(Grid g, Phys ph, Field
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-      lo[q] = fminf(lo[q], __shfl_xor_sync(0xffffffffu, lo[q], o));
+      lo[0][q] = fminf(lo[0][q], __shfl_xor_sync(0xffffffffu, lo[0][q], o));
+      lo[1][q] = fminf(lo[1][q], __shfl_xor_sync(0xffffffffu, lo[1][q], o));
       hi[q] = fminf(hi[q], __shfl_xor_sync(0xffffffffu, hi[q], o));
     }
   floored = __any_sync(0xffffffffu, floored);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const long long gw = t >> 5;
-  if (lane == 0 && gw < sc.nwarps) {
-    sc.lo[gw] = lo[0];
-    sc.lo[sc.nwarps + gw] = lo[1];
-    sc.lo[2 * sc.nwarps + gw] = lo[2];
+  if (lane == 0) {
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      const long long gw = (base + u * kDtScreenThreads) >> 5;   // the 32 consecutive cells of this warp's half
+      if (gw < sc.nwarps) {
+        sc.lo[gw] = lo[u][0];
+        sc.lo[sc.nwarps + gw] = lo[u][1];
+        sc.lo[2 * sc.nwarps + gw] = lo[u][2];
+      }
+    }
   }
-  __shared__ float wh[3][8];
+  __shared__ float wh[3][kDtScreenThreads / 32];
   if (lane == 0)
     for (int q = 0; q < 3; q++) wh[q][w] = hi[q];
   if (lane == 0 && floored) atomicOr(&sc.words[3], 1u);
