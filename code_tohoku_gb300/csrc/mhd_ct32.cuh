@@ -35,22 +35,45 @@ struct CT32Args {
 };
 
 #ifdef MHD_FP32_KERNELS
+// Two faces per thread, blockDim apart (coalesced), the six loads of both
+// issued before either is used.
 __global__ void __launch_bounds__(256) face_velocity32_kernel(Grid g, Fields f, double *vf0, double *vf1,
                                                               double *vf2) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
-  if (t >= (long long)nx1 * ny1 * nz1) return;
-  int i, j, k;
-  split3(t, nx1, ny1, i, j, k);
-  i += 1; j += 1; k += 1;
-  long long a = gidx(g, i, j, k);
+  const int nx1 = g.n[0] + 1, ny1 = g.n[1] + 1, nz1 = g.n[2] + 1;
+  const long long n = (long long)nx1 * ny1 * nz1;
+  const long long t0 = (long long)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+  const int sy = (int)g.st[1], sz = (int)g.st[2];
+  double v[2][6];
+  int aa[2], ijk[2][3];
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const long long t = t0 + u * blockDim.x;
+    aa[u] = -1;
+    if (t < n) {
+      int i, j, k;
+      split3(t, nx1, ny1, i, j, k);
+      i += 1; j += 1; k += 1;
+      const int a = (int)gidx(g, i, j, k);
+      aa[u] = a;
+      ijk[u][0] = i; ijk[u][1] = j; ijk[u][2] = k;
+      v[u][0] = f.U[1][a]; v[u][1] = f.U[1][a - 1];
+      v[u][2] = f.U[2][a]; v[u][3] = f.U[2][a - sy];
+      v[u][4] = f.U[3][a]; v[u][5] = f.U[3][a - sz];
+    }
+  }
   const float *dx = g.dxf[0], *dy = g.dxf[1], *dz = g.dxf[2];
-  if (j <= g.n[1] && k <= g.n[2])
-    vf0[a] = f2d(__fdividef(dx[i] * d2f(f.U[1][a]) + dx[i + 1] * d2f(f.U[1][a - 1]), dx[i] + dx[i + 1]));
-  if (i <= g.n[0] && k <= g.n[2])
-    vf1[a] = f2d(__fdividef(dy[j] * d2f(f.U[2][a]) + dy[j + 1] * d2f(f.U[2][a - g.st[1]]), dy[j] + dy[j + 1]));
-  if (i <= g.n[0] && j <= g.n[1])
-    vf2[a] = f2d(__fdividef(dz[k] * d2f(f.U[3][a]) + dz[k + 1] * d2f(f.U[3][a - g.st[2]]), dz[k] + dz[k + 1]));
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const int a = aa[u];
+    if (a < 0) continue;
+    const int i = ijk[u][0], j = ijk[u][1], k = ijk[u][2];
+    if (j <= g.n[1] && k <= g.n[2])
+      vf0[a] = f2d(__fdividef(dx[i] * d2f(v[u][0]) + dx[i + 1] * d2f(v[u][1]), dx[i] + dx[i + 1]));
+    if (i <= g.n[0] && k <= g.n[2])
+      vf1[a] = f2d(__fdividef(dy[j] * d2f(v[u][2]) + dy[j + 1] * d2f(v[u][3]), dy[j] + dy[j + 1]));
+    if (i <= g.n[0] && j <= g.n[1])
+      vf2[a] = f2d(__fdividef(dz[k] * d2f(v[u][4]) + dz[k + 1] * d2f(v[u][5]), dz[k] + dz[k + 1]));
+  }
 }
 
 // Two cells per thread (block-strided, so every warp access stays

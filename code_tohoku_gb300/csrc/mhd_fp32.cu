@@ -153,7 +153,7 @@ cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double 
 
 cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s) {
   long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
-  face_velocity32_kernel<<<blocks_for(n, 256), 256, 0, s>>>(g, f, v0, v1, v2);
+  face_velocity32_kernel<<<blocks_for(n, 512), 256, 0, s>>>(g, f, v0, v1, v2);
   return cudaGetLastError();
 }
 

@@ -59,7 +59,7 @@ cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const doubl
 
 cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s) {
   long long n = (long long)g.n[0] * g.n[1] * g.n[2];
-  cell_b_kernel<<<nblk(n, 256), 256, 0, s>>>(g, f);
+  cell_b_kernel<<<nblk(n, 512), 256, 0, s>>>(g, f);
   return cudaGetLastError();
 }
 

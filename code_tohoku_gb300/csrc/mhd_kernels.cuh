@@ -1050,17 +1050,33 @@ __device__ __forceinline__ double half_exact(double x) {
   return 0.5 * x;
 }
 
-__global__ void cell_b_kernel(Grid g, Fields f) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  if (t >= (long long)nx * ny * nz) return;
-  int i, j, k;
-  split3(t, nx, ny, i, j, k);
-  i += 1; j += 1; k += 1;
-  long long a = gidx(g, i, j, k);
-  f.bcc[0][a] = half_exact(f.U[5][a] + f.U[5][a + 1]);
-  f.bcc[1][a] = half_exact(f.U[6][a] + f.U[6][a + g.st[1]]);
-  f.bcc[2][a] = half_exact(f.U[7][a] + f.U[7][a + g.st[2]]);
+// two cells per thread, blockDim apart (every warp access stays coalesced),
+// the six loads of both issued before either is used
+__global__ void __launch_bounds__(256) cell_b_kernel(Grid g, Fields f) {
+  const long long n = (long long)g.n[0] * g.n[1] * g.n[2];
+  const long long t0 = (long long)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+  double v[2][6];
+  long long aa[2];
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const long long t = t0 + u * blockDim.x;
+    aa[u] = -1;
+    if (t < n) {
+      const long long a = gidx_lin(g, t, g.n[0], g.n[1]);
+      aa[u] = a;
+      v[u][0] = f.U[5][a]; v[u][1] = f.U[5][a + 1];
+      v[u][2] = f.U[6][a]; v[u][3] = f.U[6][a + g.st[1]];
+      v[u][4] = f.U[7][a]; v[u][5] = f.U[7][a + g.st[2]];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    const long long a = aa[u];
+    if (a < 0) continue;
+    f.bcc[0][a] = half_exact(v[u][0] + v[u][1]);
+    f.bcc[1][a] = half_exact(v[u][2] + v[u][3]);
+    f.bcc[2][a] = half_exact(v[u][4] + v[u][5]);
+  }
 }
 
 #endif  // MHD_COMMON_KERNELS
