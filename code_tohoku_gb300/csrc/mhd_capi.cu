@@ -18,6 +18,10 @@
 #include "mhd_conv.cuh"
 #include "mhd_launch.h"
 
+// full-grid FP64 arrays of a handle, one allocation: 8 U + 8 species + 3 Bcc
+// + 3 face velocities + 3 EMF + pnew + the chemistry's nde and ndtot
+static constexpr int kStateArrays = 8 + 8 + 3 + 3 + 3 + 1 + 2;
+
 using namespace mhd;
 
 struct mhd_handle {
@@ -156,6 +160,7 @@ int check_err(mhd_handle *h) {
   if (e & ERRB_NONFINITE) return fail(h, MHD_ERR_NONFINITE, "non-finite value in the state (time %.17g)", h->time);
   if (e & ERRB_DT) return fail(h, MHD_ERR_DT, "non-positive time-step limit (err at Couran/Stblty)");
   if (e & ERRB_TC) return fail(h, MHD_ERR_CUDA, "tensor-core completion wait timed out in SOURCE");
+  if (e & ERRB_TMA) return fail(h, MHD_ERR_CUDA, "a sweep's wait for its staged inputs timed out");
   return MHD_OK;
 }
 
@@ -250,10 +255,8 @@ int mhd_create(const mhd_params *p, mhd_handle **out) {
   ph.in.on[0] = p->bc[0] == 4;
   ph.in.on[1] = p->bc[1] == 4;
 
-  // full-grid arrays: 8 U + 8 species + 3 Bcc + 3 face velocities + 3 EMF +
-  // pnew + the chemistry's nde and ndtot
-  const int narr = 8 + 8 + 3 + 3 + 3 + 1 + 2;
-  size_t bytes = (size_t)narr * (size_t)g.ncell * sizeof(double);
+  // the full-grid arrays (kStateArrays), one allocation
+  size_t bytes = (size_t)kStateArrays * (size_t)g.ncell * sizeof(double);
   if (cudaMalloc(&h->block, bytes) != cudaSuccess) {
     cudaGetLastError();
     delete h;
@@ -655,7 +658,7 @@ int mhd_sweep(mhd_handle *h, int dir, double dt) {
   h->sh2_valid = false;   // the sweeps move the species
   SweepArgs a{};
   a.g = h->g; a.ph = h->ph; a.f = h->f; a.dt = dt; a.err = h->err;
-  if (h->p.precision == MHD_PREC_FP32) CK(sweep_fp32(dir, a, h->stream));
+  if (h->p.precision == MHD_PREC_FP32) CK(sweep_fp32(dir, a, h->block, kStateArrays, h->stream));
   else CK(sweep_fp64(dir, a, h->stream));
   return MHD_OK;
 }

@@ -1,6 +1,8 @@
 // mhd_fp32.cu — chosen form: reconstruction, Riemann solver, characteristic
 // and EMF arithmetic in FP32; accumulation into the FP64 state.  Built with
 // the default contraction (FMA) enabled.
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #define MHD_FP32_KERNELS
 #include "mhd_sweep32.cuh"
@@ -67,12 +69,74 @@ constexpr int kSweepZThreads = MHD_SWEEP_Z_THREADS;
 #define MHD_SWEEP_Z_PENCILS 8
 #endif
 constexpr int kSweepZPencils = MHD_SWEEP_Z_PENCILS;
+#ifndef MHD_SWEEP_Z_MINB
+#define MHD_SWEEP_Z_MINB 1
+#endif
 
-template <int DIR, int P, int LS, int NT, int MINB>
-static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
+// Bit d of MHD_SWEEP_TMA set: the direction-d sweep (y or z) stages its
+// FP64 inputs with TMA box loads (see SweepTma) when the grid allows it:
+// pencils of up to 2 kStageRows - 4 cells, an even padded row (row strides a
+// multiple of 16 bytes) and every input array inside the state allocation.
+// Measured at 256^3 (ms, per-thread loads -> TMA): y 2.07 -> 1.99 with two
+// CTAs per SM, whose load and compute phases overlap; z 2.26 -> 2.36 with
+// its one CTA per SM, where the three staging rounds are exposed.  So the y
+// sweep only, by default.
+#ifndef MHD_SWEEP_TMA
+#define MHD_SWEEP_TMA 2
+#endif
+constexpr int kSweepTmaStride = 2 * kStageRows;
+
+// the driver's tensor-map encoder, resolved once (null when unavailable)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// the tensor map and array indices of the direction-DIR sweep's staged
+// inputs, pencil groups of P columns; false when the grid or the arrays do
+// not meet the TMA rules
+template <int DIR, int P>
+static bool sweep_tma_map(const SweepArgs &a, const double *block, int narr, SweepTma &T) {
+  const Grid &g = a.g;
+  const int L = g.n[DIR] + 4;
+  if (!block || g.s[0] % 2 != 0 || L > kSweepTmaStride || (P * 8) % 16 != 0) return false;
+  T = SweepTma{};
+  T.nbox = (L + kStageRows - 1) / kStageRows;
+  constexpr int C1 = (DIR + 1) % 3, C2 = (DIR + 2) % 3;
+  const Fields &f = a.f;
+  const double *in[SF_COUNT] = {f.bcc[C1], f.bcc[C2], f.U[0], f.U[1 + DIR], f.U[1 + C1], f.U[1 + C2], f.U[4],
+                                f.sp[0],   f.sp[1],   f.sp[2], f.sp[3],     f.sp[4],     f.U[5 + DIR], f.bcc[DIR]};
+  const long long nc = g.ncell;
+  for (int q = 0; q < SF_COUNT; q++) {
+    const long long d = (long long)(in[q] - block);
+    if (d < 0 || d % nc != 0 || d / nc >= narr) return false;
+    T.fld[q] = (int)(d / nc);
+  }
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)g.s[0], (cuuint64_t)g.s[1], (cuuint64_t)g.s[2], (cuuint64_t)narr};
+  const cuuint64_t strides[3] = {(cuuint64_t)g.s[0] * 8, (cuuint64_t)g.s[0] * g.s[1] * 8, (cuuint64_t)nc * 8};
+  const cuuint32_t box[4] = {(cuuint32_t)P, DIR == 1 ? (cuuint32_t)kStageRows : 1u,
+                             DIR == 2 ? (cuuint32_t)kStageRows : 1u, 1u};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(&T.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<double *>(block), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int DIR, int P, int LS, int NT, int MINB, bool TM = false>
+static cudaError_t launch32(const SweepArgs &a, cudaStream_t s, const SweepTma &T = SweepTma{}) {
   const Grid &g = a.g;
   size_t smem = sweep32_smem_bytes(g.n[DIR], P, LS);
-  auto k = sweep32_kernel<DIR, P, NT, MINB, LS>;
+  auto k = sweep32_kernel<DIR, P, NT, MINB, LS, TM>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   // x sweep: P adjacent y rows per CTA; y and z sweeps: P adjacent x columns
@@ -82,12 +146,12 @@ static cudaError_t launch32(const SweepArgs &a, cudaStream_t s) {
   if (DIR == 0) grid = dim3(g.n[1] / P, g.n[2]);
   else if (DIR == 1) grid = dim3(xgroups, g.n[2]);
   else grid = dim3(xgroups, g.n[1]);
-  k<<<grid, NT, smem, s>>>(a);
+  k<<<grid, NT, smem, s>>>(a, T);
   return cudaGetLastError();
 }
 
 template <int DIR>
-static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
+static cudaError_t launch32_d(const SweepArgs &a, const double *block, int narr, cudaStream_t s) {
   constexpr int NT = sweep_threads<DIR>(), MB = kSweepMinBlocks;
   // the x sweep needs P to divide ny; the y and z sweeps pad their groups
   const int nb = (DIR == 0) ? a.g.n[1] : 4;
@@ -99,8 +163,22 @@ static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
   // within a page or two, is faster with four: 2.41 against 2.52, and the x
   // sweep with four rows and two CTAs: 2.16 against 2.58)
   if constexpr (DIR == 2) {
+    if (((MHD_SWEEP_TMA >> 2) & 1) && L <= kSweepTmaStride &&
+        sweep32_smem_bytes(a.g.n[DIR], kSweepZPencils, kSweepTmaStride) <=
+            (MHD_SWEEP_Z_MINB > 1 ? kSweepSmemPerCta : 226 * 1024)) {
+      SweepTma T;
+      if (sweep_tma_map<DIR, kSweepZPencils>(a, block, narr, T))
+        return launch32<DIR, kSweepZPencils, kSweepTmaStride, kSweepZThreads, MHD_SWEEP_Z_MINB, true>(a, s, T);
+    }
     if (L <= kSweepFixedStride && sweep32_smem_bytes(a.g.n[DIR], kSweepZPencils, kSweepFixedStride) <= 226 * 1024)
       return launch32<DIR, kSweepZPencils, kSweepFixedStride, kSweepZThreads, 1>(a, s);
+  }
+  if constexpr (DIR == 1) {
+    if (((MHD_SWEEP_TMA >> 1) & 1) && L <= kSweepTmaStride &&
+        sweep32_smem_bytes(a.g.n[DIR], 4, kSweepTmaStride) <= kSweepSmemPerCta) {
+      SweepTma T;
+      if (sweep_tma_map<DIR, 4>(a, block, narr, T)) return launch32<DIR, 4, kSweepTmaStride, NT, MB, true>(a, s, T);
+    }
   }
   if (MHD_SWEEP_MAX_PENCILS >= 4 && nb % 4 == 0 && L <= kSweepFixedStride &&
       sweep32_smem_bytes(a.g.n[DIR], 4, kSweepFixedStride) <= kSweepSmemPerCta)
@@ -121,10 +199,10 @@ static cudaError_t launch32_d(const SweepArgs &a, cudaStream_t s) {
   return launch32<DIR, 1, 0, NT, MB>(a, s);
 }
 
-cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s) {
-  if (dir == 0) return launch32_d<0>(a, s);
-  if (dir == 1) return launch32_d<1>(a, s);
-  return launch32_d<2>(a, s);
+cudaError_t sweep_fp32(int dir, const SweepArgs &a, const double *block, int narr, cudaStream_t s) {
+  if (dir == 0) return launch32_d<0>(a, block, narr, s);
+  if (dir == 1) return launch32_d<1>(a, block, narr, s);
+  return launch32_d<2>(a, block, narr, s);
 }
 int dt_screen_warps(const Grid &g) {
   const long long n = (long long)g.n[0] * g.n[1] * g.n[2];

@@ -27,6 +27,7 @@ enum : int {
   ERRB_DT = 2,
   ERRB_IMC = 4,
   ERRB_TC = 8,            // a tensor-core completion wait timed out (the network was switched off)
+  ERRB_TMA = 16,          // a sweep's wait for its TMA-staged inputs timed out
 };
 
 struct Grid {

@@ -20,7 +20,9 @@ size_t sweep_smem_bytes(const Grid &g, int dir, int P);
 cudaError_t sweep_fp64(int dir, const SweepArgs &a, cudaStream_t s);
 cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s);
 // chosen form (FP32 reconstruction / Riemann / characteristics / EMF)
-cudaError_t sweep_fp32(int dir, const SweepArgs &a, cudaStream_t s);
+// block / narr: the allocation of narr equal-sized FP64 arrays that holds
+// the state (the y and z sweeps stage their inputs from it with TMA)
+cudaError_t sweep_fp32(int dir, const SweepArgs &a, const double *block, int narr, cudaStream_t s);
 // stiff_mode 0: the bisection for stiff cells; STIFF_NETWORK / STIFF_NEWTON:
 // the guess-and-polish path of source32_fused_kernel
 cudaError_t source_fp32(const Source32Args &a, int stiff_mode, cudaStream_t s);

@@ -1,5 +1,7 @@
 // mhd_tc.cuh — Blackwell tensor-core primitives (tcgen05, TMEM, mbarrier)
-// in inline PTX, for the surrogate network's 128-row tiles.
+// in inline PTX, for the surrogate network's 128-row tiles, and the tensor
+// memory-access (TMA) box load the chosen-form sweeps stage their inputs
+// with.
 //
 // One CTA of 128 threads owns one tile: thread r holds row r (one cell).
 // Operands are BF16 in shared memory in the no-swizzle K-major layout of
@@ -76,6 +78,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     if (ok) return true;
   }
   return false;
+}
+
+// the mbarrier's initialisation visible to the asynchronous proxy (TMA)
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// one arrival that also expects tx bytes of asynchronous copies
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// TMA: one box of a 4-D tiled tensor map into shared memory at dst (128-byte
+// aligned), completing tx bytes on the mbarrier; coordinates in elements,
+// innermost first (the innermost times the element size a multiple of 16)
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const void *tmap, int c0, int c1, int c2, int c3,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread

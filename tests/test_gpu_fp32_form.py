@@ -46,8 +46,12 @@ def test_fp32_mass_conserved_and_divb():
 
 
 # (260, 8, 8) and (8, 8, 300): pencils longer than 256 cells take the sweep
-# kernel with the run-time buffer stride, as the 512^3 grid does
-@pytest.mark.parametrize("shape", [(12, 10, 8), (9, 7, 11), (18, 13, 6), (20, 12, 16), (260, 8, 8), (8, 8, 300)])
+# kernel with the run-time buffer stride, as the 512^3 grid does.  An even
+# nx stages the y sweep's inputs with TMA boxes of 132 positions (one box
+# per pencil group; two for (10, 150, 6), whose second box ends beyond the
+# grid); an odd nx keeps the per-thread loads.
+@pytest.mark.parametrize("shape", [(12, 10, 8), (9, 7, 11), (18, 13, 6), (20, 12, 16), (10, 150, 6), (260, 8, 8),
+                                   (8, 8, 300)])
 def test_fp32_close_to_oracle_on_any_grid(shape):
     st = _random_box(shape)
     g = native.Mhd3D(st.params, precision=native.PREC_FP32)
