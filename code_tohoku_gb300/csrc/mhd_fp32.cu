@@ -124,7 +124,8 @@ static bool sweep_tma_map(const SweepArgs &a, const double *block, int narr, Swe
   if (!enc) return false;
   const cuuint64_t dims[4] = {(cuuint64_t)g.s[0], (cuuint64_t)g.s[1], (cuuint64_t)g.s[2], (cuuint64_t)narr};
   const cuuint64_t strides[3] = {(cuuint64_t)g.s[0] * 8, (cuuint64_t)g.s[0] * g.s[1] * 8, (cuuint64_t)nc * 8};
-  const cuuint32_t box[4] = {(cuuint32_t)P, DIR == 1 ? (cuuint32_t)kStageRows : 1u,
+  const cuuint32_t box[4] = {DIR == 0 ? (cuuint32_t)kStageRows : (cuuint32_t)P,
+                             DIR == 0 ? (cuuint32_t)P : DIR == 1 ? (cuuint32_t)kStageRows : 1u,
                              DIR == 2 ? (cuuint32_t)kStageRows : 1u, 1u};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   return enc(&T.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<double *>(block), dims, strides, box, estr,
@@ -172,6 +173,13 @@ static cudaError_t launch32_d(const SweepArgs &a, const double *block, int narr,
     }
     if (L <= kSweepFixedStride && sweep32_smem_bytes(a.g.n[DIR], kSweepZPencils, kSweepFixedStride) <= 226 * 1024)
       return launch32<DIR, kSweepZPencils, kSweepFixedStride, kSweepZThreads, 1>(a, s);
+  }
+  if constexpr (DIR == 0) {
+    if ((MHD_SWEEP_TMA & 1) && nb % 4 == 0 && L <= kSweepTmaStride &&
+        sweep32_smem_bytes(a.g.n[DIR], 4, kSweepTmaStride) <= kSweepSmemPerCta) {
+      SweepTma T;
+      if (sweep_tma_map<DIR, 4>(a, block, narr, T)) return launch32<DIR, 4, kSweepTmaStride, NT, MB, true>(a, s, T);
+    }
   }
   if constexpr (DIR == 1) {
     if (((MHD_SWEEP_TMA >> 1) & 1) && L <= kSweepTmaStride &&

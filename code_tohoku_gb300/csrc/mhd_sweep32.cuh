@@ -180,12 +180,11 @@ struct PencilRun {
   }
 };
 
-// The TMA load phase of the y and z sweeps.  The handle's FP64 arrays are
-// one allocation of equal-sized arrays, seen by the tensor map as a 4-D
-// tensor (x, y, z, array); a box is P x columns by kStageRows positions
-// along the sweep of one array (y sweep {P, R, 1, 1}, z sweep {P, 1, R, 1}),
-// so an array's pencil group lands in shared memory as [position][pencil],
-// the layout of the FP32 buffers.  fld holds the array index of each input,
+// The TMA load phase of the sweeps.  The handle's FP64 arrays are one
+// allocation of equal-sized arrays, seen by the tensor map as a 4-D tensor
+// (x, y, z, array); a box is kStageRows positions along the sweep of P
+// pencils of one array (x sweep {R, P, 1, 1}, y sweep {P, R, 1, 1}, z sweep
+// {P, 1, R, 1}).  fld holds the array index of each input,
 // in the order of the stage rounds (SF_*).
 constexpr int kStageRows = 132;   // positions per box: two boxes cover a 256-cell pencil and its ghosts
 enum {
@@ -203,11 +202,11 @@ struct SweepTma {
 // LS > 0: every pencil buffer is LS positions long, a compile-time stride,
 // so each shared-memory access is one load or store at a constant offset
 // from a per-item base address; LS = 0: the stride is n+4, computed at run
-// time (any length).  TM: the y or z sweep stages its FP64 inputs with TMA
-// box loads (LS = 2 kStageRows, the staged rows of a pencil group).
+// time (any length).  TM: the sweep stages its FP64 inputs with TMA box
+// loads (LS = 2 kStageRows, the staged positions of a pencil group).
 template <int DIR, int P, int NT, int MINB, int LS, bool TM = false>
 __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __grid_constant__ SweepTma T) {
-  static_assert(!TM || (DIR != 0 && LS == 2 * kStageRows && P % 2 == 0), "TMA staging: y/z sweeps, staged stride");
+  static_assert(!TM || (LS == 2 * kStageRows && P % 2 == 0), "TMA staging: staged stride, 16-byte rows");
   extern __shared__ __align__(128) float smf[];
   const Grid &g = A.g;
   const int N = g.n[DIR];
@@ -402,13 +401,25 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __
     const uint32_t sbase = tc::smem_u32(smf);
     const int slot_doubles = LB * P;   // one slot: LB positions x P pencils of FP64
     const double *stg = reinterpret_cast<const double *>(smf);
-    auto st = [&](int slot, int i, int p) -> double { return stg[slot * slot_doubles + (i + 1) * P + p]; };
+    // staged layout: y and z sweeps [position][pencil] (the box's columns
+    // are the pencils); x sweep [box][pencil][position in the box] (the
+    // box's rows are the pencils)
+    auto st = [&](int slot, int i, int p) -> double {
+      if constexpr (DIR == 0) {
+        const int r = i + 1, b = r / kStageRows;
+        return stg[slot * slot_doubles + (b * P + p) * kStageRows + (r - b * kStageRows)];
+      } else {
+        return stg[slot * slot_doubles + (i + 1) * P + p];
+      }
+    };
     if (tid == 0) {
       tc::mbar_init(&tbar, 1);
       tc::fence_mbar_init();
     }
     __syncthreads();
-    const int cx0 = P * (int)blockIdx.x;   // padded x of the group's first column
+    // y and z sweeps: padded x of the group's first column; x sweep: padded
+    // y of its first row
+    const int cx0 = DIR == 0 ? P * (int)blockIdx.x + 2 : P * (int)blockIdx.x;
     const int ct = (int)blockIdx.y + 2;    // padded index of the other transverse coordinate
     bool ok = (sbase & 127u) == 0;         // TMA writes 128-byte aligned boxes
     if (!ok && tid == 0) flag(A.err, ERRB_TMA);
@@ -419,7 +430,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __
         for (int q = 0; q < nf; q++)
           for (int b = 0; b < T.nbox; b++) {
             const uint32_t dst = sbase + (uint32_t)((q * slot_doubles + b * kStageRows * P) * 8);
-            if (DIR == 1) tc::tma_load_4d(dst, &T.map, cx0, b * kStageRows, ct, T.fld[f0 + q], &tbar);
+            if (DIR == 0) tc::tma_load_4d(dst, &T.map, b * kStageRows, cx0, ct, T.fld[f0 + q], &tbar);
+            else if (DIR == 1) tc::tma_load_4d(dst, &T.map, cx0, b * kStageRows, ct, T.fld[f0 + q], &tbar);
             else tc::tma_load_4d(dst, &T.map, cx0, ct, b * kStageRows, T.fld[f0 + q], &tbar);
           }
       }
