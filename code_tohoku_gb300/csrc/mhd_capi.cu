@@ -6,6 +6,7 @@
 // issued here as a ghost exchange (ghost_fill_all) on the same fields and directions.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -88,6 +89,8 @@ struct mhd_handle {
   // first use)
   cudaStream_t io_stream = nullptr;
   cudaEvent_t ev_io[3] = {nullptr, nullptr, nullptr};
+  // mhd_step_host, chosen form: one event per slab of the last sweep
+  cudaEvent_t ev_slab[9] = {};
   std::vector<double> rdx_host, rdxc_host;   // staging for the async coordinate copies
   std::vector<float> dxf_host;
   std::string msg;
@@ -390,6 +393,8 @@ int mhd_destroy(mhd_handle *h) {
   }
   for (int e = 0; e < 3; e++)
     if (h->ev_io[e]) cudaEventDestroy(h->ev_io[e]);
+  for (cudaEvent_t e : h->ev_slab)
+    if (e) cudaEventDestroy(e);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return MHD_OK;
@@ -772,10 +777,86 @@ int mhd_step(mhd_handle *h, double tsave, double *dt, int *st) {
 }
 
 namespace {
+// Slabs of the last sweep in mhd_step_host's chosen form.  Without
+// chemistry rho and the species are final once the last sweep has passed
+// over them, so that sweep runs as kCopySlabs launches, each over a slab of
+// its pencil groups (z slabs for the x and y sweeps, y slabs for the z
+// sweep); after each, the ghost cells of rho and the species that lie in
+// the slab are filled (the passes of the exchange that stay inside it) and
+// the copy stream takes the slab's planes or rows back while the next slab
+// runs.  The ghost layers along the slab direction follow at the end, with
+// every pass.  The link back to the host is the bound of the call, so it
+// starts about a sweep earlier than after the whole sweep.
+constexpr int kCopySlabs = 8;
+
+int last_sweep_slabs(mhd_handle *h, int dir, double d, double *U_out, double *species_out) {
+  const Grid &g = h->g;
+  Fields &f = h->f;
+  TRY(need_inflow(h));
+  h->sh2_valid = false;   // the sweeps move the species
+  const int nby = dir == 2 ? g.n[1] : g.n[2];   // the sweep's transverse block index: y for z, else z
+  const int rdim = dir == 2 ? 1 : 2;            // the slab's coordinate
+  const int fdirs = dir == 2 ? 5 : 3;           // exchange passes that stay inside a slab
+  const int K = std::min(kCopySlabs, nby);
+  for (int e = 0; e <= K; e++)
+    if (!h->ev_slab[e]) CKR(cudaEventCreateWithFlags(&h->ev_slab[e], cudaEventDisableTiming));
+  const size_t nc = (size_t)g.ncell, row = (size_t)g.s[0], plane = (size_t)g.s[0] * g.s[1];
+  FillArgs fr{};   // rho: two layers, every direction (:2481-2486, CC(2))
+  fr.nf = 1;
+  fr.f[0] = f.U[0];
+  fr.rule[0] = IN_RHO;
+  fr.in = h->ph.in;
+  FillArgs fs{};   // species 0-4 (thermal SOURCE): one layer, interior transverse lines
+  fs.nf = 5;
+  for (int q = 0; q < 5; q++) {
+    fs.f[q] = f.sp[q];
+    fs.rule[q] = IN_SPEC + q;
+  }
+  fs.spmask = 31u;
+  fs.in = h->ph.in;
+  const bool sp_fill = h->p.ifthrm == 2;
+  // the copies back of rho and the 8 species over padded [lo, hi) along rdim
+  auto copy_back = [&](int lo, int hi) -> cudaError_t {
+    for (int q = 0; q < 9; q++) {
+      const double *src = q == 0 ? f.U[0] : f.sp[q - 1];
+      double *dst = q == 0 ? U_out : species_out + (size_t)(q - 1) * nc;
+      cudaError_t e;
+      if (rdim == 2)
+        e = cudaMemcpyAsync(dst + lo * plane, src + lo * plane, (size_t)(hi - lo) * plane * sizeof(double),
+                            cudaMemcpyDeviceToHost, h->io_stream);
+      else
+        e = cudaMemcpy2DAsync(dst + lo * row, plane * sizeof(double), src + lo * row, plane * sizeof(double),
+                              (size_t)(hi - lo) * row * sizeof(double), (size_t)g.s[2], cudaMemcpyDeviceToHost,
+                              h->io_stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+  SweepArgs a{};
+  a.g = g; a.ph = h->ph; a.f = f; a.dt = d; a.err = h->err;
+  for (int sl = 0; sl < K; sl++) {
+    a.by0 = (int)((long long)nby * sl / K);
+    a.by1 = (int)((long long)nby * (sl + 1) / K);
+    CK(sweep_fp32(dir, a, h->block, kStateArrays, h->stream));
+    CK(ghost_fill_slab(g, fr, fdirs, 2, rdim, a.by0 + 2, a.by1 + 2, false, h->stream));
+    if (sp_fill) CK(ghost_fill_slab(g, fs, fdirs, 1, rdim, a.by0 + 2, a.by1 + 2, false, h->stream));
+    CKR(cudaEventRecord(h->ev_slab[sl], h->stream));
+    CKR(cudaStreamWaitEvent(h->io_stream, h->ev_slab[sl], 0));
+    CKR(copy_back(a.by0 + 2, a.by1 + 2));
+  }
+  CK(ghost_fill_slab(g, fr, 7, 2, rdim, 2, nby + 2, true, h->stream));
+  if (sp_fill) CK(ghost_fill_slab(g, fs, 7, 1, rdim, 2, nby + 2, true, h->stream));
+  CKR(cudaEventRecord(h->ev_slab[K], h->stream));
+  CKR(cudaStreamWaitEvent(h->io_stream, h->ev_slab[K], 0));
+  CKR(copy_back(0, 2));
+  CKR(copy_back(nby + 2, nby + 4));
+  return MHD_OK;
+}
+
 // the EVOLVE iteration of mhd_advance for mhd_step_host, copying arrays
 // back as soon as they are final: without chemistry rho and the species are
-// final after the sweeps (once their ghosts are filled), the face field
-// after CC
+// final after the sweeps (once their ghosts are filled; in the chosen form
+// slab by slab during the last sweep), the face field after CC
 // late_species: species 5-7 are still coming in on the copy stream (event
 // ev_io[2]); the first sweep, their first reader, waits for them
 int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, bool late_species) {
@@ -785,10 +866,14 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, 
   if (h->p.ifgrv == 2) TRY(gravity_half_kick(h, d));   // EVOLVE :607
   TRY(mhd_source(h, 0.5 * d));
   if (late_species) CKR(cudaStreamWaitEvent(h->stream, h->ev_io[2], 0));
-  for (int q = 0; q < 3; q++) TRY(mhd_sweep(h, orders[h->ifevo - 1][q], d));
+  const int *order = orders[h->ifevo - 1];
   h->ifevo = h->ifevo % 6 + 1;
   const bool early = h->p.ifchem != 2;
-  if (early) {
+  const bool slabs = early && h->p.precision == MHD_PREC_FP32;
+  for (int q = 0; q < (slabs ? 2 : 3); q++) TRY(mhd_sweep(h, order[q], d));
+  if (slabs) {
+    TRY(last_sweep_slabs(h, order[2], d, U_out, species_out));
+  } else if (early) {
     // the ghost fills CC(2) and SOURCE would make, made now
     TRY(fill(h, {f.U[0]}, 7, 2, 0, {IN_RHO}));
     if (h->p.ifthrm == 2)

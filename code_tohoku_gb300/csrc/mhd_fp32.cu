@@ -144,10 +144,14 @@ static cudaError_t launch32(const SweepArgs &a, cudaStream_t s, const SweepTma &
   // starting at padded x = P*blockIdx.x, which covers x = -1 .. n+2
   const unsigned xgroups = (unsigned)((g.n[0] + 2 + P - 1) / P);
   dim3 grid;
-  if (DIR == 0) grid = dim3(g.n[1] / P, g.n[2]);
-  else if (DIR == 1) grid = dim3(xgroups, g.n[2]);
-  else grid = dim3(xgroups, g.n[1]);
-  k<<<grid, NT, smem, s>>>(a, T);
+  const int nby = (DIR == 2) ? g.n[1] : g.n[2];   // transverse block index: z for x and y, y for z
+  const int by0 = a.by1 > 0 ? a.by0 : 0, by1 = a.by1 > 0 ? a.by1 : nby;
+  if (by0 < 0 || by1 > nby || by0 >= by1) return cudaErrorInvalidValue;
+  if (DIR == 0) grid = dim3(g.n[1] / P, by1 - by0);
+  else grid = dim3(xgroups, by1 - by0);
+  SweepArgs ar = a;
+  ar.by0 = by0;
+  k<<<grid, NT, smem, s>>>(ar, T);
   return cudaGetLastError();
 }
 

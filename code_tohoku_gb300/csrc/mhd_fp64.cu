@@ -28,7 +28,16 @@ cudaError_t emf_fp64(int e, const CTArgs &a, cudaStream_t s) { return launch_emf
 static unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 cudaError_t ghost_fill_all(const Grid &g, const FillArgs &f, int dirs, int nol, cudaStream_t s) {
+  return ghost_fill_slab(g, f, dirs, nol, -1, 0, 0, false, s);
+}
+
+cudaError_t ghost_fill_slab(const Grid &g, const FillArgs &f, int dirs, int nol, int rdim, int rlo, int rhi,
+                            bool outside, cudaStream_t s) {
   FillAll r{};
+  r.rdim = rdim;
+  r.rlo = rlo;
+  r.rhi = rhi;
+  r.rout = outside ? 1 : 0;
   const bool mk[3] = {(dirs & 1) != 0, (dirs & 2) != 0, (dirs & 4) != 0};
   for (int reg = 0; reg < 3; reg++) {
     if (!mk[reg]) continue;

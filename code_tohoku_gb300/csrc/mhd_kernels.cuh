@@ -398,6 +398,9 @@ struct FillArgs {
 // and free / periodic sides).
 struct FillAll {
   long long nreg[3];   // threads per array in the x, y and z shells
+  // rdim >= 0: only the ghost cells whose padded index along rdim lies in
+  // [rlo, rhi) (a slab of the grid), or outside it when rout is set
+  int rdim, rlo, rhi, rout;
 };
 __device__ __forceinline__ int fill_layer(int f, int nol, int N) {   // f-th filled ghost index
   return f < nol ? 1 - nol + f : N + 1 + (f - nol);
@@ -428,6 +431,7 @@ __global__ void ghost_fill_all_kernel(Grid g, FillArgs a, int dirs, int nol, Fil
     for (int d = 0; d < 3; d++)
       c[d] = d == reg ? fill_layer(e[d], nol, N[d]) : (d < reg ? fill_other(e[d], mk[d], nol, N[d]) : e[d] - 1);
   }
+  if (r.rdim >= 0 && ((c[r.rdim] + 1 >= r.rlo && c[r.rdim] + 1 < r.rhi) == (r.rout != 0))) return;
   double *F = a.f[fi];
   const bool species = (a.spmask >> fi) & 1u;
   const int rule = a.rule[fi];
@@ -486,6 +490,9 @@ struct SweepArgs {
   Fields f;
   double dt;
   int *err;
+  // the chosen-form sweep may run over the pencil groups of blockIdx.y in
+  // [by0, by1) only (by1 = 0: all of them); the plain form runs them all
+  int by0, by1;
 };
 
 template <int DIR, int P>

@@ -51,6 +51,10 @@ cudaError_t surrogate_pack(const float *master, SurNet *net, cudaStream_t s);
 // precision-independent FP64 kernels (built in the FP64 unit)
 // one ghost exchange over every direction in dirs, one launch
 cudaError_t ghost_fill_all(const Grid &g, const FillArgs &f, int dirs, int nol, cudaStream_t s);
+// the same exchange restricted to the ghost cells whose padded index along
+// rdim lies in [rlo, rhi), or outside it (rdim = -1: all)
+cudaError_t ghost_fill_slab(const Grid &g, const FillArgs &f, int dirs, int nol, int rdim, int rlo, int rhi,
+                            bool outside, cudaStream_t s);
 cudaError_t face_velocity(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
 cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const double *ex, const double *ey, double dt,
                    cudaStream_t s);

@@ -156,16 +156,17 @@ struct PencilRun {
   int b0, sp, sd;   // 32-bit cell offsets: the padded grid has fewer than 2^31 cells
   unsigned act;   // bit p: pencil p is an interior pencil
   int plast;      // last pencil inside the padded grid
-  __device__ PencilRun(const Grid &g) {
+  // by: the CTA's transverse block index (blockIdx.y plus the launch's offset)
+  __device__ PencilRun(const Grid &g, int by) {
     sd = (int)g.st[DIR];
     act = (1u << P) - 1;
     plast = P - 1;
     if (DIR == 0) {
-      b0 = (int)gidx(g, -1, blockIdx.x * P + 1, blockIdx.y + 1);
+      b0 = (int)gidx(g, -1, blockIdx.x * P + 1, by + 1);
       sp = (int)g.st[1];
     } else {
       const int x0 = (int)blockIdx.x * P - 1;
-      b0 = (int)((DIR == 1) ? gidx(g, x0, -1, blockIdx.y + 1) : gidx(g, x0, blockIdx.y + 1, -1));
+      b0 = (int)((DIR == 1) ? gidx(g, x0, -1, by + 1) : gidx(g, x0, by + 1, -1));
       sp = 1;
       act = 0;
       for (int p = 0; p < P; p++)
@@ -219,7 +220,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __
   const float kb = (float)A.ph.kb;
   const int tid = threadIdx.x;
   const double *rdx = g.rdx[DIR];
-  PencilRun<DIR, P> pc(g);
+  const int by = (int)blockIdx.y + A.by0;   // transverse block index (a launch may cover a slab)
+  PencilRun<DIR, P> pc(g, by);
   constexpr int C1 = (DIR + 1) % 3, C2 = (DIR + 2) % 3;
   auto Fb = [&](int b, int i, int p) -> float & { return smf[b * LP + (i + 1) * P + p]; };
   auto cx = [&](int c, int i) -> float { return cf[c * LB + i + 1]; };
@@ -234,10 +236,10 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __
     if (!inR && (perR ? i == 2 : i == N)) fn(N + 2);
   };
   // value of an inflow ghost cell gi of pencil p under rule r (DIR == 0:
-  // pencil p is row (blockIdx.x*P+p+1, blockIdx.y+1)); two rules of this
+  // pencil p is row (blockIdx.x*P+p+1, by+1)); two rules of this
   // kernel's derived buffers: the species sum of gamma and the remap switch
   auto inflow32 = [&](int r, int side, int gi, int p) -> float {
-    const int j = blockIdx.x * P + p + 1, k = blockIdx.y + 1;
+    const int j = blockIdx.x * P + p + 1, k = by + 1;
     if (r == IN_SSUM) {
       const double rho = inflow_rho(g, A.ph.in, side, gi, j, k);
       const double *cm = A.ph.in.cm;
@@ -420,7 +422,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __
     // y and z sweeps: padded x of the group's first column; x sweep: padded
     // y of its first row
     const int cx0 = DIR == 0 ? P * (int)blockIdx.x + 2 : P * (int)blockIdx.x;
-    const int ct = (int)blockIdx.y + 2;    // padded index of the other transverse coordinate
+    const int ct = by + 2;                 // padded index of the other transverse coordinate
     bool ok = (sbase & 127u) == 0;         // TMA writes 128-byte aligned boxes
     if (!ok && tid == 0) flag(A.err, ERRB_TMA);
     auto round = [&](int r, int f0, int nf) {

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from code_tohoku_gb300 import native, problems
+from test_gpu_fp32_form import _random_box
 from test_gpu_inflow import shock_tube
 
 pytestmark = pytest.mark.gpu
@@ -37,6 +38,27 @@ def run_both(st, precision, steps, inflow=None):
 def test_step_host_equals_device_steps(precision):
     st = problems.colliding_flows(16)
     Ur, Sr, U, S = run_both(st, precision, 4)
+    assert np.array_equal(Ur.view(np.int64), U.view(np.int64))
+    assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
+
+
+def test_step_host_slabs_every_sweep_order():
+    """The chosen form copies rho and the species back slab by slab during
+    the last sweep (z slabs after an x or y sweep, y slabs after a z sweep):
+    six steps take every sweep order, on a grid whose extents differ and do
+    not divide into equal slabs."""
+    st = _random_box((24, 18, 13))
+    Ur, Sr, U, S = run_both(st, native.PREC_FP32, 6)
+    assert np.array_equal(Ur.view(np.int64), U.view(np.int64))
+    assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
+
+
+def test_step_host_slabs_inflow():
+    """Slabbed copies with BC=4 inflow on both x sides (the slab exchanges
+    apply the inflow rules of rho and the species), chosen form."""
+    st = shock_tube(16, 12, 10)
+    inflow, dinit = problems.shock_tube_inflow()
+    Ur, Sr, U, S = run_both(st, native.PREC_FP32, 4, inflow=(inflow, None, dinit))
     assert np.array_equal(Ur.view(np.int64), U.view(np.int64))
     assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
 
