@@ -89,8 +89,10 @@ struct mhd_handle {
   // first use)
   cudaStream_t io_stream = nullptr;
   cudaEvent_t ev_io[3] = {nullptr, nullptr, nullptr};
-  // mhd_step_host, chosen form: one event per slab of the last sweep
+  // mhd_step_host, chosen form: one event per slab of the last sweep, and
+  // per slab of the late species copies the first sweep waits for
   cudaEvent_t ev_slab[9] = {};
+  cudaEvent_t ev_late[8] = {};
   std::vector<double> rdx_host, rdxc_host;   // staging for the async coordinate copies
   std::vector<float> dxf_host;
   std::string msg;
@@ -394,6 +396,8 @@ int mhd_destroy(mhd_handle *h) {
   for (int e = 0; e < 3; e++)
     if (h->ev_io[e]) cudaEventDestroy(h->ev_io[e]);
   for (cudaEvent_t e : h->ev_slab)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->ev_late)
     if (e) cudaEventDestroy(e);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -788,19 +792,47 @@ namespace {
 // every pass.  The link back to the host is the bound of the call, so it
 // starts about a sweep earlier than after the whole sweep.
 constexpr int kCopySlabs = 8;
+// slabs of rows (after or before a z sweep) are copied with 2-D copies of
+// one row range per plane
+#ifndef MHD_COPY_SLABS_ROWS
+#define MHD_COPY_SLABS_ROWS 8
+#endif
+constexpr int kCopySlabsRows = MHD_COPY_SLABS_ROWS;
+constexpr int kSweepOrders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
+
+// the slabs of a direction-dir sweep: K ranges of its transverse block index
+// (z for the x and y sweeps, y for the z sweep), i.e. of the padded
+// coordinate rdim from lo(s) + 2 to lo(s + 1) + 2
+struct Slabs {
+  int nby, rdim, K;
+  Slabs(const Grid &g, int dir)
+      : nby(dir == 2 ? g.n[1] : g.n[2]), rdim(dir == 2 ? 1 : 2),
+        K(std::min(dir == 2 ? kCopySlabsRows : kCopySlabs, dir == 2 ? g.n[1] : g.n[2])) {}
+  int lo(int s) const { return (int)((long long)nby * s / K); }
+};
+
+// copy of one array over padded [lo, hi) along rdim: whole planes (rdim 2)
+// or those rows of every plane (rdim 1)
+cudaError_t copy_range(const Grid &g, int rdim, double *dst, const double *src, int lo, int hi, cudaMemcpyKind kind,
+                       cudaStream_t st) {
+  const size_t row = (size_t)g.s[0], plane = (size_t)g.s[0] * g.s[1];
+  if (rdim == 2)
+    return cudaMemcpyAsync(dst + lo * plane, src + lo * plane, (size_t)(hi - lo) * plane * sizeof(double), kind, st);
+  return cudaMemcpy2DAsync(dst + lo * row, plane * sizeof(double), src + lo * row, plane * sizeof(double),
+                           (size_t)(hi - lo) * row * sizeof(double), (size_t)g.s[2], kind, st);
+}
 
 int last_sweep_slabs(mhd_handle *h, int dir, double d, double *U_out, double *species_out) {
   const Grid &g = h->g;
   Fields &f = h->f;
   TRY(need_inflow(h));
   h->sh2_valid = false;   // the sweeps move the species
-  const int nby = dir == 2 ? g.n[1] : g.n[2];   // the sweep's transverse block index: y for z, else z
-  const int rdim = dir == 2 ? 1 : 2;            // the slab's coordinate
-  const int fdirs = dir == 2 ? 5 : 3;           // exchange passes that stay inside a slab
-  const int K = std::min(kCopySlabs, nby);
+  const Slabs sb(g, dir);
+  const int nby = sb.nby, rdim = sb.rdim, K = sb.K;
+  const int fdirs = dir == 2 ? 5 : 3;   // exchange passes that stay inside a slab
   for (int e = 0; e <= K; e++)
     if (!h->ev_slab[e]) CKR(cudaEventCreateWithFlags(&h->ev_slab[e], cudaEventDisableTiming));
-  const size_t nc = (size_t)g.ncell, row = (size_t)g.s[0], plane = (size_t)g.s[0] * g.s[1];
+  const size_t nc = (size_t)g.ncell;
   FillArgs fr{};   // rho: two layers, every direction (:2481-2486, CC(2))
   fr.nf = 1;
   fr.f[0] = f.U[0];
@@ -820,14 +852,7 @@ int last_sweep_slabs(mhd_handle *h, int dir, double d, double *U_out, double *sp
     for (int q = 0; q < 9; q++) {
       const double *src = q == 0 ? f.U[0] : f.sp[q - 1];
       double *dst = q == 0 ? U_out : species_out + (size_t)(q - 1) * nc;
-      cudaError_t e;
-      if (rdim == 2)
-        e = cudaMemcpyAsync(dst + lo * plane, src + lo * plane, (size_t)(hi - lo) * plane * sizeof(double),
-                            cudaMemcpyDeviceToHost, h->io_stream);
-      else
-        e = cudaMemcpy2DAsync(dst + lo * row, plane * sizeof(double), src + lo * row, plane * sizeof(double),
-                              (size_t)(hi - lo) * row * sizeof(double), (size_t)g.s[2], cudaMemcpyDeviceToHost,
-                              h->io_stream);
+      const cudaError_t e = copy_range(g, rdim, dst, src, lo, hi, cudaMemcpyDeviceToHost, h->io_stream);
       if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -835,8 +860,8 @@ int last_sweep_slabs(mhd_handle *h, int dir, double d, double *U_out, double *sp
   SweepArgs a{};
   a.g = g; a.ph = h->ph; a.f = f; a.dt = d; a.err = h->err;
   for (int sl = 0; sl < K; sl++) {
-    a.by0 = (int)((long long)nby * sl / K);
-    a.by1 = (int)((long long)nby * (sl + 1) / K);
+    a.by0 = sb.lo(sl);
+    a.by1 = sb.lo(sl + 1);
     CK(sweep_fp32(dir, a, h->block, kStateArrays, h->stream));
     CK(ghost_fill_slab(g, fr, fdirs, 2, rdim, a.by0 + 2, a.by1 + 2, false, h->stream));
     if (sp_fill) CK(ghost_fill_slab(g, fs, fdirs, 1, rdim, a.by0 + 2, a.by1 + 2, false, h->stream));
@@ -853,24 +878,45 @@ int last_sweep_slabs(mhd_handle *h, int dir, double d, double *U_out, double *sp
   return MHD_OK;
 }
 
+// The first sweep of mhd_step_host's chosen form in the slabs of its
+// direction, each waiting for that slab of species 5-7 (ev_late), which the
+// copy stream brings in last: the sweep starts on the first slab while the
+// others are still on the link.
+int first_sweep_slabs(mhd_handle *h, int dir, double d) {
+  TRY(need_inflow(h));
+  h->sh2_valid = false;   // the sweeps move the species
+  const Slabs sb(h->g, dir);
+  SweepArgs a{};
+  a.g = h->g; a.ph = h->ph; a.f = h->f; a.dt = d; a.err = h->err;
+  for (int sl = 0; sl < sb.K; sl++) {
+    a.by0 = sb.lo(sl);
+    a.by1 = sb.lo(sl + 1);
+    CKR(cudaStreamWaitEvent(h->stream, h->ev_late[sl], 0));
+    CK(sweep_fp32(dir, a, h->block, kStateArrays, h->stream));
+  }
+  return MHD_OK;
+}
+
 // the EVOLVE iteration of mhd_advance for mhd_step_host, copying arrays
 // back as soon as they are final: without chemistry rho and the species are
 // final after the sweeps (once their ghosts are filled; in the chosen form
 // slab by slab during the last sweep), the face field after CC
 // late_species: species 5-7 are still coming in on the copy stream (event
-// ev_io[2]); the first sweep, their first reader, waits for them
-int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, bool late_species) {
+// ev_io[2]; by slabs of the first sweep, events ev_late, when late_slabs);
+// the first sweep, their first reader, waits for them
+int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, bool late_species,
+                   bool late_slabs) {
   const size_t nc = (size_t)h->g.ncell, nb = nc * sizeof(double);
   Fields &f = h->f;
-  static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
   if (h->p.ifgrv == 2) TRY(gravity_half_kick(h, d));   // EVOLVE :607
   TRY(mhd_source(h, 0.5 * d));
-  if (late_species) CKR(cudaStreamWaitEvent(h->stream, h->ev_io[2], 0));
-  const int *order = orders[h->ifevo - 1];
+  if (late_species && !late_slabs) CKR(cudaStreamWaitEvent(h->stream, h->ev_io[2], 0));
+  const int *order = kSweepOrders[h->ifevo - 1];
   h->ifevo = h->ifevo % 6 + 1;
   const bool early = h->p.ifchem != 2;
   const bool slabs = early && h->p.precision == MHD_PREC_FP32;
-  for (int q = 0; q < (slabs ? 2 : 3); q++) TRY(mhd_sweep(h, order[q], d));
+  if (late_species && late_slabs) TRY(first_sweep_slabs(h, order[0], d));
+  for (int q = (late_species && late_slabs) ? 1 : 0; q < (slabs ? 2 : 3); q++) TRY(mhd_sweep(h, order[q], d));
   if (slabs) {
     TRY(last_sweep_slabs(h, order[2], d, U_out, species_out));
   } else if (early) {
@@ -908,7 +954,7 @@ namespace {
 // mhd_step_host after the copies in: CC(4), the time step (mhd_step's
 // clipping), then the step with its copies back
 int step_host_run(mhd_handle *h, double tsave, double *dt, int *st, double *U_out, double *species_out,
-                  bool late_species) {
+                  bool late_species, bool late_slabs) {
   Fields &f = h->f;
   CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
   TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
@@ -920,7 +966,7 @@ int step_host_run(mhd_handle *h, double tsave, double *dt, int *st, double *U_ou
   if (!(d > 0.0)) return fail(h, MHD_ERR_DT, "dt <= 0 after clipping (time %.17g)", h->time);
   *dt = d;
   *st = s;
-  return step_host_body(h, d, U_out, species_out, late_species);
+  return step_host_body(h, d, U_out, species_out, late_species, late_slabs);
 }
 }  // namespace
 
@@ -955,11 +1001,32 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
       return fail(h, MHD_ERR_CUDA, "state copy: %s", cudaGetErrorString(e));
     }
   }
+  // In the chosen form those three arrays come in by slabs of the first
+  // sweep (interior slabs in the sweep's order, then the ghost layers), an
+  // event after each slab, and the sweep's slabs wait for their own.
+  const bool late_slabs = late && h->p.precision == MHD_PREC_FP32;
   if (late) {
     cudaError_t e = cudaEventRecord(h->ev_io[2], h->stream);   // after everything queued before (readers included)
     if (e == cudaSuccess) e = cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0);
-    for (int q = 5; q < 8 && e == cudaSuccess; q++)
-      e = cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->io_stream);
+    if (late_slabs) {
+      const Slabs sb(g, kSweepOrders[h->ifevo - 1][0]);
+      for (int sl = 0; sl < sb.K && e == cudaSuccess; sl++) {
+        if (!h->ev_late[sl]) e = cudaEventCreateWithFlags(&h->ev_late[sl], cudaEventDisableTiming);
+        for (int q = 5; q < 8 && e == cudaSuccess; q++)
+          e = copy_range(g, sb.rdim, f.sp[q], species_in + q * nc, sb.lo(sl) + 2, sb.lo(sl + 1) + 2,
+                         cudaMemcpyHostToDevice, h->io_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(h->ev_late[sl], h->io_stream);
+      }
+      for (int q = 5; q < 8 && e == cudaSuccess; q++) {
+        e = copy_range(g, sb.rdim, f.sp[q], species_in + q * nc, 0, 2, cudaMemcpyHostToDevice, h->io_stream);
+        if (e == cudaSuccess)
+          e = copy_range(g, sb.rdim, f.sp[q], species_in + q * nc, sb.nby + 2, sb.nby + 4, cudaMemcpyHostToDevice,
+                         h->io_stream);
+      }
+    } else {
+      for (int q = 5; q < 8 && e == cudaSuccess; q++)
+        e = cudaMemcpyAsync(f.sp[q], species_in + q * nc, nb, cudaMemcpyHostToDevice, h->io_stream);
+    }
     if (e == cudaSuccess) e = cudaEventRecord(h->ev_io[2], h->io_stream);
     if (e != cudaSuccess) {
       cudaStreamSynchronize(h->io_stream);   // no copy from the caller's buffers outlives the call
@@ -971,7 +1038,7 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   // never touched after return
   double d = 0.0;
   int s = 0;
-  const int r = step_host_run(h, tsave, &d, &s, U_out, species_out, late);
+  const int r = step_host_run(h, tsave, &d, &s, U_out, species_out, late, late_slabs);
   const cudaError_t es = cudaStreamSynchronize(h->io_stream);
   if (r != MHD_OK) {
     cudaStreamSynchronize(h->stream);   // its copies into U_out too
