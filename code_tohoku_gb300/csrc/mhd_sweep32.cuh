@@ -209,6 +209,10 @@ template <int DIR, int P, int NT, int MINB, int LS, bool TM = false>
 __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __grid_constant__ SweepTma T) {
   static_assert(!TM || (LS == 2 * kStageRows && P % 2 == 0), "TMA staging: staged stride, 16-byte rows");
   extern __shared__ __align__(128) float smf[];
+  // the x and y sweeps convert with the branching form (mhd_conv.cuh)
+  constexpr bool kBranchConv = DIR != 2;
+  auto d2f = [](double v) { return d2f_t<kBranchConv>(v); };
+  auto f2d = [](float v) { return f2d_t<kBranchConv>(v); };
   const Grid &g = A.g;
   const int N = g.n[DIR];
   const int L = N + 4;
