@@ -93,6 +93,9 @@ struct mhd_handle {
   // per slab of the late species copies the first sweep waits for
   cudaEvent_t ev_slab[9] = {};
   cudaEvent_t ev_late[8] = {};
+  // ... and per z slab of the state's copy in, which CC(4) and the time
+  // step's screen take slab by slab
+  cudaEvent_t ev_in[9] = {};
   std::vector<double> rdx_host, rdxc_host;   // staging for the async coordinate copies
   std::vector<float> dxf_host;
   std::string msg;
@@ -399,6 +402,8 @@ int mhd_destroy(mhd_handle *h) {
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : h->ev_late)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->ev_in)
+    if (e) cudaEventDestroy(e);
   if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return MHD_OK;
@@ -526,21 +531,35 @@ int mhd_download(mhd_handle *h, double *U, double *species, double *bcc) {
   return check_err(h);
 }
 
-int mhd_timestep(mhd_handle *h, double *dt, int *st) {
+}  // extern "C"
+
+namespace {
+// the reduction words of the time step at their starting values
+int timestep_reset(mhd_handle *h) {
+  CKR(cudaMemsetAsync(h->dtred, 0xff, 2 * sizeof(unsigned long long), h->stream));
+  if (h->p.precision == MHD_PREC_FP32) {
+    CKR(cudaMemsetAsync(h->dtwords, 0xff, 3 * sizeof(unsigned), h->stream));
+    CKR(cudaMemsetAsync(h->dtwords + 3, 0, sizeof(unsigned), h->stream));
+  }
+  return MHD_OK;
+}
+
+// mhd_timestep; screened: the chosen form's words were reset and every cell
+// screened by the caller (mhd_step_host, slab by slab as the state comes in)
+int timestep_impl(mhd_handle *h, double *dt, int *st, bool screened) {
   if (!h || !dt || !st) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
-  CKR(cudaMemsetAsync(h->dtred, 0xff, 2 * sizeof(unsigned long long), h->stream));
   const bool fp32 = h->p.precision == MHD_PREC_FP32;
+  if (!screened) TRY(timestep_reset(h));
   if (fp32) {
     // an FP32 screen of every cell, then the FP64 limits of the cells that
     // can hold the minimum: the same dt as the plain form, bit for bit.  The
     // screen reads S and H2 of the interior cells from SOURCE's arrays while
     // the species are unchanged since (the same floats).
-    CKR(cudaMemsetAsync(h->dtwords, 0xff, 3 * sizeof(unsigned), h->stream));
-    CKR(cudaMemsetAsync(h->dtwords + 3, 0, sizeof(unsigned), h->stream));
-    CK(dt_screen_fp32(h->g, h->ph, h->f, h->sh2_valid ? h->sh2_32 : nullptr, h->dtlo, h->dtwords, h->err,
-                      h->stream));
+    if (!screened)
+      CK(dt_screen_fp32(h->g, h->ph, h->f, h->sh2_valid ? h->sh2_32 : nullptr, h->dtlo, h->dtwords, h->err,
+                        h->stream));
     CK(dt_refine(h->g, h->ph, h->f, h->dtlo, h->dtwords, h->dtred, h->stream));
     CKR(cudaMemcpyAsync(h->h_small + 6, h->dtwords + 3, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
   } else {
@@ -576,6 +595,11 @@ int mhd_timestep(mhd_handle *h, double *dt, int *st) {
   *st = s;
   return MHD_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int mhd_timestep(mhd_handle *h, double *dt, int *st) { return timestep_impl(h, dt, st, false); }
 
 namespace {
 // the thermal branch of SOURCE (ifthrm = 2, :2477-2572); rho_sp_filled:
@@ -955,14 +979,31 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, 
 namespace {
 // mhd_step_host after the copies in: CC(4), the time step (mhd_step's
 // clipping), then the step with its copies back
+// in_slabs: the state comes in by z slabs (events ev_in), and CC(4) and the
+// time step's screen take each slab once it and the next have arrived (CC(4)
+// reads the z faces of the plane above)
 int step_host_run(mhd_handle *h, double tsave, double *dt, int *st, double *U_out, double *species_out,
-                  bool late_species, bool late_slabs) {
+                  bool late_species, bool late_slabs, bool in_slabs) {
   Fields &f = h->f;
-  CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
-  TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
   double d;
   int s;
-  TRY(mhd_timestep(h, &d, &s));
+  if (in_slabs) {
+    const Slabs zs(h->g, 0);
+    const long long plane = (long long)h->g.n[0] * h->g.n[1];
+    TRY(timestep_reset(h));
+    for (int sl = 0; sl < zs.K; sl++) {
+      const long long c0 = plane * zs.lo(sl), c1 = plane * zs.lo(sl + 1);
+      CKR(cudaStreamWaitEvent(h->stream, h->ev_in[sl + 1], 0));
+      CK(cell_b_range(h->g, f, c0, c1, h->stream));   // CC(4) as after mhd_upload
+      CK(dt_screen_fp32_range(h->g, h->ph, f, nullptr, h->dtlo, h->dtwords, h->err, c0, c1, h->stream));
+    }
+    TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
+    TRY(timestep_impl(h, &d, &s, true));
+  } else {
+    CK(cell_b(h->g, f, h->stream));   // CC(4) as after mhd_upload
+    TRY(fill(h, {f.bcc[0], f.bcc[1], f.bcc[2]}, 7, 2, 0, {IN_BCC1, IN_B2, IN_B3}));
+    TRY(mhd_timestep(h, &d, &s));
+  }
   if (h->time + d > h->p.tfinal) d = h->p.tfinal - h->time;
   if (h->time + d > tsave) d = tsave - h->time;
   if (!(d > 0.0)) return fail(h, MHD_ERR_DT, "dt <= 0 after clipping (time %.17g)", h->time);
@@ -989,8 +1030,38 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   // come in on the copy stream, after the other copies, while those kernels
   // run; the first sweep waits for them.
   const bool late = h->p.ifchem != 2 && h->p.ifrad != 2;
+  // In the chosen form (with species 5-7 late) the other 13 arrays come in
+  // on the copy stream by z slabs, an event after each, so that CC(4) and
+  // the time step's screen run on each slab while the next ones are on the
+  // link; the screen's blocks must not straddle a slab.
+  const bool in_slabs = late && h->p.precision == MHD_PREC_FP32 &&
+                        ((long long)g.n[0] * g.n[1]) % kDtScreenCells == 0;
   h->sh2_valid = false;
-  {
+  if (in_slabs) {
+    const Slabs zs(g, 0);
+    const int nz = g.n[2];
+    cudaError_t e = cudaEventRecord(h->ev_io[2], h->stream);   // after everything queued before (readers included)
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0);
+    auto copy13 = [&](int lo, int hi) -> cudaError_t {
+      cudaError_t r = cudaSuccess;
+      for (int q = 0; q < 13 && r == cudaSuccess; q++) {
+        double *dst = q < 8 ? f.U[q] : f.sp[q - 8];
+        const double *src = q < 8 ? U_in + q * nc : species_in + (q - 8) * nc;
+        r = copy_range(g, 2, dst, src, lo, hi, cudaMemcpyHostToDevice, h->io_stream);
+      }
+      return r;
+    };
+    if (e == cudaSuccess) e = copy13(0, 2);
+    for (int sl = 0; sl <= zs.K && e == cudaSuccess; sl++) {
+      e = sl < zs.K ? copy13(zs.lo(sl) + 2, zs.lo(sl + 1) + 2) : copy13(nz + 2, nz + 4);
+      if (e == cudaSuccess && !h->ev_in[sl]) e = cudaEventCreateWithFlags(&h->ev_in[sl], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(h->ev_in[sl], h->io_stream);
+    }
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(h->io_stream);   // no copy from the caller's buffers outlives the call
+      return fail(h, MHD_ERR_CUDA, "state copy: %s", cudaGetErrorString(e));
+    }
+  } else {
     // a failed enqueue waits for the copies already queued from U_in and
     // species_in, so no copy from the caller's buffers outlives the call
     cudaError_t e = cudaSuccess;
@@ -1008,8 +1079,12 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   // event after each slab, and the sweep's slabs wait for their own.
   const bool late_slabs = late && h->p.precision == MHD_PREC_FP32;
   if (late) {
-    cudaError_t e = cudaEventRecord(h->ev_io[2], h->stream);   // after everything queued before (readers included)
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0);
+    // (with in_slabs the copy stream already follows the main stream)
+    cudaError_t e = cudaSuccess;
+    if (!in_slabs) {
+      e = cudaEventRecord(h->ev_io[2], h->stream);   // after everything queued before (readers included)
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0);
+    }
     if (late_slabs) {
       const Slabs sb(g, kSweepOrders[h->ifevo - 1][0]);
       for (int sl = 0; sl < sb.K && e == cudaSuccess; sl++) {
@@ -1040,7 +1115,7 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
   // never touched after return
   double d = 0.0;
   int s = 0;
-  const int r = step_host_run(h, tsave, &d, &s, U_out, species_out, late, late_slabs);
+  const int r = step_host_run(h, tsave, &d, &s, U_out, species_out, late, late_slabs, in_slabs);
   const cudaError_t es = cudaStreamSynchronize(h->io_stream);
   if (r != MHD_OK) {
     cudaStreamSynchronize(h->stream);   // its copies into U_out too

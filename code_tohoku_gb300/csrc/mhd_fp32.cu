@@ -226,9 +226,15 @@ cudaError_t dt_screen_fp32(const Grid &g, const Phys &ph, const Fields &f, const
   // two cells per thread (a capped grid of 4864 blocks, ~13 cells per
   // thread and 50x fewer atomics, took 385 us at 256^3 against 333-358 for
   // one cell per thread)
-  DtScreen sc{lo, words, dt_screen_warps(g)};
-  dt32_screen_kernel<<<(unsigned)((n + kDtScreenCells - 1) / kDtScreenCells), kDtScreenThreads, 0, s>>>(g, ph, f,
-                                                                                                      sh2, sc, err);
+  return dt_screen_fp32_range(g, ph, f, sh2, lo, words, err, 0, n, s);
+}
+cudaError_t dt_screen_fp32_range(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, float *lo,
+                                 unsigned *words, int *err, long long c0, long long c1, cudaStream_t s) {
+  if (c0 % kDtScreenCells != 0) return cudaErrorInvalidValue;
+  if (c1 <= c0) return cudaSuccess;
+  DtScreen sc{lo, words, dt_screen_warps(g), (int)(c0 / kDtScreenCells)};
+  dt32_screen_kernel<<<(unsigned)((c1 - c0 + kDtScreenCells - 1) / kDtScreenCells), kDtScreenThreads, 0, s>>>(
+      g, ph, f, sh2, sc, err);
   return cudaGetLastError();
 }
 

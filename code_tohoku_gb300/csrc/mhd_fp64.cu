@@ -67,8 +67,12 @@ cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const doubl
 }
 
 cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s) {
-  long long n = (long long)g.n[0] * g.n[1] * g.n[2];
-  cell_b_kernel<<<nblk(n, 512), 256, 0, s>>>(g, f);
+  return cell_b_range(g, f, 0, (long long)g.n[0] * g.n[1] * g.n[2], s);
+}
+
+cudaError_t cell_b_range(const Grid &g, const Fields &f, long long c0, long long c1, cudaStream_t s) {
+  if (c1 <= c0) return cudaSuccess;
+  cell_b_kernel<<<nblk(c1 - c0, 512), 256, 0, s>>>(g, f, c0, c1);
   return cudaGetLastError();
 }
 

@@ -1059,10 +1059,11 @@ __device__ __forceinline__ double half_exact(double x) {
 }
 
 // two cells per thread, blockDim apart (every warp access stays coalesced),
-// the six loads of both issued before either is used
-__global__ void __launch_bounds__(256) cell_b_kernel(Grid g, Fields f) {
-  const long long n = (long long)g.n[0] * g.n[1] * g.n[2];
-  const long long t0 = (long long)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+// the six loads of both issued before either is used; interior cells of
+// linear index [c0, c1)
+__global__ void __launch_bounds__(256) cell_b_kernel(Grid g, Fields f, long long c0, long long c1) {
+  const long long n = c1;
+  const long long t0 = c0 + (long long)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
   double v[2][6];
   long long aa[2];
 #pragma unroll

@@ -38,6 +38,11 @@ cudaError_t temp_fp32(const Grid &g, const Fields &f, const double *pin, double 
 int dt_screen_warps(const Grid &g);
 cudaError_t dt_screen_fp32(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, float *lo,
                            unsigned *words, int *err, cudaStream_t s);
+// the screen of the interior cells of linear index [c0, c1); c0 and c1 - c0
+// multiples of kDtScreenCells (or c1 the last cell), so the slabs' blocks
+// are the whole screen's
+cudaError_t dt_screen_fp32_range(const Grid &g, const Phys &ph, const Fields &f, const float *sh2, float *lo,
+                                 unsigned *words, int *err, long long c0, long long c1, cudaStream_t s);
 cudaError_t face_velocity_fp32(const Grid &g, const Fields &f, double *v0, double *v1, double *v2, cudaStream_t s);
 cudaError_t ct_prep_fp32(const Grid &g, const Fields &f, double *const vf[3], double kb, const CT32Args &a,
                          cudaStream_t s);
@@ -59,6 +64,8 @@ cudaError_t face_velocity(const Grid &g, const Fields &f, double *v0, double *v1
 cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const double *ex, const double *ey, double dt,
                    cudaStream_t s);
 cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s);
+// CC(4) for the interior cells of linear index [c0, c1) (i fastest, then j, k)
+cudaError_t cell_b_range(const Grid &g, const Fields &f, long long c0, long long c1, cudaStream_t s);
 cudaError_t source_pass(const SourceArgs &a, cudaStream_t s);
 cudaError_t chem_step(const Grid &g, const Phys &ph, const Fields &f, double dt, int *err, cudaStream_t s);
 cudaError_t chem_totals(const Grid &g, const Fields &f, int plus, cudaStream_t s);

@@ -73,6 +73,9 @@ struct Source32Args {
 // implicit update P_b / (1 + c Lambda_b / P_b) (the explicit update when
 // Lambda_b heats).
 enum : int { STIFF_NETWORK = 1, STIFF_NEWTON = 2 };
+// the FP32 time-step screen: threads per block and cells per block (two per
+// thread)
+constexpr int kDtScreenThreads = 256, kDtScreenCells = 2 * kDtScreenThreads;
 constexpr int kFusedTiles = 2;                  // 128-cell tiles per CTA of the stiff-cell kernel
 constexpr int kFusedThreads = 128 * kFusedTiles;
 // block size of the explicit pass that lists the stiff cells (one list
@@ -367,6 +370,7 @@ struct DtScreen {
   float *lo;          // [3][nwarps]: per warp, the smallest lower end of c, tau, alpha
   unsigned *words;    // [0..2] smallest upper ends (float bits), [3] a cooling time at the floor
   int nwarps;
+  int boff;           // block index of the launch's first block (a slab of the grid)
 };
 // The FP32 rounding of these quantities stays below ~1e-6 relative (inputs
 // rounded once, IEEE quotients, the approximate square root): eta = 2^-14
@@ -383,12 +387,11 @@ constexpr float kDtEtaCoolSpecies = 1.0f / 256.0f;
 // screen moves ~72 bytes a cell and one cell per thread left it waiting on
 // memory.  The per-warp lower ends stay per 32 consecutive cells (the unit
 // the refine kernel walks).
-constexpr int kDtScreenThreads = 256, kDtScreenCells = 2 * kDtScreenThreads;
 __global__ void __launch_bounds__(kDtScreenThreads) dt32_screen_kernel(Grid g, Phys ph, Fields f, const float *sh2,
                                                                        DtScreen sc, int *err) {
   const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
   const long long ncells = (long long)nx * ny * nz;
-  const long long base = (long long)blockIdx.x * kDtScreenCells + threadIdx.x;
+  const long long base = ((long long)blockIdx.x + sc.boff) * kDtScreenCells + threadIdx.x;
   const float INF = __int_as_float(0x7f800000);
   const float dn = 1.0f - kDtEta, up = 1.0f + kDtEta;
   // the inputs of both cells first: rho, v1..v3, p, Bcc1..3 (and S, H2)
