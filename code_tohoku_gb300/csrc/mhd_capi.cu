@@ -824,6 +824,12 @@ constexpr int kCopySlabs = 8;
 #define MHD_COPY_SLABS_ROWS 4
 #endif
 constexpr int kCopySlabsRows = MHD_COPY_SLABS_ROWS;
+// slabs of the first sweep (and of the late species copies it waits for):
+// 26.49 -> 26.39 ms per call at 256^3 with four instead of eight
+#ifndef MHD_FIRST_SWEEP_SLABS
+#define MHD_FIRST_SWEEP_SLABS 4
+#endif
+constexpr int kFirstSweepSlabs = MHD_FIRST_SWEEP_SLABS;
 constexpr int kSweepOrders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
 
 // the slabs of a direction-dir sweep: K ranges of its transverse block index
@@ -831,9 +837,10 @@ constexpr int kSweepOrders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, 
 // coordinate rdim from lo(s) + 2 to lo(s + 1) + 2
 struct Slabs {
   int nby, rdim, K;
-  Slabs(const Grid &g, int dir)
+  // kmax: at most that many slabs (0: kCopySlabs, kCopySlabsRows for rows)
+  Slabs(const Grid &g, int dir, int kmax = 0)
       : nby(dir == 2 ? g.n[1] : g.n[2]), rdim(dir == 2 ? 1 : 2),
-        K(std::min(dir == 2 ? kCopySlabsRows : kCopySlabs, dir == 2 ? g.n[1] : g.n[2])) {}
+        K(std::min(kmax > 0 ? kmax : (dir == 2 ? kCopySlabsRows : kCopySlabs), dir == 2 ? g.n[1] : g.n[2])) {}
   int lo(int s) const { return (int)((long long)nby * s / K); }
 };
 
@@ -911,7 +918,7 @@ int last_sweep_slabs(mhd_handle *h, int dir, double d, double *U_out, double *sp
 int first_sweep_slabs(mhd_handle *h, int dir, double d) {
   TRY(need_inflow(h));
   h->sh2_valid = false;   // the sweeps move the species
-  const Slabs sb(h->g, dir);
+  const Slabs sb(h->g, dir, std::min(kFirstSweepSlabs, dir == 2 ? kCopySlabsRows : kCopySlabs));
   SweepArgs a{};
   a.g = h->g; a.ph = h->ph; a.f = h->f; a.dt = d; a.err = h->err;
   for (int sl = 0; sl < sb.K; sl++) {
@@ -979,9 +986,10 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, 
 namespace {
 // mhd_step_host after the copies in: CC(4), the time step (mhd_step's
 // clipping), then the step with its copies back
-// in_slabs: the state comes in by z slabs (events ev_in), and CC(4) and the
-// time step's screen take each slab once it and the next have arrived (CC(4)
-// reads the z faces of the plane above)
+// in_slabs: the state comes in by z slabs (events ev_in; the ghost planes
+// with the first and the last), and CC(4) and the time step's screen take
+// each slab once it and the next have arrived (CC(4) reads the z faces of
+// the plane above)
 int step_host_run(mhd_handle *h, double tsave, double *dt, int *st, double *U_out, double *species_out,
                   bool late_species, bool late_slabs, bool in_slabs) {
   Fields &f = h->f;
@@ -993,7 +1001,7 @@ int step_host_run(mhd_handle *h, double tsave, double *dt, int *st, double *U_ou
     TRY(timestep_reset(h));
     for (int sl = 0; sl < zs.K; sl++) {
       const long long c0 = plane * zs.lo(sl), c1 = plane * zs.lo(sl + 1);
-      CKR(cudaStreamWaitEvent(h->stream, h->ev_in[sl + 1], 0));
+      CKR(cudaStreamWaitEvent(h->stream, h->ev_in[std::min(sl + 1, zs.K - 1)], 0));
       CK(cell_b_range(h->g, f, c0, c1, h->stream));   // CC(4) as after mhd_upload
       CK(dt_screen_fp32_range(h->g, h->ph, f, nullptr, h->dtlo, h->dtwords, h->err, c0, c1, h->stream));
     }
@@ -1051,9 +1059,10 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
       }
       return r;
     };
-    if (e == cudaSuccess) e = copy13(0, 2);
-    for (int sl = 0; sl <= zs.K && e == cudaSuccess; sl++) {
-      e = sl < zs.K ? copy13(zs.lo(sl) + 2, zs.lo(sl + 1) + 2) : copy13(nz + 2, nz + 4);
+    // the ghost planes go with the first and the last slab (one copy per
+    // array and slab: the copy engine pays per copy)
+    for (int sl = 0; sl < zs.K && e == cudaSuccess; sl++) {
+      e = copy13(sl == 0 ? 0 : zs.lo(sl) + 2, sl == zs.K - 1 ? nz + 4 : zs.lo(sl + 1) + 2);
       if (e == cudaSuccess && !h->ev_in[sl]) e = cudaEventCreateWithFlags(&h->ev_in[sl], cudaEventDisableTiming);
       if (e == cudaSuccess) e = cudaEventRecord(h->ev_in[sl], h->io_stream);
     }
@@ -1075,8 +1084,8 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
     }
   }
   // In the chosen form those three arrays come in by slabs of the first
-  // sweep (interior slabs in the sweep's order, then the ghost layers), an
-  // event after each slab, and the sweep's slabs wait for their own.
+  // sweep (the ghost layers with the first and the last slab), an event
+  // after each slab, and the sweep's slabs wait for their own.
   const bool late_slabs = late && h->p.precision == MHD_PREC_FP32;
   if (late) {
     // (with in_slabs the copy stream already follows the main stream)
@@ -1086,19 +1095,14 @@ int mhd_step_host(mhd_handle *h, const double *U_in, const double *species_in, d
       if (e == cudaSuccess) e = cudaStreamWaitEvent(h->io_stream, h->ev_io[2], 0);
     }
     if (late_slabs) {
-      const Slabs sb(g, kSweepOrders[h->ifevo - 1][0]);
+      const int first = kSweepOrders[h->ifevo - 1][0];
+      const Slabs sb(g, first, std::min(kFirstSweepSlabs, first == 2 ? kCopySlabsRows : kCopySlabs));
       for (int sl = 0; sl < sb.K && e == cudaSuccess; sl++) {
         if (!h->ev_late[sl]) e = cudaEventCreateWithFlags(&h->ev_late[sl], cudaEventDisableTiming);
+        const int lo = sl == 0 ? 0 : sb.lo(sl) + 2, hi = sl == sb.K - 1 ? sb.nby + 4 : sb.lo(sl + 1) + 2;
         for (int q = 5; q < 8 && e == cudaSuccess; q++)
-          e = copy_range(g, sb.rdim, f.sp[q], species_in + q * nc, sb.lo(sl) + 2, sb.lo(sl + 1) + 2,
-                         cudaMemcpyHostToDevice, h->io_stream);
+          e = copy_range(g, sb.rdim, f.sp[q], species_in + q * nc, lo, hi, cudaMemcpyHostToDevice, h->io_stream);
         if (e == cudaSuccess) e = cudaEventRecord(h->ev_late[sl], h->io_stream);
-      }
-      for (int q = 5; q < 8 && e == cudaSuccess; q++) {
-        e = copy_range(g, sb.rdim, f.sp[q], species_in + q * nc, 0, 2, cudaMemcpyHostToDevice, h->io_stream);
-        if (e == cudaSuccess)
-          e = copy_range(g, sb.rdim, f.sp[q], species_in + q * nc, sb.nby + 2, sb.nby + 4, cudaMemcpyHostToDevice,
-                         h->io_stream);
       }
     } else {
       for (int q = 5; q < 8 && e == cudaSuccess; q++)
