@@ -53,6 +53,17 @@ def test_step_host_slabs_every_sweep_order():
     assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
 
 
+def test_step_host_slabbed_copy_in():
+    """With nx*ny a multiple of the time-step screen's 512-cell blocks the
+    chosen form also brings the state in by z slabs, CC(4) and the screen
+    running on each slab as it arrives: 13 planes in eight slabs of one or
+    two planes, six steps (every sweep order)."""
+    st = _random_box((32, 16, 13))
+    Ur, Sr, U, S = run_both(st, native.PREC_FP32, 6)
+    assert np.array_equal(Ur.view(np.int64), U.view(np.int64))
+    assert np.array_equal(Sr.view(np.int64), S.view(np.int64))
+
+
 def test_step_host_slabs_inflow():
     """Slabbed copies with BC=4 inflow on both x sides (the slab exchanges
     apply the inflow rules of rho and the species), chosen form."""
