@@ -61,8 +61,12 @@ constexpr int kSweepFixedStride = MHD_SWEEP_FIXED_STRIDE;
 #define MHD_SWEEP_LONG_THREADS 768
 #endif
 constexpr int kSweepLongStride = MHD_SWEEP_LONG_STRIDE;
+// 768 threads (three rounds of the 2048-2064 items of a phase; up to 85
+// registers, so the field-finish phase loads its species with rho and v):
+// 2.28 -> 2.21 ms at 256^3 against 1024 threads (two rounds and a third
+// of 8-16 items for the phases over n+1 or n+2 positions)
 #ifndef MHD_SWEEP_Z_THREADS
-#define MHD_SWEEP_Z_THREADS 1024
+#define MHD_SWEEP_Z_THREADS 768
 #endif
 constexpr int kSweepZThreads = MHD_SWEEP_Z_THREADS;
 #ifndef MHD_SWEEP_Z_PENCILS
@@ -161,7 +165,7 @@ static cudaError_t launch32_d(const SweepArgs &a, const double *block, int narr,
   // the x sweep needs P to divide ny; the y and z sweeps pad their groups
   const int nb = (DIR == 0) ? a.g.n[1] : 4;
   const int L = a.g.n[DIR] + 4;
-  // the z sweep: eight x columns per CTA, one 1024-thread CTA per SM.  Its
+  // the z sweep: eight x columns per CTA, one CTA per SM (kSweepZThreads).  Its
   // pencils cross a 2 MB page every four cells, and wider groups spread the
   // CTAs running at once over fewer pages: 2.68 ms at 256^3 against 2.99
   // with four columns and two CTAs per SM (the y sweep, whose pencils stay
