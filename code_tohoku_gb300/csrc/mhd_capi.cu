@@ -830,6 +830,10 @@ constexpr int kCopySlabsRows = MHD_COPY_SLABS_ROWS;
 #define MHD_FIRST_SWEEP_SLABS 4
 #endif
 constexpr int kFirstSweepSlabs = MHD_FIRST_SWEEP_SLABS;
+// the handle's events: ev_slab[9] (a slab count plus one), ev_late[8], ev_in[9]
+static_assert(kCopySlabs >= 1 && kCopySlabs <= 8 && kCopySlabsRows >= 1 && kCopySlabsRows <= 8 &&
+                  kFirstSweepSlabs >= 1 && kFirstSweepSlabs <= 8,
+              "slab counts are bounded by the handle's event arrays");
 constexpr int kSweepOrders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
 
 // the slabs of a direction-dir sweep: K ranges of its transverse block index
