@@ -12,19 +12,21 @@
 
 namespace mhd {
 // Sweep launch shapes.  The default: two CTAs per SM (the pencil buffers
-// of P = 4 pencils of 256 cells take 92 KB), 384 threads for the x sweep and
-// 576 for the y sweep; the z sweep and pencils longer than 256 cells take
-// the shapes chosen in launch32_d below.  Measured at 256^3 on GB300 with
-// P = 4 and two CTAs per SM (ms per sweep x / y / z): 288 threads 2.91 /
-// 3.57 / 3.70; 384: 2.36 / 2.96 / 3.17; 576: 2.42 / 2.68 / 3.13 (before the
-// compile-time stride and the load changes of the kernel).  More warps per
-// SM hide the shared-memory and global-load latency of the phases; the x
-// sweep's contiguous rows need fewer.  The register budget this leaves (78
-// / 56 per thread) holds the kernel without spills because the global-load
-// phases are not unrolled (see MHD_SWEEP_GLOBAL_UNROLL).  The thread counts
-// can be overridden at build time for experiments.
+// of P = 4 pencils of 256 cells take 92 KB), 512 threads for the x sweep
+// (64 registers; at 256^3 1.69 -> 1.65 ms against 384 threads with 80
+// registers, 1.88 with 448) and 576 for the y sweep (56 registers; 544 and
+// 512 threads measured the same or slower); the z sweep and pencils longer
+// than 256 cells take the shapes chosen in launch32_d below.  First
+// measured at 256^3 on GB300 with P = 4 and two CTAs per SM (ms per sweep x
+// / y / z): 288 threads 2.91 / 3.57 / 3.70; 384: 2.36 / 2.96 / 3.17; 576:
+// 2.42 / 2.68 / 3.13 (before the compile-time stride and the load changes
+// of the kernel).  More warps per SM hide the shared-memory and global-load
+// latency of the phases.  The register budget this leaves (64 / 56 per
+// thread) holds the kernel without spills because the global-load phases
+// are not unrolled (see MHD_SWEEP_GLOBAL_UNROLL).  The thread counts can be
+// overridden at build time for experiments.
 #ifndef MHD_SWEEP_THREADS_X
-#define MHD_SWEEP_THREADS_X 384
+#define MHD_SWEEP_THREADS_X 512
 #endif
 #ifndef MHD_SWEEP_THREADS_YZ
 #define MHD_SWEEP_THREADS_YZ 576

@@ -136,10 +136,10 @@ constexpr int kMergeLoads = MHD_SWEEP_MERGE_LOADS;
 constexpr int kHoistLoads = MHD_SWEEP_HOIST_LOADS;
 // Bit d set: the field-finish phase of the direction-d sweep also loads its
 // eight species with rho and v; clear: in one batch after the field finish
-// (the y sweep runs at 56 registers, where twelve FP64 values held at once
-// spill; x and z have the room).
+// (the x and y sweeps run at 64 and 56 registers, where twelve FP64 values
+// held at once spill; the z sweep, one 768-thread CTA per SM, has the room).
 #ifndef MHD_SWEEP_HOIST_SPECIES
-#define MHD_SWEEP_HOIST_SPECIES 5
+#define MHD_SWEEP_HOIST_SPECIES 4
 #endif
 constexpr int kHoistSpecies = MHD_SWEEP_HOIST_SPECIES;
 
