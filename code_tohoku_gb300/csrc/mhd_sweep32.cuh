@@ -119,9 +119,12 @@ constexpr int kSmemUnroll = MHD_SWEEP_SMEM_UNROLL;
 #endif
 constexpr int kGlobalUnroll = MHD_SWEEP_GLOBAL_UNROLL;
 // Bit d set: the load phase of the direction-d sweep issues all loads of a
-// position in one pass; clear: one pass per field group.
+// position in one pass, in kernels with at least 64 registers a thread
+// (NT * MINB <= 1024; the one pass holds 14 FP64 values) and a compile-time
+// buffer stride; clear, or otherwise: one pass per field group.  The z sweep with 768 threads and
+// one CTA per SM: 2.21 -> 2.17 ms at 256^3 with the one pass.
 #ifndef MHD_SWEEP_MERGE_LOADS
-#define MHD_SWEEP_MERGE_LOADS 1
+#define MHD_SWEEP_MERGE_LOADS 5
 #endif
 constexpr int kMergeLoads = MHD_SWEEP_MERGE_LOADS;
 // Bit d set: the finishing phases of the direction-d sweep load every FP64
@@ -129,13 +132,15 @@ constexpr int kMergeLoads = MHD_SWEEP_MERGE_LOADS;
 // Measured at 256^3 (ms, x / y / z): hoisted 2.16 / 2.41 / 2.61, in place
 // 2.23 / 2.47 / 2.68 (the z sweep with eight columns per CTA; with four and
 // two CTAs per SM it was the other way round, 3.21 hoisted against 3.01).
-// Merging the load pass (kMergeLoads) helps the x sweep only (z: 2.69).
+// (Merging the load pass did not help the z sweep of 1024 threads and 64
+// registers: 2.69.)
 #ifndef MHD_SWEEP_HOIST_LOADS
 #define MHD_SWEEP_HOIST_LOADS 7
 #endif
 constexpr int kHoistLoads = MHD_SWEEP_HOIST_LOADS;
 // Bit d set: the field-finish phase of the direction-d sweep also loads its
-// eight species with rho and v; clear: in one batch after the field finish
+// eight species with rho and v (with the register and stride conditions of
+// kMergeLoads); clear: in one batch after the field finish
 // (the x and y sweeps run at 64 and 56 registers, where twelve FP64 values
 // held at once spill; the z sweep, one 768-thread CTA per SM, has the room).
 #ifndef MHD_SWEEP_HOIST_SPECIES
@@ -488,7 +493,7 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __
       Fb(F_SW, i, p) = d2f(st(3, i, p));
       if (edge(i)) load_ghosts(i, p, bn);
     }
-  } else if ((kMergeLoads >> DIR) & 1) {
+  } else if constexpr (((kMergeLoads >> DIR) & 1) != 0 && NT * MINB <= 1024 && LS > 0) {
     // one pass over the interior cells: the transverse field and the state,
     // all loads of a position issued together so that a thread waits for
     // memory once per position rather than once per field group
@@ -738,7 +743,8 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(SweepArgs A, const __
     const double *src[12] = {A.f.U[0],  A.f.U[1 + DIR], A.f.U[1 + C1], A.f.U[1 + C2],
                              A.f.sp[0], A.f.sp[1],      A.f.sp[2],     A.f.sp[3],
                              A.f.sp[4], A.f.sp[5],      A.f.sp[6],     A.f.sp[7]};
-    constexpr bool hoist = ((kHoistLoads >> DIR) & 1) != 0, hoist_sp = ((kHoistSpecies >> DIR) & 1) != 0;
+    constexpr bool hoist = ((kHoistLoads >> DIR) & 1) != 0;
+    constexpr bool hoist_sp = ((kHoistSpecies >> DIR) & 1) != 0 && NT * MINB <= 1024 && LS > 0;
     double pre[12];
     if constexpr (hoist) {
 #pragma unroll
