@@ -85,8 +85,9 @@ constexpr int kSweepZPencils = MHD_SWEEP_Z_PENCILS;
 // multiple of 16 bytes) and every input array inside the state allocation.
 // Measured at 256^3 (ms, per-thread loads -> TMA): y 2.07 -> 1.99 with two
 // CTAs per SM, whose load and compute phases overlap; z 2.26 -> 2.36 with
-// its one CTA per SM, where the three staging rounds are exposed.  So the y
-// sweep only, by default.
+// its one CTA per SM, where the three staging rounds are exposed; x 1.65 ->
+// 1.80 (its one-pass loads of contiguous rows already hit L1 for 46 % of
+// their sectors).  So the y sweep only, by default.
 #ifndef MHD_SWEEP_TMA
 #define MHD_SWEEP_TMA 2
 #endif
