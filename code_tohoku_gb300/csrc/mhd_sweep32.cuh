@@ -122,9 +122,10 @@ constexpr int kGlobalUnroll = MHD_SWEEP_GLOBAL_UNROLL;
 // position in one pass, in kernels with at least 64 registers a thread
 // (NT * MINB <= 1024; the one pass holds 14 FP64 values) and a compile-time
 // buffer stride; clear, or otherwise: one pass per field group.  The z sweep with 768 threads and
-// one CTA per SM: 2.21 -> 2.17 ms at 256^3 with the one pass.
+// one CTA per SM: 2.21 -> 2.17 ms at 256^3 with the one pass; the 512^3 y
+// sweep (768 threads, one CTA per SM) 19.46 -> 19.29 ms.
 #ifndef MHD_SWEEP_MERGE_LOADS
-#define MHD_SWEEP_MERGE_LOADS 5
+#define MHD_SWEEP_MERGE_LOADS 7
 #endif
 constexpr int kMergeLoads = MHD_SWEEP_MERGE_LOADS;
 // Bit d set: the finishing phases of the direction-d sweep load every FP64
@@ -141,10 +142,11 @@ constexpr int kHoistLoads = MHD_SWEEP_HOIST_LOADS;
 // Bit d set: the field-finish phase of the direction-d sweep also loads its
 // eight species with rho and v (with the register and stride conditions of
 // kMergeLoads); clear: in one batch after the field finish
-// (the x and y sweeps run at 64 and 56 registers, where twelve FP64 values
-// held at once spill; the z sweep, one 768-thread CTA per SM, has the room).
+// (the x sweep runs at 64 registers, where twelve FP64 values held at once
+// spill; the z sweep and the 512^3 y sweep, one 768-thread CTA per SM, have
+// the room).
 #ifndef MHD_SWEEP_HOIST_SPECIES
-#define MHD_SWEEP_HOIST_SPECIES 4
+#define MHD_SWEEP_HOIST_SPECIES 6
 #endif
 constexpr int kHoistSpecies = MHD_SWEEP_HOIST_SPECIES;
 

@@ -45,13 +45,13 @@ def test_fp32_mass_conserved_and_divb():
     assert d1["divb_max"] <= 1e-11
 
 
-# (260, 8, 8) and (8, 8, 300): pencils longer than 256 cells take the sweep
-# kernel with the run-time buffer stride, as the 512^3 grid does.  An even
+# (260, 8, 8), (8, 300, 8) and (8, 8, 300): pencils longer than 256 cells
+# take the sweep kernels of the 512^3 grid (a second compile-time stride).  An even
 # nx stages the y sweep's inputs with TMA boxes of 132 positions (one box
 # per pencil group; two for (10, 150, 6), whose second box ends beyond the
 # grid); an odd nx keeps the per-thread loads.
 @pytest.mark.parametrize("shape", [(12, 10, 8), (9, 7, 11), (18, 13, 6), (20, 12, 16), (10, 150, 6), (260, 8, 8),
-                                   (8, 8, 300)])
+                                   (8, 300, 8), (8, 8, 300)])
 def test_fp32_close_to_oracle_on_any_grid(shape):
     st = _random_box(shape)
     g = native.Mhd3D(st.params, precision=native.PREC_FP32)
