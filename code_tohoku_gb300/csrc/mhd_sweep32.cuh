@@ -132,7 +132,8 @@ constexpr int kMergeLoads = MHD_SWEEP_MERGE_LOADS;
 // value of a position before using any; clear: each value where it is used.
 // Measured at 256^3 (ms, x / y / z): hoisted 2.16 / 2.41 / 2.61, in place
 // 2.23 / 2.47 / 2.68 (the z sweep with eight columns per CTA; with four and
-// two CTAs per SM it was the other way round, 3.21 hoisted against 3.01).
+// two CTAs per SM it was the other way round, 3.21 hoisted against 3.01);
+// with the current shapes x / y hoisted 1.65 / 1.94, in place 1.70 / 2.14.
 // (Merging the load pass did not help the z sweep of 1024 threads and 64
 // registers: 2.69.)
 #ifndef MHD_SWEEP_HOIST_LOADS
