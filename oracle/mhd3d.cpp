@@ -1581,6 +1581,27 @@ double o3d_step(void *h, double tsave, int *st) {
 
 void o3d_destroy(void *h) { delete static_cast<Mhd3D *>(h); }
 
+// The species cooling function and the reaction rates at temperature T for
+// the species, nde, ndtot and columns of padded cell c, with those inputs:
+// out[0] Fcool; out[1..21] zeta, kHrec, kHerec, kH2, kH2ph, kH2dH, kH2de,
+// kCO, kCOph, kCi, kCrec, kCOde, kCOdH, kHie, kHeie, kCie, kHiH, kHeiH, kCiH,
+// kCOdHep, kH2dHep; out[22..29] the 8 species; out[30] nde; out[31] ndtot;
+// out[32..41] the 10 columns (test infrastructure: a second restatement of
+// Fcool and RATES checks these)
+void o3d_chem_probe(void *h, double T, long long c, double *out) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  out[0] = m->FcoolSpecies(T, (size_t)c);
+  const Mhd3D::Rates r = m->RATES(T, (size_t)c);
+  const double k[21] = {r.zeta,  r.kHrec, r.kHerec, r.kH2,  r.kH2ph, r.kH2dH, r.kH2de,
+                        r.kCO,   r.kCOph, r.kCi,    r.kCrec, r.kCOde, r.kCOdH, r.kHie,
+                        r.kHeie, r.kCie,  r.kHiH,   r.kHeiH, r.kCiH,  r.kCOdHep, r.kH2dHep};
+  for (int q = 0; q < 21; q++) out[1 + q] = k[q];
+  for (int s = 0; s < 8; s++) out[22 + s] = m->sp[s][(size_t)c];
+  out[30] = m->nde[(size_t)c];
+  out[31] = m->ndtot[(size_t)c];
+  for (int q = 0; q < 10; q++) out[32 + q] = m->col[q].empty() ? 0.0 : m->col[q][(size_t)c];
+}
+
 // BC=4 inflow data: in = rho_ref, v[2][3], p[2], b[2][3], cm[8] (species
 // slots H,p,H2,He,He+,C,C+,CO); dtf = the DTF reservoir as REAL*4 values in
 // the padded layout of U (DTF(-1..nx+2,-1..ny+2,-1..nz+2)), or NULL for a

@@ -67,6 +67,7 @@ def lib():
         L.o3d_columns.argtypes = [ctypes.c_void_p, _P]
         L.o3d_potential.argtypes = [ctypes.c_void_p, _P]
         L.o3d_gravity_solve.argtypes = [ctypes.c_void_p]
+        L.o3d_chem_probe.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong, _P]
         L.o3d_ki_label.restype = ctypes.c_double
         L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
@@ -154,6 +155,13 @@ class Oracle3D:
         the left and the right), padded layout."""
         out = np.zeros((10,) + self.shape)
         lib().o3d_columns(self.h, _ptr(out))
+        return out
+
+    def chem_probe(self, T, c):
+        """Species Fcool and the 21 RATES at temperature T for padded cell c,
+        with the cell's species, nde, ndtot and columns (see o3d_chem_probe)."""
+        out = np.zeros(42)
+        lib().o3d_chem_probe(self.h, float(T), int(c), _ptr(out))
         return out
 
     def potential(self):
