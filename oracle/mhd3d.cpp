@@ -1588,6 +1588,27 @@ void o3d_destroy(void *h) { delete static_cast<Mhd3D *>(h); }
 // kCOdHep, kH2dHep; out[22..29] the 8 species; out[30] nde; out[31] ndtot;
 // out[32..41] the 10 columns (test infrastructure: a second restatement of
 // Fcool and RATES checks these)
+// The chemistry network of padded cell c over dt (SOURCE's CHEM branch for
+// one cell, at the cell's current pressure): out[0..7] the species before,
+// out[8] nde and out[9] ndtot before, out[10] the pressure, out[11..20] the
+// columns; out[21..28] the species after, out[29] nde, out[30] ndtot and
+// out[31] rho after (test infrastructure, as o3d_chem_probe).  The cell's
+// state in the handle is left as the network leaves it.
+void o3d_chem_cell_probe(void *h, long long c, double dt, double *out) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  const size_t cc = (size_t)c;
+  for (int s = 0; s < 8; s++) out[s] = m->sp[s][cc];
+  out[8] = m->nde[cc];
+  out[9] = m->ndtot[cc];
+  out[10] = m->U[5][cc];
+  for (int q = 0; q < 10; q++) out[11 + q] = m->col[q].empty() ? 0.0 : m->col[q][cc];
+  m->CHEM_cell(cc, dt);
+  for (int s = 0; s < 8; s++) out[21 + s] = m->sp[s][cc];
+  out[29] = m->nde[cc];
+  out[30] = m->ndtot[cc];
+  out[31] = m->U[1][cc];
+}
+
 void o3d_chem_probe(void *h, double T, long long c, double *out) {
   Mhd3D *m = static_cast<Mhd3D *>(h);
   out[0] = m->FcoolSpecies(T, (size_t)c);

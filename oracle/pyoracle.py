@@ -68,6 +68,7 @@ def lib():
         L.o3d_potential.argtypes = [ctypes.c_void_p, _P]
         L.o3d_gravity_solve.argtypes = [ctypes.c_void_p]
         L.o3d_chem_probe.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong, _P]
+        L.o3d_chem_cell_probe.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double, _P]
         L.o3d_ki_label.restype = ctypes.c_double
         L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
@@ -162,6 +163,13 @@ class Oracle3D:
         with the cell's species, nde, ndtot and columns (see o3d_chem_probe)."""
         out = np.zeros(42)
         lib().o3d_chem_probe(self.h, float(T), int(c), _ptr(out))
+        return out
+
+    def chem_cell_probe(self, c, dt):
+        """The chemistry network of padded cell c over dt, with the cell's
+        inputs and results (see o3d_chem_cell_probe)."""
+        out = np.zeros(32)
+        lib().o3d_chem_cell_probe(self.h, int(c), float(dt), _ptr(out))
         return out
 
     def potential(self):

@@ -7,9 +7,13 @@ The oracle evaluates exp, log and real powers with its own deterministic
 routines and NumPy with the C library's, so the two agree to a few ulps per
 operation: rates to 1e-12 relative, Fcool to 1e-12 of the sum of the
 magnitudes of its ten terms (it is a difference of cooling and heating).
-The cells carry SHIELD's columns (ifrad = 2, INITIA's 20 iterations) and
-temperatures from 10 K to 10^5 K, so every branch of fesc, ATN5 and kHrec
-is taken."""
+The cells carry SHIELD's columns (ifrad = 2, INITIA's 20 iterations),
+random molecular, atomic and ionised fractions and temperatures from 10 K
+to 10^5 K, so every branch of fesc, ATN5 and kHrec is taken.  The network
+(SOURCE's CHEM branch, :2580-2770, Omexp :3134-3140) is restated the same
+way, stage by stage, and compared cell by cell after one step; changing a
+stage's rate, a transfer term or an electron density that a stage reads
+makes it fail."""
 import numpy as np
 
 from oracle.pyoracle import Oracle3D
@@ -123,8 +127,7 @@ def rates(T, sp, ne, col):
 
 
 def test_fcool_and_rates_match_an_independent_restatement():
-    st = chem_state(n=10, seed=5)
-    st.params = st.params.replace(ifrad=2)
+    st = mixed_state(5)
     o = Oracle3D(st.params)
     o.upload(st)
     s = 10 + 4   # padded extent
@@ -143,3 +146,147 @@ def test_fcool_and_rates_match_an_independent_restatement():
     assert checked == 44
     # the columns are not trivial: shielding is exercised
     assert np.any(out[32:42] > 0.0)
+
+
+KB = 8.63359                                     # :11
+M_H, M_HE, M_H2 = 1.0, 4.0, 2.0                  # :27
+
+
+def omexp(eps):   # :3134-3140
+    return ((0.5 + fsign(0.5, eps - 1.0e-4)) * (1.0 - np.exp(-eps))
+            + (0.5 - fsign(0.5, eps - 1.0e-4))
+            * (eps - 0.5 * eps ** 2 + 0.16666666666666667 * eps ** 3 - 4.16666666666666667e-2 * eps ** 4))
+
+
+def chem_network(sp, ne, nt, pres, col, dt, rmin):
+    """SOURCE's CHEM branch for one cell (:2580-2770), stage by stage."""
+    H, p, H2, He, Hep, C, Cp, CO = (float(v) for v in sp)
+    T = pres / KB / (p + H + H2 + He + Hep)
+    (zeta, kHrec, kHerec, kH2, kH2ph, kH2dH, kH2de, kCO, kCOph, kCi, kCrec, kCOde, kCOdH, kHie, kHeie, kCie,
+     kHiH, kHeiH, kCiH, kCOdHep, kH2dHep) = rates(T, sp, ne, col)
+    # H recombination and ionization by cosmic rays
+    a = kHrec * ne
+    e, r, om = np.exp(-dt * (zeta + a)), 1.0 / (zeta + a), omexp(dt * (zeta + a))
+    H, p = (a * H + zeta * H * e + a * p * om) * r, (zeta * p + a * p * e + zeta * H * om) * r
+    ne = p + Hep + Cp
+    # He recombination and ionization by cosmic rays
+    a = kHerec * ne
+    e, r, om = np.exp(-dt * (zeta + a)), 1.0 / (zeta + a), omexp(dt * (zeta + a))
+    He, Hep = (a * He + zeta * He * e + a * Hep * om) * r, (zeta * Hep + a * Hep * e + zeta * He * om) * r
+    ne = p + Hep + Cp
+    # H2 formation, UV and electron dissociation
+    a = kH2ph + kH2de * ne
+    b = a + 2.0 * kH2 * nt
+    e, om = np.exp(-dt * b), omexp(dt * b)
+    H, H2 = (((H + 2.0 * H2 * om) * a + 2.0 * kH2 * H * nt * e) / b,
+             ((2.0 * H2 + H * om) * kH2 * nt + a * H2 * e) / b)
+    # H2 dissociation by H collisions
+    a = H + 2.0 * H2
+    e = np.exp(-dt * a * kH2dH)
+    r = 1.0 / (H + 2.0 * H2 * e)
+    H, H2 = H * a * r, H2 * a * e * r
+    # CO formation
+    e, om = np.exp(-dt * kCO * nt), omexp(dt * kCO * nt)
+    CO, Cp = CO + om * Cp, e * Cp
+    ne = p + Hep + Cp
+    # CO dissociation by UV, electrons and H
+    q = dt * (kCOph + kCOde * ne + kCOdH * H)
+    e, om = np.exp(-q), omexp(q)
+    C, CO = C + om * CO, e * CO
+    # C recombination and ionization by cosmic rays and UV
+    a = kCrec * ne
+    e, r, om = np.exp(-dt * (kCi + a)), 1.0 / (kCi + a), omexp(dt * (kCi + a))
+    C, Cp = (a * C + kCi * C * e + a * Cp * om) * r, (kCi * Cp + a * Cp * e + kCi * C * om) * r
+    ne = p + Hep + Cp
+    # H, He, C ionization by electrons
+    H_, He_, C_ = H * np.exp(-dt * kHie * ne), He * np.exp(-dt * kHeie * ne), C * np.exp(-dt * kCie * ne)
+    p, Hep, Cp = omexp(dt * kHie * ne) * H + p, omexp(dt * kHeie * ne) * He + Hep, omexp(dt * kCie * ne) * C + Cp
+    H, He, C = H_, He_, C_
+    ne = p + Hep + Cp
+    # H, He, C ionization by H, H2 and p collisions
+    r = 1.0 / (1.0 + kHiH * dt * H)
+    H, p = H * r, p + r * kHiH * dt * H ** 2
+    q = H + p + H2
+    He_, C_ = He * np.exp(-dt * kHeiH * q), C * np.exp(-dt * kCiH * q)
+    Hep, Cp = omexp(dt * kHeiH * q) * He + Hep, omexp(dt * kCiH * q) * C + Cp
+    He, C = He_, C_
+    ne = p + Hep + Cp
+    # H2 dissociation by He+ recombination
+    a = Hep - H2
+    if a >= 0.0:
+        e = np.exp(-dt * kH2dHep * a)
+        r = 1.0 / (Hep - H2 * e)
+        Hep_, H2 = Hep * a * r, H2 * a * r * e
+        d = Hep * (1.0 - a * r)
+    else:
+        e = np.exp(dt * kH2dHep * a)
+        r = 1.0 / (Hep * e - H2)
+        Hep_, H2 = Hep * a * r * e, H2 * a * r
+        d = Hep * (1.0 - a * r * e)
+    Hep, p, H, He = Hep_, p + d, H + d, He + d
+    # CO dissociation by He+ recombination
+    a = Hep - CO
+    if a >= 0.0:
+        e = np.exp(-dt * kCOdHep * a)
+        r = 1.0 / (Hep - CO * e)
+        Hep_, CO = Hep * a * r, CO * a * r * e
+        d = Hep * (1.0 - a * r)
+    else:
+        e = np.exp(dt * kCOdHep * a)
+        r = 1.0 / (Hep * e - CO)
+        Hep_, CO = Hep * a * r * e, CO * a * r
+        d = Hep * (1.0 - a * r * e)
+    Hep, Cp, He = Hep_, Cp + d, He + d
+    # floors (:178-179), then nde, ndtot and rho
+    floors = (0.91 * rmin, 1e-20, 1e-20, 0.09 * rmin, 1e-20, 1e-20, 1e-20, 1e-20)
+    out = [max(f, v) for f, v in zip(floors, (H, p, H2, He, Hep, C, Cp, CO))]
+    H, p, H2, He, Hep, C, Cp, CO = out
+    ne = p + Hep + Cp
+    nt = p + H + 2.0 * H2 + He + Hep
+    rho = M_H * p + M_H * H + M_H2 * H2 + M_HE * He + M_HE * Hep
+    return np.array(out), ne, nt, rho
+
+
+def mixed_state(seed):
+    """The chemistry workload with every composition the network acts on:
+    in each cell random fractions of the H nuclei in H2 and of the C nuclei
+    in CO and C (the rest ionised or atomic), and temperatures from cold
+    molecular to warm ionised gas."""
+    st = chem_state(n=10, seed=seed)
+    st.params = st.params.replace(ifrad=2)
+    rng = np.random.default_rng(seed + 100)
+    sp = st.species
+    shape = sp[0].shape
+    hn, hen, cn = sp[0] + sp[1] + 2 * sp[2], sp[3] + sp[4], sp[5] + sp[6] + sp[7]
+    fh2, fp = rng.uniform(0.0, 0.45, shape), 10.0 ** rng.uniform(-4.0, -0.5, shape)
+    sp[2] = fh2 * hn
+    sp[1] = fp * (hn - 2 * sp[2])
+    sp[0] = hn - 2 * sp[2] - sp[1]
+    fhep = 10.0 ** rng.uniform(-4.0, -0.5, shape)
+    sp[4], sp[3] = fhep * hen, (1 - fhep) * hen
+    fco, fc = rng.uniform(0.0, 0.9, shape), rng.uniform(0.0, 0.5, shape)
+    sp[7] = fco * cn
+    sp[5] = fc * (cn - sp[7])
+    sp[6] = cn - sp[7] - sp[5]
+    st.U[4] *= 10.0 ** rng.uniform(-1.5, 0.5, shape)
+    return st
+
+
+def test_chemistry_network_matches_an_independent_restatement():
+    st = mixed_state(7)
+    o = Oracle3D(st.params)
+    o.upload(st)
+    s = 10 + 4
+    rng = np.random.default_rng(13)
+    for q in range(60):
+        i, j, k = (int(v) for v in rng.integers(2, 12, size=3))
+        dt = 10.0 ** rng.uniform(-4.0, 0.0)
+        out = o.chem_cell_probe(i + s * (j + s * k), dt)
+        sp, ne, nt, pres, col = out[0:8], out[8], out[9], out[10], out[11:21]
+        sp1, ne1, nt1, rho1 = chem_network(sp, ne, nt, pres, col, dt, st.params.rmin)
+        # each species against its element's total: a stage moves nuclei
+        # between species, so absolute agreement is relative to the element
+        tot = np.array([sp[0] + sp[1] + 2 * sp[2]] * 3 + [sp[3] + sp[4]] * 2 + [sp[5] + sp[6] + sp[7]] * 3)
+        np.testing.assert_allclose(out[21:29], sp1, rtol=1e-11, atol=1e-12 * tot.max())
+        np.testing.assert_allclose(out[21:29] / tot, sp1 / tot, rtol=0.0, atol=1e-11)
+        np.testing.assert_allclose([out[29], out[30], out[31]], [ne1, nt1, rho1], rtol=1e-11)
