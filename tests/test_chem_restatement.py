@@ -290,3 +290,55 @@ def test_chemistry_network_matches_an_independent_restatement():
         np.testing.assert_allclose(out[21:29], sp1, rtol=1e-11, atol=1e-12 * tot.max())
         np.testing.assert_allclose(out[21:29] / tot, sp1 / tot, rtol=0.0, atol=1e-11)
         np.testing.assert_allclose([out[29], out[30], out[31]], [ne1, nt1, rho1], rtol=1e-11)
+
+
+def shield_pass(U, sp, col_old, dx1, n):
+    """SHIELD (:2924-3036) on one block holding every line whole: the C+
+    optical-depth source of each interior cell from the previous tCII
+    columns, then along each x line the columns from the left and from the
+    right, each cell adding half its width times its value before and after
+    its own column is stored.  nde and ndtot are rebuilt from the species
+    first, as SOURCE does before calling SHIELD (:2460-2463)."""
+    nx, ny, nz = n
+    H, p, H2, He, Hep, C, Cp, CO = sp
+    nde = p + Hep + Cp
+    ndtot = p + H + 2.0 * H2 + He + Hep
+    dxh = 0.5 * dx1
+    out = np.zeros_like(col_old)
+    for k in range(2, nz + 2):
+        for j in range(2, ny + 2):
+            src = np.zeros(nx + 4)
+            for i in range(2, nx + 2):
+                b21 = fesc(col_old[8][k, j, i]) + fesc(col_old[9][k, j, i])
+                T = U[4][k, j, i] / (KB * (p[k, j, i] + H[k, j, i] + H2[k, j, i] + He[k, j, i] + Hep[k, j, i]))
+                n1, n2 = levc2(T, b21, H[k, j, i], H2[k, j, i], nde[k, j, i], Cp[k, j, i])
+                src[i] = 1.15563e1 * (n1 - n2) * (1.0 / DV)
+            vals = (ndtot[k, j], H2[k, j], C[k, j], CO[k, j], src)
+            for side, rng_i in ((0, range(2, nx + 2)), (1, range(nx + 1, 1, -1))):
+                acc = [0.0] * 5
+                for i in rng_i:
+                    for q in range(5):
+                        acc[q] += dxh * vals[q][i]
+                        out[2 * q + side][k, j, i] = acc[q]
+                        acc[q] += dxh * vals[q][i]
+    return out
+
+
+def test_shield_pass_matches_an_independent_restatement():
+    """One SHIELD pass (the one at the start of SOURCE) against its
+    restatement, from the columns INITIA's twenty passes left; the column
+    order of the handle is Ntot, NH2, NnC, NCO, tCII, each from the left
+    and from the right."""
+    st = mixed_state(9)
+    o = Oracle3D(st.params)
+    o.upload(st)
+    col0 = o.columns()
+    U0, sp0, _ = o.download()
+    o.source(1.0e-6)
+    col1 = o.columns()
+    n = (st.params.nx, st.params.ny, st.params.nz)
+    ref = shield_pass(U0, sp0, col0, st.dx[2], n)
+    inner = (slice(None), slice(2, -2), slice(2, -2), slice(2, -2))
+    got, want = col1[inner], ref[inner]
+    assert np.all(want[:8] > 0.0) and np.any(want[8:] != 0.0)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-300)
