@@ -1623,6 +1623,23 @@ void o3d_chem_probe(void *h, double T, long long c, double *out) {
   for (int q = 0; q < 10; q++) out[32 + q] = m->col[q].empty() ? 0.0 : m->col[q][(size_t)c];
 }
 
+// Constrained transport of the handle's state with its intermediates (test
+// infrastructure, as o3d_chem_probe): CC(1), CCT for the three edges and
+// CC(3).  out holds 17 padded arrays: U(1..8) as CCT read them (after the
+// exchanges of CC(1) and of CC(2)'s density), Vfc(1..3), EMF(1..3), then
+// U(6..8) after CC(3).
+void o3d_ct_probe(void *h, double dt, double *out) {
+  Mhd3D *m = static_cast<Mhd3D *>(h);
+  const size_t n = m->ncell;
+  m->CC1();
+  for (int e = 0; e < 3; e++) m->CCT(e, dt);
+  for (int f = 1; f <= 8; f++) memcpy(out + (f - 1) * n, m->U[f].data(), n * sizeof(double));
+  for (int c = 1; c <= 3; c++) memcpy(out + (7 + c) * n, m->Vfc[c].data(), n * sizeof(double));
+  for (int c = 1; c <= 3; c++) memcpy(out + (10 + c) * n, m->EMF[c].data(), n * sizeof(double));
+  m->CC3(dt);
+  for (int f = 6; f <= 8; f++) memcpy(out + (8 + f) * n, m->U[f].data(), n * sizeof(double));
+}
+
 // BC=4 inflow data: in = rho_ref, v[2][3], p[2], b[2][3], cm[8] (species
 // slots H,p,H2,He,He+,C,C+,CO); dtf = the DTF reservoir as REAL*4 values in
 // the padded layout of U (DTF(-1..nx+2,-1..ny+2,-1..nz+2)), or NULL for a

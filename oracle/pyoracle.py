@@ -69,6 +69,7 @@ def lib():
         L.o3d_gravity_solve.argtypes = [ctypes.c_void_p]
         L.o3d_chem_probe.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong, _P]
         L.o3d_chem_cell_probe.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double, _P]
+        L.o3d_ct_probe.argtypes = [ctypes.c_void_p, ctypes.c_double, _P]
         L.o3d_ki_label.restype = ctypes.c_double
         L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
@@ -171,6 +172,14 @@ class Oracle3D:
         out = np.zeros(32)
         lib().o3d_chem_cell_probe(self.h, int(c), float(dt), _ptr(out))
         return out
+
+    def ct_probe(self, dt):
+        """Constrained transport over dt with its intermediates (see
+        o3d_ct_probe): U(1..8) as CCT read them, Vfc(1..3), EMF(1..3) and
+        U(6..8) after the face update, each padded."""
+        out = np.zeros((17,) + self.shape)
+        lib().o3d_ct_probe(self.h, float(dt), _ptr(out))
+        return out[0:8], out[8:11], out[11:14], out[14:17]
 
     def potential(self):
         """Phi (self-gravity, ifgrv = 2) in the padded layout."""
