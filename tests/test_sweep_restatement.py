@@ -1,0 +1,354 @@
+"""One dimensionally split sweep, MHD (3DMHD-CfCA/MCF3DSGincfca3.f90:
+1264-1324), restated in NumPy from the Fortran and checked against the
+oracle's C++ bit for bit on every padded array it leaves behind:
+
+* the two-layer exchanges along the sweep before each phase (BC_MPI and
+  BC_MPI_OT at :1355, :1357, :1960, :1974, :1572, :1581, :1594): a periodic
+  image, then the free-boundary copy of the edge cell where bc = 1 — for the
+  species only on rows whose transverse indices are interior;
+* RHS (:1330-1467): VLIMIT slopes (:1692-1804) with the T < 3 switch to
+  minmod, the domain-of-dependence offsets, the positivity masks, the
+  interface adiabatic index from the mean species, the Lagrangian Riemann
+  solver (RIEMAN, :1474-1551, four fixed iterations) and the Lagrangian
+  update of density, normal momentum, energy, the transverse field and the
+  species;
+* MOC (:1939-2098): the face-normal field interpolated to the moved
+  interfaces, the upwinded characteristic states by the sign of B_n,
+  CHAREQ (:2101-2111) and the transverse momentum, energy and field update;
+* REMAP (:1556-1686): upwind fluxes of fifteen columns (U1-U5, the two
+  Lagrangian fields, the eight species) back onto the Eulerian grid;
+* the primitive conversion with the density, pressure and species floors
+  (:1291-1321).
+
+The slopes read T = 1.27 U5 / (kb U1) from whatever U5 holds in each phase
+(pressure in RHS, specific energy in MOC, energy density in REMAP), as the
+reference does.  Each direction is worked in its own frame (sweep, M, L) =
+(x, y, z), (y, z, x), (z, x, y), like the reference's index maps
+(:1370-1372).  The oracle supplies the cell-centred field of CC(4) only."""
+import numpy as np
+import pytest
+
+from code_tohoku_gb300 import problems
+from oracle.pyoracle import Oracle3D
+
+EPS = 1e-10
+
+
+def sgn(a, b):
+    return np.copysign(np.abs(a), b)
+
+
+def fmax2(a, b):
+    return np.where(b > a, b, a)
+
+
+def fmin2(a, b):
+    return np.where(b < a, b, a)
+
+
+def local(A, d):
+    """Array [z, y, x] in the frame of sweep d: axes (sweep, M, L)."""
+    return np.transpose(A, (2 - d, 2 - (d + 1) % 3, 2 - (d + 2) % 3))
+
+
+def exchange(a, N, bc, species=False):
+    """Two ghost layers along axis 0 (padded interior 2..N+1) on every row:
+    periodic images, then the copy of the edge cell on a free (bc = 1) side,
+    for the species only on rows with interior transverse indices."""
+    a[0:2] = a[N:N + 2]
+    a[N + 2:N + 4] = a[2:4]
+    rows = (slice(None), slice(2, a.shape[1] - 2), slice(2, a.shape[2] - 2)) if species else (slice(None),) * 3
+    r = a[rows]
+    if bc[0] == 1:
+        r[0] = r[2]
+        r[1] = r[2]
+    if bc[1] == 1:
+        r[N + 2] = r[N + 1]
+        r[N + 3] = r[N + 1]
+
+
+def slope(q, u1, u5, dxx, kb, N):
+    """VLIMIT along axis 0 for i = 0..N+1, returned at padded index i+1
+    (zeros elsewhere); dxx broadcasts against q (padded along axis 0)."""
+    lo, hi = 1, N + 3
+    qp, q0, qm = q[lo + 1:hi + 1], q[lo:hi], q[lo - 1:hi - 1]
+    d0, dm, dp = dxx[lo:hi], dxx[lo - 1:hi - 1], dxx[lo + 1:hi + 1]
+    delp = qp - q0
+    delm = q0 - qm
+    flmt = fmax2(0.0, (2.0 * delp * delm + EPS) / (delp * delp + delm * delm + EPS))
+    g = flmt * (qp - qm) / (d0 + 0.5 * dm + 0.5 * dp)
+    T = 1.27 * u5[lo:hi] / (kb * u1[lo:hi])
+    delp = 2.0 * delp / (d0 + dp)
+    delm = 2.0 * delm / (d0 + dm)
+    gmm = (0.5 + sgn(0.5, delp * delm)) * sgn(1.0, delp) * fmin2(np.abs(delp), np.abs(delm))
+    out = np.zeros_like(q)
+    out[lo:hi] = g * (0.5 - sgn(0.5, T - 3.0)) + gmm * (0.5 + sgn(0.5, T - 3.0))
+    return out
+
+
+def posmask(q, fallback):
+    return (0.5 - sgn(0.5, -q)) * q + (0.5 + sgn(0.5, -q)) * fallback
+
+
+def riemann(gam, L, R):
+    """RIEMAN: Lagrangian wave speeds by four fixed-point iterations."""
+    g1, g2, g3, p1, p3 = gam - 1.0, gam - 2.0, gam - 3.0, gam + 1.0, gam + 3.0
+    D1, V1, P1, B1 = L[0], L[1], L[2], 0.5 * L[3]
+    D2, V2, P2, B2 = R[0], R[1], R[2], 0.5 * R[3]
+    P1 = P1 + B1
+    P2 = P2 + B2
+    GP1, GP2 = g1 * P1, g1 * P2
+    GP1B1 = g3 * P1 - g2 * B1 * 2.0
+    GP2B2 = g3 * P2 - g2 * B2 * 2.0
+    Pa = (P1 + P2) * 0.5
+    for _ in range(4):
+        pp1 = p3 * Pa + GP1B1
+        q1 = np.sqrt((pp1 + np.sqrt(pp1 * pp1 - 8.0 * (Pa - P1) * (p1 * Pa + GP1))) * D1) * 0.5
+        pp2 = p3 * Pa + GP2B2
+        q2 = np.sqrt((pp2 + np.sqrt(pp2 * pp2 - 8.0 * (Pa - P2) * (p1 * Pa + GP2))) * D2) * 0.5
+        old = Pa
+        Pa = (q2 * P1 + q1 * P2 + q2 * q1 * (V1 - V2)) / (q2 + q1)
+        Pa = np.where(Pa <= 0.0, 0.1 * old, Pa)
+    Va = (q1 * V1 + q2 * V2 + P1 - P2) / (q2 + q1)
+    return Pa, Va
+
+
+def chareq(QL1, QL2, QL3, QR1, QR2, QR3):
+    sp, sm = np.sqrt(QL3), np.sqrt(QR3)
+    Va = (sp * QL1 + sm * QR1 + QR2 - QL2) / (sp + sm)
+    Ba = (sp * sm * (QR1 - QL1) + sp * QR2 + sm * QL2) / (sp + sm)
+    return Ba, Va
+
+
+def heavy(s):   # H + p + He + He+ and H2, of the slots H, p, H2, He, He+, ...
+    return s[0] + s[1] + s[3] + s[4], s[2]
+
+
+def sweep(d, U, sp, Bcc, coords, p, dt):
+    """MHD for direction d on copies of U (8 padded fields), the species
+    and Bcc; returns the new U and species."""
+    U, sp = U.copy(), sp.copy()
+    n = (p.nx, p.ny, p.nz)
+    N = n[d]
+    bc = (p.bc[2 * d], p.bc[2 * d + 1])
+    xelr, dxelr = coords[2 * d], coords[2 * d + 1]
+    VN = 1 + d
+    BT1, BT2 = ((1, 2), (2, 0), (0, 1))[d]           # Bcc components, 0-based
+    VT1, VT2 = ((2, 3), (3, 1), (1, 2))[d]           # U fields, 0-based
+    BN = 5 + d
+    Ul = [local(U[f], d) for f in range(8)]
+    Sl = [local(sp[s], d) for s in range(8)]
+    Bl = [local(Bcc[c], d) for c in range(3)]
+    M, L = Ul[0].shape[1] - 4, Ul[0].shape[2] - 4
+    pen = (slice(None), slice(2, M + 2), slice(2, L + 2))   # the interior pencils
+    u = lambda f: Ul[f][pen]
+    s_ = lambda s: Sl[s][pen]
+    b_ = lambda c: Bl[c][pen]
+    col = lambda v: v[:, None, None]
+    X = col(xelr)
+    DX = col(dxelr)
+    A = slice(1, N + 2)      # padded index of i = 0..N
+    B = slice(2, N + 3)      # i + 1
+    I = slice(2, N + 2)      # i = 1..N
+    Im = slice(1, N + 1)     # i - 1
+    kb, fac = p.kb, p.facdep
+    with np.errstate(all="ignore"):
+        # ===== RHS
+        for f in (0, VN, 4):
+            exchange(Ul[f], N, bc)
+        for s in range(8):
+            exchange(Sl[s], N, bc, species=True)
+        g1 = slope(u(0), u(0), u(4), DX, kb, N)
+        gVN = slope(u(VN), u(0), u(4), DX, kb, N)
+        g5 = slope(u(4), u(0), u(4), DX, kb, N)
+        gB1 = slope(b_(BT1), u(0), u(4), DX, kb, N)
+        gB2 = slope(b_(BT2), u(0), u(4), DX, kb, N)
+        hv, h2 = heavy([s_(s) for s in range(8)])
+        gam = (5.0 * hv + 7.0 * h2) / (3.0 * hv + 5.0 * h2)
+        cm = np.sqrt((gam * u(4) + b_(BT1) * b_(BT1) + b_(BT2) * b_(BT2)) / u(0))
+        dep1 = fmax2(0.0, 0.5 * (DX[A] - cm[A] * dt) * fac)
+        dep2 = fmax2(0.0, 0.5 * (DX[B] - cm[B] * dt) * fac)
+        QL1 = posmask(u(0)[A] + dep1 * g1[A], u(0)[A])
+        QR1 = posmask(u(0)[B] - dep2 * g1[B], u(0)[B])
+        QL2 = u(VN)[A] + dep1 * gVN[A]
+        QR2 = u(VN)[B] - dep2 * gVN[B]
+        QL3 = posmask(u(4)[A] + dep1 * g5[A], u(4)[A])
+        QR3 = posmask(u(4)[B] - dep2 * g5[B], u(4)[B])
+        l1, l2 = b_(BT1)[A] + dep1 * gB1[A], b_(BT2)[A] + dep1 * gB2[A]
+        r1, r2 = b_(BT1)[B] - dep2 * gB1[B], b_(BT2)[B] - dep2 * gB2[B]
+        QL4, QR4 = l1 * l1 + l2 * l2, r1 * r1 + r2 * r2
+        mean = [0.5 * (s_(s)[A] + s_(s)[B]) for s in range(8)]
+        hm, h2m = mean[0] + mean[1] + mean[3] + mean[4], mean[2]
+        gi = (5.0 * hm + 7.0 * h2m) / (3.0 * hm + 5.0 * h2m)
+        Pa, Va = riemann(gi, (QL1, QL2, QL3, QL4), (QR1, QR2, QR3, QR4))   # i = 0..N at [0..N]
+        xlag = np.broadcast_to(X, u(0).shape).copy()
+        dm = DX[A] * u(0)[A]
+        xlag[A] = xlag[A] + Va * dt
+        dxl = xlag[I] - xlag[Im]
+        g1c = (2.0 * hv[I] + 2.0 * h2[I]) / (3.0 * hv[I] + 5.0 * h2[I])
+        rho = u(0)[I]
+        E = u(4)[I] / (rho * g1c) + 0.5 * (u(1)[I] * u(1)[I] + u(2)[I] * u(2)[I] + u(3)[I] * u(3)[I]) \
+            + 0.5 * (b_(0)[I] * b_(0)[I] + b_(1)[I] * b_(1)[I] + b_(2)[I] * b_(2)[I]) / rho
+        u(0)[I] = dm[1:] / dxl
+        u(VN)[I] = u(VN)[I] - dt / dm[1:] * (Pa[1:] - Pa[:-1])
+        u(4)[I] = E - dt / dm[1:] * (Pa[1:] * Va[1:] - Pa[:-1] * Va[:-1])
+        Blg = [np.zeros_like(xlag), np.zeros_like(xlag)]
+        Blg[0][I] = b_(BT1)[I] * DX[I] / dxl
+        Blg[1][I] = b_(BT2)[I] * DX[I] / dxl
+        for s in range(8):
+            s_(s)[I] = DX[I] * s_(s)[I] / dxl
+        Vfc = np.zeros_like(xlag)
+        Vfc[2:N + 3] = Va                                   # Vfc(i) = Va(i-1), i = 1..N+1
+
+        # ===== MOC
+        for f in (0, VT1, VT2, BN):
+            exchange(Ul[f], N, bc)
+        dxlag = np.zeros_like(xlag)
+        dxlag[I] = xlag[I] - xlag[Im]
+        for a in (dxlag, Blg[0], Blg[1]):
+            exchange(a, N, bc)
+        gm1 = slope(u(0), u(0), u(4), dxlag, kb, N)
+        gT1 = slope(u(VT1), u(0), u(4), dxlag, kb, N)
+        gT2 = slope(u(VT2), u(0), u(4), dxlag, kb, N)
+        gL1 = slope(Blg[0], u(0), u(4), dxlag, kb, N)
+        gL2 = slope(Blg[1], u(0), u(4), dxlag, kb, N)
+        C = slice(3, N + 4)      # i + 2
+        bn = u(BN)
+        Bnap = bn[B] + (xlag[A] - X[A]) * (bn[C] - bn[A]) / (X[B] - X[0:N + 1])
+        deni = np.sqrt((dxlag[A] + dxlag[B]) / (dxlag[A] * u(0)[B] + dxlag[B] * u(0)[A]))
+        pos = Bnap > 0.0
+        ca = np.abs(Bnap * deni) * 0.5 * dt
+        dA, dB = dxlag[A], dxlag[B]
+        # Bn > 0: depend1 from cell i, depend2 from cell i+1; else swapped
+        dep1 = np.where(pos, (0.5 * dA - fmin2(dA, ca)) * fac, (0.5 * dB - fmin2(dB, ca)) * fac)
+        dep2 = np.where(pos, (0.5 * dB - fmin2(dB, ca)) * fac, (0.5 * dA - fmin2(dA, ca)) * fac)
+
+        def upwind(q, g):
+            ql = np.where(pos, q[A] + dep1 * g[A], q[B] - dep1 * g[B])
+            qr = np.where(pos, q[B] - dep2 * g[B], q[A] + dep2 * g[A])
+            return ql, qr
+
+        QL11, QR11 = upwind(u(VT1), gT1)
+        QL12, QR12 = upwind(Blg[0], gL1)
+        QL21, QR21 = upwind(u(VT2), gT2)
+        QL22, QR22 = upwind(Blg[1], gL2)
+        ql, qr = upwind(u(0), gm1)
+        QL13 = posmask(ql, np.where(pos, u(0)[A], u(0)[B]))
+        QR13 = posmask(qr, np.where(pos, u(0)[B], u(0)[A]))
+        Bay, Vay = chareq(QL11, QL12, QL13, QR11, QR12, QR13)
+        Baz, Vaz = chareq(QL21, QL22, QL13, QR21, QR22, QR13)
+        bp = Bnap[1:]                                         # i = 1..N
+        bm = bn[I] + (xlag[Im] - X[Im]) * (bn[3:N + 3] - bn[Im]) / (X[I] - X[0:N])
+        vp, vm = Vfc[3:N + 3], Vfc[I]
+        DL = dxlag[I]
+        rho = u(0)[I]
+        u(VN)[I] = u(VN)[I] * rho + dt / DL * 0.5 * (bp * bp - bm * bm)
+        u(VT1)[I] = u(VT1)[I] * rho + dt / DL * (bp * Bay[1:] - bm * Bay[:-1])
+        u(VT2)[I] = u(VT2)[I] * rho + dt / DL * (bp * Baz[1:] - bm * Baz[:-1])
+        u(4)[I] = u(4)[I] * rho + dt / DL * ((0.5 * bp * vp + Bay[1:] * Vay[1:] + Baz[1:] * Vaz[1:]) * bp
+                                             - (0.5 * bm * vm + Bay[:-1] * Vay[:-1] + Baz[:-1] * Vaz[:-1]) * bm)
+        Blg[0][I] = Blg[0][I] + dt / DL * (bp * Vay[1:] - bm * Vay[:-1])
+        Blg[1][I] = Blg[1][I] + dt / DL * (bp * Vaz[1:] - bm * Vaz[:-1])
+
+        # ===== REMAP
+        for a in Blg:
+            exchange(a, N, bc)
+        for f in range(5):
+            exchange(Ul[f], N, bc)
+        for s in range(8):
+            exchange(Sl[s], N, bc, species=True)
+        cols = [u(f) for f in range(5)] + Blg + [s_(s) for s in range(8)]
+        grd = [slope(q, u(0), u(4), dxlag, kb, N) for q in cols]
+        vadt = Vfc[B] * dt
+        neg = vadt <= 0.0
+        depn = 0.5 * (dxlag[B] + vadt) * fac
+        depp = 0.5 * (dxlag[A] - vadt) * fac
+        F = [np.where(neg, -vadt * (q[B] - depn * g[B]), -vadt * (q[A] + depp * g[A])) for q, g in zip(cols, grd)]
+        for q, f in zip(cols, F):
+            q[I] = (q[I] * dxlag[I] + f[1:] - f[:-1]) / (X[I] - X[Im])
+
+        # ===== primitive variables and floors, interior cells
+        K = (slice(2, N + 2),) + pen[1:]
+        r = fmax2(1.27 * p.rmin, Ul[0][K])
+        Ul[0][K] = r
+        invd = 1.0 / r
+        for f in (1, 2, 3):
+            Ul[f][K] = Ul[f][K] * invd
+        hv, h2 = heavy([Sl[s][K] for s in range(8)])
+        g1c = (2.0 * hv + 2.0 * h2) / (3.0 * hv + 5.0 * h2)
+        ekin = 0.5 * (Ul[1][K] * Ul[1][K] + Ul[2][K] * Ul[2][K] + Ul[3][K] * Ul[3][K]) * r
+        Bt = Bl[d][K]
+        emag = 0.5 * (Bt * Bt + Blg[0][I] * Blg[0][I] + Blg[1][I] * Blg[1][I])
+        pr = (Ul[4][K] - ekin - emag) * g1c
+        Ul[4][K] = fmin2(p.pmax, fmax2(p.pmin, pr))
+        floors = (p.rmin * 0.91, 1e-20, 1e-20, p.rmin * 0.09, 1e-20, 1e-20, 1e-20, 1e-20)
+        for s in range(8):
+            Sl[s][K] = fmax2(floors[s], Sl[s][K])
+    return U, sp
+
+
+def make_state(n, bc, seed):
+    nx, ny, nz = n
+    p = problems.MhdParams(nx, ny, nz, bc=bc)
+    sh = (nz + 4, ny + 4, nx + 4)
+    rng = np.random.default_rng(seed)
+    axes = []
+    for m, length in zip(n, (20.0, 17.0, 15.0)):
+        dx = np.full(m + 4, length / m) * rng.uniform(0.75, 1.25, m + 4)
+        x = np.empty(m + 4)
+        x[0] = -dx[1]
+        for i in range(1, m + 4):
+            x[i] = x[i - 1] + dx[i]
+        axes += [x, dx]
+    U = np.zeros((8,) + sh)
+    U[0] = problems.MU * np.exp(rng.normal(0.0, 0.7, sh))
+    U[1:4] = rng.normal(0.0, 3.0, (3,) + sh)
+    U[5:8] = rng.normal(0.0, 3.0, (3,) + sh)
+    sp = np.zeros((8,) + sh)
+    frac = rng.uniform(0.0, 0.4, sh)            # molecular fraction varies gamma
+    nH = U[0] / problems.MU
+    sp[0] = 0.91 * nH * (1.0 - frac) * rng.uniform(0.9, 1.0, sh)
+    sp[1] = 0.91 * nH * 0.01 * rng.uniform(0.5, 1.5, sh)
+    sp[2] = 0.5 * 0.91 * nH * frac
+    sp[3] = 0.09 * nH * rng.uniform(0.95, 1.0, sh)
+    sp[4] = 0.09 * nH * 0.006 * rng.uniform(0.5, 1.5, sh)
+    for s, x in ((5, 1e-8), (6, 1.4e-4), (7, 1e-20)):
+        sp[s] = x * nH * rng.uniform(0.5, 1.5, sh)
+    T = rng.uniform(1.0, 6.0, sh)               # both sides of the 3000 K switch
+    U[4] = T * problems.KB * U[0] / 1.27
+    return problems.MhdState(p, U, sp, *axes)
+
+
+CASES = [((10, 9, 8), (1, 1, 3, 3, 3, 3)), ((9, 8, 10), (3, 3, 3, 3, 3, 3)), ((8, 10, 9), (3, 3, 1, 1, 1, 1))]
+
+
+@pytest.mark.parametrize("n,bc", CASES)
+@pytest.mark.parametrize("d", [0, 1, 2])
+def test_sweep_matches_an_independent_restatement(d, n, bc):
+    st = make_state(n, bc, 31 + d)
+    p = st.params
+    o = Oracle3D(p)
+    o.upload(st)
+    U0, sp0, bcc = o.download()
+    # CC(4)'s cell-centred field on the interior
+    nx, ny, nz = n
+    K, J, I = slice(2, nz + 2), slice(2, ny + 2), slice(2, nx + 2)
+    assert np.array_equal(bcc[0][K, J, I], 0.5 * (U0[5][K, J, I] + U0[5][K, J, 3:nx + 3]))
+    c = [np.max(np.sqrt((5.0 / 3.0 * U0[4] + bcc[0] ** 2 + bcc[1] ** 2 + bcc[2] ** 2) / U0[0]))]
+    dt = 0.3 * min(st.dx.min(), st.dy.min(), st.dz.min()) / (np.max(np.abs(U0[1:4])) + c[0])
+    o.sweep(d, dt)
+    U1, sp1, _ = o.download()
+    coords = (st.x, st.dx, st.y, st.dy, st.z, st.dz)
+    U2, sp2 = sweep(d, U0, sp0, bcc, coords, p, dt)
+    assert np.all(np.isfinite(U1)) and np.all(np.isfinite(sp1))
+    for f in range(8):
+        assert np.array_equal(U1[f], U2[f]), f
+    for s in range(8):
+        assert np.array_equal(sp1[s], sp2[s]), s
+    # the sweep moved every field it owns, and the floors and the T switch
+    # both sides were met
+    for f in range(5):
+        assert np.any(U1[f] != U0[f]), f
+    T = 1.27 * U0[4] / (p.kb * U0[0])
+    assert np.any(T < 3.0) and np.any(T > 3.0)
+    assert np.any(U1[4][K, J, I] == p.pmin)
