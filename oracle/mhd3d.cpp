@@ -1623,6 +1623,14 @@ void o3d_chem_probe(void *h, double T, long long c, double *out) {
   for (int q = 0; q < 10; q++) out[32 + q] = m->col[q].empty() ? 0.0 : m->col[q][(size_t)c];
 }
 
+// The oracle's elementary functions over n values (test infrastructure:
+// restatements in other languages call the same exp, log10 and exp10 so
+// that they can agree bit for bit): fn 0 exp, 1 log10, 2 exp10.
+void o3d_detmath(int fn, const double *x, double *y, long long n) {
+  for (long long q = 0; q < n; q++)
+    y[q] = fn == 0 ? detmath::exp(x[q]) : (fn == 1 ? detmath::log10(x[q]) : detmath::exp10(x[q]));
+}
+
 // Constrained transport of the handle's state with its intermediates (test
 // infrastructure, as o3d_chem_probe): CC(1), CCT for the three edges and
 // CC(3).  out holds 17 padded arrays: U(1..8) as CCT read them (after the
