@@ -32,11 +32,16 @@ def fill_free_x_periodic_yz(a, n):
     a[nz + 3, :, :] = a[3, :, :]
 
 
-def dissip(U, n):
+def dissip(U, n, fill=None):
+    """fill(q, v), when given, replaces the free-x / periodic-y,z exchange
+    of velocity component q (1..3)."""
     nx, ny, nz = n
     vx, vy, vz = (U[q].copy() for q in (1, 2, 3))
-    for v in (vx, vy, vz):
-        fill_free_x_periodic_yz(v, n)
+    for q, v in zip((1, 2, 3), (vx, vy, vz)):
+        if fill is None:
+            fill_free_x_periodic_yz(v, n)
+        else:
+            fill(q, v)
     out = [vx.copy(), vy.copy(), vz.copy()]
     J = slice(1, ny + 3)   # j = 0..ny+1 (padded 1..ny+2)
     K = slice(1, nz + 3)

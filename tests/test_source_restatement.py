@@ -73,10 +73,14 @@ def exchange1(a, N, bc, species=False):
         r[N + 2] = r[N + 1]
 
 
-def exchange_all(a, p, species=False):
+def exchange_all(a, p, species=False, kind=None, xfill=None, U1=None):
+    """x, y, z in turn; xfill(kind, a, 1, 1, U1, None) replaces x's."""
     n = (p.nx, p.ny, p.nz)
     for d in range(3):
-        exchange1(local(a, d), n[d], (p.bc[2 * d], p.bc[2 * d + 1]), species)
+        if d == 0 and xfill is not None:
+            xfill(kind, local(a, 0), 1, 1, local(U1, 0), None)
+        else:
+            exchange1(local(a, d), n[d], (p.bc[2 * d], p.bc[2 * d + 1]), species)
 
 
 def gammi1(sp):
@@ -84,7 +88,7 @@ def gammi1(sp):
     return (2.0 * h + 2.0 * sp[2]) / (3.0 * h + 5.0 * sp[2])
 
 
-def source_thermal(U, sp, st, dt):
+def source_thermal(U, sp, st, dt, xfill=None):
     p = st.params
     U, sp = U.copy(), sp.copy()
     nx, ny, nz = p.nx, p.ny, p.nz
@@ -92,10 +96,10 @@ def source_thermal(U, sp, st, dt):
     dx, dy, dz = st.dx, st.dy, st.dz
     kb, kc = p.kb, p.kcond
     with np.errstate(all="ignore"):
-        exchange_all(U[0], p)
-        exchange_all(U[4], p)
+        exchange_all(U[0], p, False, ("U", 0), xfill, U[0])
+        exchange_all(U[4], p, False, ("U", 4), xfill, U[0])
         for s in range(8):
-            exchange_all(sp[s], p, species=True)
+            exchange_all(sp[s], p, True, ("sp", s), xfill, U[0])
         ntot = sp[1] + sp[0] + sp[2] + sp[3] + sp[4]          # p, H, H2, He, He+
         nimc = sp[0] + sp[1] + sp[3] + sp[4] + sp[2]          # H, p, He, He+, H2
 
@@ -124,7 +128,7 @@ def source_thermal(U, sp, st, dt):
         stats = {}
         for ps in (0, 1):
             if ps == 1:
-                exchange_all(U[4], p)
+                exchange_all(U[4], p, False, ("U", 4), xfill, U[0])
             Tn, div = temps_fluxes()
             C = fcool_ki(Tn, NN)
             expl = dt <= 0.2 * Pn / (g1c * np.abs(C))

@@ -21,23 +21,28 @@ from test_sweep_restatement import exchange, local, make_state, sweep
 ORDERS = ((0, 1, 2), (1, 2, 0), (2, 0, 1), (0, 2, 1), (1, 0, 2), (2, 1, 0))
 
 
-def fill(a, p, dirs):
-    """Two ghost layers in the given directions, in that order."""
+def fill(a, p, dirs, kind=None, xfill=None, U1=None):
+    """Two ghost layers in the given directions, in that order;
+    xfill(kind, a, 2, 1, U1, None) replaces the exchange along x."""
     n = (p.nx, p.ny, p.nz)
     for d in dirs:
-        exchange(local(a, d), n[d], (p.bc[2 * d], p.bc[2 * d + 1]))
+        if d == 0 and xfill is not None:
+            xfill(kind, local(a, 0), 2, 1, local(U1, 0), None)
+        else:
+            exchange(local(a, d), n[d], (p.bc[2 * d], p.bc[2 * d + 1]))
 
 
-def ct(U, st, dt):
+def ct(U, st, dt, xfill=None):
     """CC(1), CC(2) + CCT for the three edges, CC(3), CC(4); returns U and
     the new cell-centred field."""
     p = st.params
     n = (p.nx, p.ny, p.nz)
     dx = (st.dx, st.dy, st.dz)
     U = U.copy()
+    F = lambda a, dirs, kind: fill(a, p, dirs, kind, xfill, U[0])
     for d, fields in ((0, (1, 6, 7)), (1, (2, 5, 7)), (2, (3, 5, 6))):
         for f in fields:
-            fill(U[f], p, [d])
+            F(U[f], [d], ("U", f))
     Vfc = [np.full_like(U[0], np.nan) for _ in range(3)]
     for d in range(3):
         N, M, L = n[d], n[(d + 1) % 3], n[(d + 2) % 3]
@@ -46,12 +51,12 @@ def ct(U, st, dt):
         d0 = w[2:N + 3][:, None, None]
         T = (slice(2, M + 2), slice(2, L + 2))
         V[(slice(2, N + 3),) + T] = (dm * v[(slice(2, N + 3),) + T] + d0 * v[(slice(1, N + 2),) + T]) / (dm + d0)
-    fill(Vfc[1], p, [0])
-    fill(Vfc[2], p, [0, 1])
-    fill(Vfc[0], p, [1, 2])
-    fill(Vfc[1], p, [2])
-    fill(U[4], p, [0, 1, 2])
-    fill(U[0], p, [0, 1, 2])
+    F(Vfc[1], [0], ("Vfc", 1))
+    F(Vfc[2], [0, 1], ("Vfc", 2))
+    F(Vfc[0], [1, 2], ("Vfc", 0))
+    F(Vfc[1], [2], ("Vfc", 1))
+    F(U[4], [0, 1, 2], ("U", 4))
+    F(U[0], [0, 1, 2], ("U", 0))
     E = []
     for e in range(3):
         da, db, dc = e, (e + 1) % 3, (e + 2) % 3
@@ -73,22 +78,24 @@ def ct(U, st, dt):
     bcc[1][K, J, I] = 0.5 * (U[6][K, J, I] + U[6][K, sh(J), I])
     bcc[2][K, J, I] = 0.5 * (U[7][K, J, I] + U[7][sh(K), J, I])
     for c in range(3):
-        fill(bcc[c], p, [0, 1, 2])
+        F(bcc[c], [0, 1, 2], ("Bcc", c))
     return U, bcc
 
 
-def step(U, sp, bcc, st, ifevo):
+def step(U, sp, bcc, st, ifevo, xfill=None, dfill=None):
+    """One iteration; xfill replaces the x exchanges as in the parts,
+    dfill(q, v) DISSIP's exchange of velocity component q."""
     p = st.params
     dt, lim, _ = timestep(U, sp, bcc, st)
-    U, sp, _ = source_thermal(U, sp, st, 0.5 * dt)
+    U, sp, _ = source_thermal(U, sp, st, 0.5 * dt, xfill)
     coords = (st.x, st.dx, st.y, st.dy, st.z, st.dz)
     for d in ORDERS[ifevo - 1]:
-        U, sp = sweep(d, U, sp, bcc, coords, p, dt)
-    U, bcc = ct(U, st, dt)
-    U, sp, _ = source_thermal(U, sp, st, 0.5 * dt)
+        U, sp = sweep(d, U, sp, bcc, coords, p, dt, xfill)
+    U, bcc = ct(U, st, dt, xfill)
+    U, sp, _ = source_thermal(U, sp, st, 0.5 * dt, xfill)
     if p.dissip:
         U = U.copy()
-        U[1:4] = dissip(U, (p.nx, p.ny, p.nz))
+        U[1:4] = dissip(U, (p.nx, p.ny, p.nz), dfill)
     return U, sp, bcc, dt, lim
 
 

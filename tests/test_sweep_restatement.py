@@ -124,9 +124,12 @@ def heavy(s):   # H + p + He + He+ and H2, of the slots H, p, H2, He, He+, ...
     return s[0] + s[1] + s[3] + s[4], s[2]
 
 
-def sweep(d, U, sp, Bcc, coords, p, dt):
+def sweep(d, U, sp, Bcc, coords, p, dt, xfill=None):
     """MHD for direction d on copies of U (8 padded fields), the species
-    and Bcc; returns the new U and species."""
+    and Bcc; returns the new U and species.  xfill(kind, a, nol, mode, U1,
+    Bcc1), when given, replaces the exchanges along x (the x sweep's axis
+    0): kind names the array — ("U", f), ("sp", s), ("dxlag",), ("Blg", k)
+    — and U1, Bcc1 are the density and x field in the same frame."""
     U, sp = U.copy(), sp.copy()
     n = (p.nx, p.ny, p.nz)
     N = n[d]
@@ -152,12 +155,19 @@ def sweep(d, U, sp, Bcc, coords, p, dt):
     I = slice(2, N + 2)      # i = 1..N
     Im = slice(1, N + 1)     # i - 1
     kb, fac = p.kb, p.facdep
+
+    def ex(kind, a, mode=1, species=False):
+        if d == 0 and xfill is not None:
+            xfill(kind, a, 2, mode, Ul[0], Bl[0])
+        else:
+            exchange(a, N, bc, species)
+
     with np.errstate(all="ignore"):
         # ===== RHS
         for f in (0, VN, 4):
-            exchange(Ul[f], N, bc)
+            ex(("U", f), Ul[f])
         for s in range(8):
-            exchange(Sl[s], N, bc, species=True)
+            ex(("sp", s), Sl[s], species=True)
         g1 = slope(u(0), u(0), u(4), DX, kb, N)
         gVN = slope(u(VN), u(0), u(4), DX, kb, N)
         g5 = slope(u(4), u(0), u(4), DX, kb, N)
@@ -202,11 +212,11 @@ def sweep(d, U, sp, Bcc, coords, p, dt):
 
         # ===== MOC
         for f in (0, VT1, VT2, BN):
-            exchange(Ul[f], N, bc)
+            ex(("U", f), Ul[f])
         dxlag = np.zeros_like(xlag)
         dxlag[I] = xlag[I] - xlag[Im]
-        for a in (dxlag, Blg[0], Blg[1]):
-            exchange(a, N, bc)
+        for kind, a in ((("dxlag",), dxlag), (("Blg", 0), Blg[0]), (("Blg", 1), Blg[1])):
+            ex(kind, a)
         gm1 = slope(u(0), u(0), u(4), dxlag, kb, N)
         gT1 = slope(u(VT1), u(0), u(4), dxlag, kb, N)
         gT2 = slope(u(VT2), u(0), u(4), dxlag, kb, N)
@@ -251,12 +261,12 @@ def sweep(d, U, sp, Bcc, coords, p, dt):
         Blg[1][I] = Blg[1][I] + dt / DL * (bp * Vaz[1:] - bm * Vaz[:-1])
 
         # ===== REMAP
-        for a in Blg:
-            exchange(a, N, bc)
+        for k in (0, 1):
+            ex(("Blg", k), Blg[k], 2)
         for f in range(5):
-            exchange(Ul[f], N, bc)
+            ex(("U", f), Ul[f], 2)
         for s in range(8):
-            exchange(Sl[s], N, bc, species=True)
+            ex(("sp", s), Sl[s], 2, species=True)
         cols = [u(f) for f in range(5)] + Blg + [s_(s) for s in range(8)]
         grd = [slope(q, u(0), u(4), dxlag, kb, N) for q in cols]
         vadt = Vfc[B] * dt
