@@ -93,7 +93,8 @@ constexpr int kSweepZPencils = MHD_SWEEP_Z_PENCILS;
 #endif
 constexpr int kSweepTmaStride = 2 * kStageRows;
 
-// the driver's tensor-map encoder, resolved once (null when unavailable)
+// the CUDA driver API's tensor-map encoder, resolved once (null when
+// unavailable)
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void *p = nullptr;
