@@ -1624,11 +1624,19 @@ void o3d_chem_probe(void *h, double T, long long c, double *out) {
 }
 
 // The oracle's elementary functions over n values (test infrastructure:
-// restatements in other languages call the same exp, log10 and exp10 so
-// that they can agree bit for bit): fn 0 exp, 1 log10, 2 exp10.
-void o3d_detmath(int fn, const double *x, double *y, long long n) {
-  for (long long q = 0; q < n; q++)
-    y[q] = fn == 0 ? detmath::exp(x[q]) : (fn == 1 ? detmath::log10(x[q]) : detmath::exp10(x[q]));
+// restatements in other languages call the same routines so that they can
+// agree bit for bit): fn 0 exp, 1 log10, 2 exp10, 3 log, 4 x**e (e[q]).
+void o3d_detmath(int fn, const double *x, const double *e, double *y, long long n) {
+  for (long long q = 0; q < n; q++) {
+    const double v = x[q];
+    switch (fn) {
+      case 0: y[q] = detmath::exp(v); break;
+      case 1: y[q] = detmath::log10(v); break;
+      case 2: y[q] = detmath::exp10(v); break;
+      case 3: y[q] = detmath::log(v); break;
+      default: y[q] = detmath::pow(v, e[q]); break;
+    }
+  }
 }
 
 // Constrained transport of the handle's state with its intermediates (test

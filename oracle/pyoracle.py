@@ -70,7 +70,7 @@ def lib():
         L.o3d_chem_probe.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_longlong, _P]
         L.o3d_chem_cell_probe.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double, _P]
         L.o3d_ct_probe.argtypes = [ctypes.c_void_p, ctypes.c_double, _P]
-        L.o3d_detmath.argtypes = [ctypes.c_int, _P, _P, ctypes.c_longlong]
+        L.o3d_detmath.argtypes = [ctypes.c_int, _P, _P, _P, ctypes.c_longlong]
         L.o3d_ki_label.restype = ctypes.c_double
         L.o3d_ki_label.argtypes = [ctypes.c_double] * 4
         _lib = L
@@ -238,10 +238,13 @@ def ki_labels(x, kb=8.63359):
     return np.array([L.o3d_ki_label(float(a), float(b), float(c), kb) for a, b, c in x])
 
 
-def detmath(fn, x):
-    """The oracle's own exp ('exp'), log10 ('log10') or 10**x ('exp10')
-    elementwise over x, for restatements that must agree bit for bit."""
-    a = np.ascontiguousarray(x, dtype=np.float64)
+def detmath(fn, x, e=None):
+    """The oracle's own exp, log10, exp10 (10**x), log or pow (x**e)
+    elementwise (x and e broadcast), for restatements that must agree bit
+    for bit."""
+    a, b = np.broadcast_arrays(np.asarray(x, dtype=np.float64), np.asarray(0.0 if e is None else e, dtype=np.float64))
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
     y = np.empty_like(a)
-    lib().o3d_detmath({"exp": 0, "log10": 1, "exp10": 2}[fn], _ptr(a), _ptr(y), a.size)
+    code = {"exp": 0, "log10": 1, "exp10": 2, "log": 3, "pow": 4}[fn]
+    lib().o3d_detmath(code, _ptr(a), _ptr(b), _ptr(y), a.size)
     return y

@@ -40,8 +40,9 @@ def fcool_ki(T, NN):
     return (NN * NN * (laml + lamc) - NN) * absl
 
 
-def imc(P, n, dt, g1c, NN, kb):
-    """IMC: bisection of P_new + CooL(P_new) dt gamma1 = P in log P."""
+def imc(P, n, dt, g1c, cool, kb):
+    """IMC: bisection of P_new + CooL(P_new) dt gamma1 = P in log P; cool(T)
+    is the cooling function of the cells at temperatures T."""
     Pu = np.full_like(P, 1.e10)
     Pd = np.full_like(P, 1.e-10)
     Pm = np.full_like(P, 1.e1)
@@ -49,7 +50,7 @@ def imc(P, n, dt, g1c, NN, kb):
     nkbi = 1.0 / (kb * n)
     active = np.ones(P.shape, dtype=bool)
     for _ in range(30):
-        C = fcool_ki(Pm * nkbi, NN)
+        C = cool(Pm * nkbi)
         iud = sgn(1.0, Pm + C * dt * g1c - P)
         Pd = np.where(active, fmax2(-iud * Pm, Pd), Pd)
         Pu = np.where(active, fmin2(2.0 * Pm / (iud + 1.0 + 1.e-10), Pu), Pu)
@@ -88,7 +89,9 @@ def gammi1(sp):
     return (2.0 * h + 2.0 * sp[2]) / (3.0 * h + 5.0 * sp[2])
 
 
-def source_thermal(U, sp, st, dt, xfill=None):
+def source_thermal(U, sp, st, dt, xfill=None, cool=None):
+    """cool(T, sel): the cooling function of the interior cells selected by
+    the mask sel (all for None) at temperatures T; KI by default."""
     p = st.params
     U, sp = U.copy(), sp.copy()
     nx, ny, nz = p.nx, p.ny, p.nz
@@ -123,6 +126,8 @@ def source_thermal(U, sp, st, dt, xfill=None):
 
         Pn = U[4][K, J, I].copy()
         NN = U[0][K, J, I] / 1.27
+        if cool is None:
+            cool = lambda T, sel: fcool_ki(T, NN if sel is None else NN[sel])
         g1c = gammi1([s[K, J, I] for s in sp])
         n = nimc[K, J, I]
         stats = {}
@@ -130,14 +135,16 @@ def source_thermal(U, sp, st, dt, xfill=None):
             if ps == 1:
                 exchange_all(U[4], p, False, ("U", 4), xfill, U[0])
             Tn, div = temps_fluxes()
-            C = fcool_ki(Tn, NN)
+            C = cool(Tn, None)
             expl = dt <= 0.2 * Pn / (g1c * np.abs(C))
+            imp = ~expl
+            sub = lambda T: cool(T, imp)
             if ps == 0:
                 P = np.where(expl, U[4][K, J, I] - g1c * C * dt * 0.5, 0.0)
-                P[~expl] = imc(U[4][K, J, I][~expl], n[~expl], dt * 0.5, g1c[~expl], NN[~expl], kb)
+                P[imp] = imc(U[4][K, J, I][imp], n[imp], dt * 0.5, g1c[imp], sub, kb)
             else:
                 P = np.where(expl, Pn - g1c * C * dt, 0.0)
-                P[~expl] = imc(Pn[~expl], n[~expl], dt, g1c[~expl], NN[~expl], kb)
+                P[imp] = imc(Pn[imp], n[imp], dt, g1c[imp], sub, kb)
             tcd = g1c * kc * np.sqrt(Tn)
             tcd = 0.49 * n * kb / tcd * (dx[I] * dx[I])[None, None, :]
             tcd = sgn(0.5, tcd - dt)
@@ -151,7 +158,8 @@ def source_thermal(U, sp, st, dt, xfill=None):
     return U, sp, stats
 
 
-def timestep(U, sp, bcc, st):
+def timestep(U, sp, bcc, st, cool=None):
+    """cool(T): the cooling function of the interior cells (KI by default)."""
     p = st.params
     nx, ny, nz = p.nx, p.ny, p.nz
     K, J, I = slice(2, nz + 2), slice(2, ny + 2), slice(2, nx + 2)
@@ -172,7 +180,7 @@ def timestep(U, sp, bcc, st):
     g1c = gammi1(s)
     alpha = g1c * p.kcond * np.sqrt(fmin2(Tn, 15.0))
     alpha = 0.4 * Nn * p.kb / alpha * (dl * dl)
-    C = fcool_ki(Tn, u[0] / 1.27)
+    C = fcool_ki(Tn, u[0] / 1.27) if cool is None else cool(Tn)
     tauC = fmax2(0.2 * (u[4] / g1c / np.abs(C)), 2.5e-4)
     tlmt = min(p.tfinal, np.min(tauC), np.min(alpha))
     dtm = min(p.tfinal, p.cfl * tcfl)
