@@ -17,6 +17,12 @@
 // before the interior changed).  Loops, operation order and floating-point
 // expressions follow the Fortran line by line; build with -ffp-contract=off.
 // exp/log10/10**x come from detmath.h, shared with the GPU kernels.
+//
+// Pinned: its 1D sibling (mhd1d.cpp) reproduces the reference's shipped
+// outputs (KIcool/cooling.dat, KIcool/bw051.dat); this file equals, bit for
+// bit, second restatements of the Fortran written independently in NumPy
+// (tests/test_*_restatement.py): every routine of EVOLVE and whole steps
+// with free, periodic and inflow boundaries, KI cooling and the chemistry.
 #include <cmath>
 #include <complex>
 #include <cstdio>
