@@ -2,10 +2,11 @@
 Fortran, vectorised over cells, and checked against the oracle bit for bit:
 Fcool with fesc and LEVC2 (3DMHD-CfCA/MCF3DSGincfca3.f90:2825-2895),
 RATES (:3040-3131), Omexp (:3134-3140), the network of SOURCE's CHEM
-branch (:2576-2776), the thermal SOURCE and the time step with the species
-cooling, and whole steps of the shipped deck's configuration — inflow on
-both x sides, the chemistry, KI-free species cooling — composed from the
-restated parts.
+branch (:2576-2776), SHIELD's column densities (:2924-3036; INITIA's twenty
+passes and SOURCE's one), the thermal SOURCE and the time step with the
+species cooling, and whole steps of the shipped deck's configuration —
+inflow on both x sides, the chemistry, KI-free species cooling — composed
+from the restated parts.
 
 exp, log and real powers are the oracle's own deterministic routines
 (called through the oracle library, as in the KI restatement); integer
@@ -18,10 +19,9 @@ import pytest
 from code_tohoku_gb300 import problems
 from oracle.pyoracle import Oracle3D, detmath
 from test_chem_restatement import mixed_state
-from test_ct_restatement import local
 from test_dissip_restatement import dissip
 from test_inflow_restatement import InflowX, dissip_fill, make_inflow
-from test_source_restatement import gammi1, source_thermal, timestep
+from test_source_restatement import source_thermal, timestep
 from test_step_restatement import ORDERS, ct
 from test_sweep_restatement import fmax2, fmin2, make_state, sgn, sweep
 
@@ -241,14 +241,44 @@ def totals(sp):
     return sp[1] + sp[4] + sp[6], sp[1] + sp[0] + 2.0 * sp[2] + sp[3] + sp[4]
 
 
-def source_chem(U, sp, nde, ndtot, col, st, dt, xfill=None):
-    """SOURCE with ifchem = 2 and no SHIELD: nde and ndtot rebuilt on the
-    interior, the thermal branch with the species cooling, the network."""
+def shield(U, sp, nde, ndtot, col, dx1, kb):
+    """SHIELD (:2924-3036) for one block holding whole x lines: the C+
+    optical-depth source of every interior cell from the previous tCII
+    columns, then the columns of ndtot, H2, C, CO and that source along each
+    x line from the left and from the right, each cell adding half its
+    width before and after its own column is stored.  col holds Ntot, NH2,
+    NnC, NCO, tCII, each from the left and from the right."""
+    nz, ny, nx = (a - 4 for a in U[0].shape)
+    K, J, I = slice(2, nz + 2), slice(2, ny + 2), slice(2, nx + 2)
+    H, p, H2, He, Hep, C, Cp, CO = (a[K, J, I] for a in sp)
+    b21 = fesc(col[8][K, J, I]) + fesc(col[9][K, J, I])
+    T = U[4][K, J, I] / (kb * (p + H + H2 + He + Hep))
+    n1, n2 = levc2(T, b21, H, H2, nde[K, J, I], Cp)
+    src = 1.15563e1 * (n1 - n2) * (1.0 / DV)
+    dxh = 0.5 * dx1
+    vals = (ndtot[K, J, I], H2, C, CO, src)
+    out = col.copy()
+    for side, order in ((0, range(nx)), (1, range(nx - 1, -1, -1))):
+        acc = [np.zeros((nz, ny)) for _ in range(5)]
+        for i in order:
+            for q in range(5):
+                acc[q] = acc[q] + dxh * vals[q][:, :, i]
+                out[2 * q + side][K, J, 2 + i] = acc[q]
+                acc[q] = acc[q] + dxh * vals[q][:, :, i]
+    return out
+
+
+def source_chem(U, sp, nde, ndtot, col, st, dt, xfill=None, with_columns=False):
+    """SOURCE with ifchem = 2: nde and ndtot rebuilt on the interior, SHIELD
+    when ifrad = 2, the thermal branch with the species cooling, the
+    network.  with_columns: return the columns too."""
     p = st.params
     K, J, I = slice(2, p.nz + 2), slice(2, p.ny + 2), slice(2, p.nx + 2)
     nde, ndtot = nde.copy(), ndtot.copy()
     e, t = totals([s[K, J, I] for s in sp])
     nde[K, J, I], ndtot[K, J, I] = e, t
+    if p.ifrad == 2:
+        col = shield(U, sp, nde, ndtot, col, st.dx[2], p.kb)
     cells = [s[K, J, I] for s in sp]
     cc = [c[K, J, I] for c in col]
     ne, nt = nde[K, J, I], ndtot[K, J, I]
@@ -265,6 +295,8 @@ def source_chem(U, sp, nde, ndtot, col, st, dt, xfill=None):
     for q in range(8):
         sp[q][K, J, I] = out[q]
     nde[K, J, I], ndtot[K, J, I], U[0][K, J, I] = ne1, nt1, rho
+    if with_columns:
+        return U, sp, nde, ndtot, col
     return U, sp, nde, ndtot
 
 
@@ -394,3 +426,34 @@ def test_shipped_deck_steps_bit_for_bit(first):
         for c in range(3):
             assert np.array_equal(bcc[c], bcco[c]), (s, c)
         xf.time += dt
+
+
+def test_shield_and_source_with_columns_bit_for_bit():
+    """INITIA's twenty SHIELD passes after the species totals of cells
+    1..n+1 (:471-479), then SOURCE with SHIELD on (ifrad = 2): the columns,
+    the state and the species."""
+    st = deck_state((10, 9, 8), (1, 1, 3, 3, 3, 3), 41)
+    st.params = st.params.replace(ifrad=2)
+    p = st.params
+    o = Oracle3D(p)
+    o.upload(st)
+    U0, sp0, _ = o.download()
+    col0 = o.columns()
+    nde, ndtot = np.zeros_like(U0[0]), np.zeros_like(U0[0])
+    Kp, Jp, Ip = slice(2, p.nz + 3), slice(2, p.ny + 3), slice(2, p.nx + 3)
+    nde[Kp, Jp, Ip], ndtot[Kp, Jp, Ip] = totals([s[Kp, Jp, Ip] for s in sp0])
+    col = np.zeros((10,) + U0[0].shape)
+    for _ in range(20):
+        col = shield(U0, sp0, nde, ndtot, col, st.dx[2], p.kb)
+    assert np.array_equal(col, col0)
+    assert np.all(col[:8][:, 2:-2, 2:-2, 2:-2] > 0.0) and np.any(col[8:] != 0.0)
+    dt = 0.01
+    o.source(dt)
+    U1, sp1, _ = o.download()
+    col1 = o.columns()
+    U2, sp2, _, _, col2 = source_chem(U0, sp0, nde, ndtot, col0, st, dt, with_columns=True)
+    assert np.array_equal(col1, col2)
+    for f in range(8):
+        assert np.array_equal(U1[f], U2[f]), f
+    for q in range(8):
+        assert np.array_equal(sp1[q], sp2[q]), q
