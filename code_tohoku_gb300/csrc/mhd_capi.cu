@@ -604,8 +604,16 @@ int mhd_timestep(mhd_handle *h, double *dt, int *st) { return timestep_impl(h, d
 namespace {
 // the thermal branch of SOURCE (ifthrm = 2, :2477-2572); rho_sp_filled:
 // the caller has already filled the ghosts of rho and the species with the
-// same values (mhd_step_host, which copies those arrays back meanwhile)
-int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
+// same values (mhd_step_host, which copies those arrays back meanwhile).
+// The predictor writes pnew, not U5; the reference updates U5 in place, so
+// its exchange between the passes (:2526-2528) leaves the predictor's values
+// in U5's one-layer ghost shell after SOURCE.  So pnew takes U5's outer
+// shell before that exchange (which copies from it), and U5 takes pnew's
+// one-layer shell after the corrector: every padded cell as the reference.
+// fill_cco: the exchange also takes species 5-7 (C, C+, CO), which the
+// thermal update does not read: the reference exchanges all eight, and the
+// second SOURCE of a step leaves them in the ghost cells its output reads.
+int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false, bool fill_cco = true) {
   // SOURCE :2481-2486 — rho, p and the species, one ghost layer, x y z
   if (rho_sp_filled) {
     TRY(fill(h, {h->f.U[4]}, 7, 1, 0, {IN_P}));
@@ -614,6 +622,7 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     const double *arr[7] = {h->f.U[0], h->f.U[4], h->f.sp[0], h->f.sp[1], h->f.sp[2], h->f.sp[3], h->f.sp[4]};
     const int rules[7] = {IN_RHO, IN_P, IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4};
     TRY(fill_mask(h, arr, 7, 7, 1, 0x7cu, rules, 7));
+    if (fill_cco) TRY(fill(h, {h->f.sp[5], h->f.sp[6], h->f.sp[7]}, 7, 1, 1, {IN_SPEC + 5, IN_SPEC + 6, IN_SPEC + 7}));
   }
   if (h->p.precision == MHD_PREC_FP32) {
     if (h->p.cooling == MHD_COOL_SURROGATE && !h->sur_net)
@@ -641,11 +650,13 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
     h->sh2_valid = true;
     CK(source_fp32(a, stiff_mode, h->stream));
     h->launches += stiff_mode ? 1 : 0;   // the stiff-cell kernel
+    CK(shell_copy(h->g, h->f.U[4], h->pnew, 2, h->stream));
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, false, h->stream));
     CK(source_fp32(a, stiff_mode, h->stream));
     h->launches += stiff_mode ? 1 : 0;
+    CK(shell_copy(h->g, h->pnew, h->f.U[4], 1, h->stream));
     return MHD_OK;
   }
   SourceArgs a{};
@@ -653,15 +664,17 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false) {
   a.dt = dt; a.err = h->err; a.imc_count = h->dtred + 2; a.skip = nullptr;
   a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
   CK(source_pass(a, h->stream));
+  CK(shell_copy(h->g, h->f.U[4], h->pnew, 2, h->stream));
   TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));   // :2526-2528
   a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
   CK(source_pass(a, h->stream));
+  CK(shell_copy(h->g, h->pnew, h->f.U[4], 1, h->stream));
   return MHD_OK;
 }
 }  // namespace
 
 namespace {
-int source_impl(mhd_handle *h, double dt, bool rho_sp_filled) {
+int source_impl(mhd_handle *h, double dt, bool rho_sp_filled, bool fill_cco = true) {
   if (!h) return MHD_ERR_ARG;
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   CKR(cudaSetDevice(h->p.device));
@@ -670,7 +683,7 @@ int source_impl(mhd_handle *h, double dt, bool rho_sp_filled) {
   // the species cooling and the network
   if (h->p.ifchem == 2 || h->p.ifrad == 2) CK(chem_totals(h->g, h->f, 0, h->stream));
   if (h->p.ifrad == 2) TRY(shield(h));   // :2466-2468
-  if (h->p.ifthrm == 2) TRY(source_thermal(h, dt, rho_sp_filled));
+  if (h->p.ifthrm == 2) TRY(source_thermal(h, dt, rho_sp_filled, fill_cco));
   // the chemistry network after the thermal update (ifchem = 2, :2576-2776)
   if (h->p.ifchem == 2) {
     if (h->p.precision == MHD_PREC_FP32) CK(chem_step_fp32(h->g, h->ph, h->f, dt, h->err, h->stream));
@@ -778,11 +791,13 @@ int mhd_advance(mhd_handle *h, double dt) {
   if (!h->uploaded) return fail(h, MHD_ERR_STATE, "no state uploaded");
   static const int orders[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
   if (h->p.ifgrv == 2) TRY(gravity_half_kick(h, dt));   // EVOLVE :607
-  TRY(mhd_source(h, 0.5 * dt));
+  // (the ghost values of species 5-7 the first SOURCE would exchange are
+  // the second's to leave; no step reads them)
+  TRY(source_impl(h, 0.5 * dt, false, false));
   for (int s = 0; s < 3; s++) TRY(mhd_sweep(h, orders[h->ifevo - 1][s], dt));
   h->ifevo = h->ifevo % 6 + 1;
   TRY(mhd_ct(h, dt));
-  TRY(mhd_source(h, 0.5 * dt));
+  TRY(source_impl(h, 0.5 * dt, false, true));
   if (h->p.ifgrv == 2) TRY(gravity(h, dt, true));        // :653
   if (h->p.dissip) TRY(mhd_dissip(h));
   h->time = h->time + dt;
@@ -890,13 +905,13 @@ int last_sweep_slabs(mhd_handle *h, int dir, double d, double *U_out, double *sp
   fr.f[0] = f.U[0];
   fr.rule[0] = IN_RHO;
   fr.in = h->ph.in;
-  FillArgs fs{};   // species 0-4 (thermal SOURCE): one layer, interior transverse lines
-  fs.nf = 5;
-  for (int q = 0; q < 5; q++) {
+  FillArgs fs{};   // the species (thermal SOURCE): one layer, interior transverse lines
+  fs.nf = 8;
+  for (int q = 0; q < 8; q++) {
     fs.f[q] = f.sp[q];
     fs.rule[q] = IN_SPEC + q;
   }
-  fs.spmask = 31u;
+  fs.spmask = 255u;
   fs.in = h->ph.in;
   const bool sp_fill = h->p.ifthrm == 2;
   // the copies back of rho and the 8 species over padded [lo, hi) along rdim
@@ -961,7 +976,7 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, 
   const size_t nc = (size_t)h->g.ncell, nb = nc * sizeof(double);
   Fields &f = h->f;
   if (h->p.ifgrv == 2) TRY(gravity_half_kick(h, d));   // EVOLVE :607
-  TRY(mhd_source(h, 0.5 * d));
+  TRY(source_impl(h, 0.5 * d, false, false));   // species 5-7 may still be on the link
   if (late_species && !late_slabs) CKR(cudaStreamWaitEvent(h->stream, h->ev_io[2], 0));
   const int *order = kSweepOrders[h->ifevo - 1];
   h->ifevo = h->ifevo % 6 + 1;
@@ -975,8 +990,9 @@ int step_host_body(mhd_handle *h, double d, double *U_out, double *species_out, 
     // the ghost fills CC(2) and SOURCE would make, made now
     TRY(fill(h, {f.U[0]}, 7, 2, 0, {IN_RHO}));
     if (h->p.ifthrm == 2)
-      TRY(fill(h, {f.sp[0], f.sp[1], f.sp[2], f.sp[3], f.sp[4]}, 7, 1, 1,
-               {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4}));
+      TRY(fill(h, {f.sp[0], f.sp[1], f.sp[2], f.sp[3], f.sp[4], f.sp[5], f.sp[6], f.sp[7]}, 7, 1, 1,
+               {IN_SPEC + 0, IN_SPEC + 1, IN_SPEC + 2, IN_SPEC + 3, IN_SPEC + 4, IN_SPEC + 5, IN_SPEC + 6,
+                IN_SPEC + 7}));
     CKR(cudaEventRecord(h->ev_io[0], h->stream));
     CKR(cudaStreamWaitEvent(h->io_stream, h->ev_io[0], 0));
     CKR(cudaMemcpyAsync(U_out, f.U[0], nb, cudaMemcpyDeviceToHost, h->io_stream));

@@ -70,6 +70,13 @@ cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s) {
   return cell_b_range(g, f, 0, (long long)g.n[0] * g.n[1] * g.n[2], s);
 }
 
+cudaError_t shell_copy(const Grid &g, const double *src, double *dst, int lay, cudaStream_t s) {
+  if (lay != 1 && lay != 2) return cudaErrorInvalidValue;
+  const long long n = 2 * ((long long)g.s[1] * g.s[2] + (long long)g.s[0] * g.s[2] + (long long)g.s[0] * g.s[1]);
+  shell_copy_kernel<<<nblk(n, 256), 256, 0, s>>>(g, src, dst, lay);
+  return cudaGetLastError();
+}
+
 cudaError_t cell_b_range(const Grid &g, const Fields &f, long long c0, long long c1, cudaStream_t s) {
   if (c1 <= c0) return cudaSuccess;
   cell_b_kernel<<<nblk(c1 - c0, 512), 256, 0, s>>>(g, f, c0, c1);

@@ -460,6 +460,37 @@ __global__ void ghost_fill_all_kernel(Grid g, FillArgs a, int dirs, int nol, Fil
   F[gidx(g, c[0], c[1], c[2])] = F[gidx(g, cur[0], cur[1], cur[2])];
 }
 
+// dst = src on the ghost shell of layer lay (1: every cell with an index 0
+// or n+1 in some direction, the cells a one-layer exchange of all three
+// directions writes; 2: every cell with an index -1 or n+2): thread per cell
+// of the six planes, each plane spanning the padded extents of the other
+// two directions (a cell on two planes is copied twice, with one value).
+// Indices are the reference's, -1..n+2.
+__global__ void __launch_bounds__(256) shell_copy_kernel(Grid g, const double *src, double *dst, int lay) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long a01 = (long long)g.s[1] * g.s[2], a02 = (long long)g.s[0] * g.s[2],
+                  a03 = (long long)g.s[0] * g.s[1];
+  const long long per[3] = {a01, a02, a03};
+  long long r = t;
+  int d = 0;
+  while (d < 3 && r >= 2 * per[d]) {
+    r -= 2 * per[d];
+    d++;
+  }
+  if (d == 3) return;
+  const int side = (int)(r / per[d]);
+  const long long q = r % per[d];
+  const int o1 = (d + 1) % 3, o2 = (d + 2) % 3;
+  const int lo = (o1 < o2) ? o1 : o2, hi = (o1 < o2) ? o2 : o1;
+  int c[3];
+  // index along d: 1 - lay or n + lay
+  c[d] = side == 0 ? 1 - lay : g.n[d] + lay;
+  c[lo] = (int)(q % g.s[lo]) - 1;
+  c[hi] = (int)(q / g.s[lo]) - 1;
+  const long long a = gidx(g, c[0], c[1], c[2]);
+  dst[a] = src[a];
+}
+
 #endif  // MHD_COMMON_KERNELS
 
 // ============================================================ the sweep

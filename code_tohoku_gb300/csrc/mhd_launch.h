@@ -64,6 +64,9 @@ cudaError_t face_velocity(const Grid &g, const Fields &f, double *v0, double *v1
 cudaError_t face_b(const Grid &g, const Fields &f, const double *ez, const double *ex, const double *ey, double dt,
                    cudaStream_t s);
 cudaError_t cell_b(const Grid &g, const Fields &f, cudaStream_t s);
+// dst = src on the ghost shell of layer lay: 1 the cells with an index 0 or
+// n+1 in some direction, 2 those with an index -1 or n+2
+cudaError_t shell_copy(const Grid &g, const double *src, double *dst, int lay, cudaStream_t s);
 // CC(4) for the interior cells of linear index [c0, c1) (i fastest, then j, k)
 cudaError_t cell_b_range(const Grid &g, const Fields &f, long long c0, long long c1, cudaStream_t s);
 cudaError_t source_pass(const SourceArgs &a, cudaStream_t s);

@@ -386,6 +386,23 @@ def test_source_with_chemistry_bit_for_bit(dt):
     assert np.any(U1[0] != U0[0]) and np.any(sp1[7] != sp0[7])
 
 
+def deck_step(U, sp, bcc, nde, ndtot, col, st, ifevo, xf):
+    """One EVOLVE iteration with the chemistry on (SHIELD off) and the x
+    exchanges of xf; returns the new state, nde, ndtot, dt and the limiter
+    id (the caller advances xf.time by dt)."""
+    p = st.params
+    coords = (st.x, st.dx, st.y, st.dy, st.z, st.dz)
+    dt, lim, _ = timestep(U, sp, bcc, st, species_cool_at(sp, nde, ndtot, col, p))
+    U, sp, nde, ndtot = source_chem(U, sp, nde, ndtot, col, st, 0.5 * dt, xf)
+    for d in ORDERS[ifevo - 1]:
+        U, sp = sweep(d, U, sp, bcc, coords, p, dt, xf)
+    U, bcc = ct(U, st, dt, xf)
+    U, sp, nde, ndtot = source_chem(U, sp, nde, ndtot, col, st, 0.5 * dt, xf)
+    U = U.copy()
+    U[1:4] = dissip(U, (p.nx, p.ny, p.nz), dissip_fill(xf, p))
+    return U, sp, bcc, nde, ndtot, dt, lim
+
+
 @pytest.mark.parametrize("first", [1, 4])
 def test_shipped_deck_steps_bit_for_bit(first):
     """Inflow on both x sides, the chemistry on, SHIELD off: the shipped
@@ -404,17 +421,9 @@ def test_shipped_deck_steps_bit_for_bit(first):
     Kp, Jp, Ip = slice(2, p.nz + 3), slice(2, p.ny + 3), slice(2, p.nx + 3)
     nde[Kp, Jp, Ip], ndtot[Kp, Jp, Ip] = totals([s[Kp, Jp, Ip] for s in sp])
     xf = InflowX(inflow, dtf, st)
-    coords = (st.x, st.dx, st.y, st.dy, st.z, st.dz)
     for s in range(3):
         ifevo = (first - 1 + s) % 6 + 1
-        dt, lim, _ = timestep(U, sp, bcc, st, species_cool_at(sp, nde, ndtot, col, p))
-        U, sp, nde, ndtot = source_chem(U, sp, nde, ndtot, col, st, 0.5 * dt, xf)
-        for d in ORDERS[ifevo - 1]:
-            U, sp = sweep(d, U, sp, bcc, coords, p, dt, xf)
-        U, bcc = ct(U, st, dt, xf)
-        U, sp, nde, ndtot = source_chem(U, sp, nde, ndtot, col, st, 0.5 * dt, xf)
-        U = U.copy()
-        U[1:4] = dissip(U, (p.nx, p.ny, p.nz), dissip_fill(xf, p))
+        U, sp, bcc, nde, ndtot, dt, lim = deck_step(U, sp, bcc, nde, ndtot, col, st, ifevo, xf)
         dto, limo = o.step()
         Uo, spo, bcco = o.download()
         assert dt == dto and lim == limo, (s, dt, dto, lim, limo)
