@@ -611,8 +611,10 @@ namespace {
 // shell before that exchange (which copies from it), and U5 takes pnew's
 // one-layer shell after the corrector: every padded cell as the reference.
 // fill_cco: the exchange also takes species 5-7 (C, C+, CO), which the
-// thermal update does not read: the reference exchanges all eight, and the
-// second SOURCE of a step leaves them in the ghost cells its output reads.
+// thermal update does not read (the reference exchanges all eight), and U5
+// takes the predictor's shell.  The first SOURCE of a step skips both: CT's
+// exchanges and the second SOURCE rewrite those ghost cells before anything
+// reads them.
 int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false, bool fill_cco = true) {
   // SOURCE :2481-2486 — rho, p and the species, one ghost layer, x y z
   if (rho_sp_filled) {
@@ -650,13 +652,13 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false, bool fi
     h->sh2_valid = true;
     CK(source_fp32(a, stiff_mode, h->stream));
     h->launches += stiff_mode ? 1 : 0;   // the stiff-cell kernel
-    CK(shell_copy(h->g, h->f.U[4], h->pnew, 2, h->stream));
+    if (fill_cco) CK(shell_copy(h->g, h->f.U[4], h->pnew, 2, h->stream));
     TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));
     a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
     CK(temp_fp32(h->g, h->f, a.pin, h->ph.kb, h->temp32, h->sh2_32, false, h->stream));
     CK(source_fp32(a, stiff_mode, h->stream));
     h->launches += stiff_mode ? 1 : 0;
-    CK(shell_copy(h->g, h->pnew, h->f.U[4], 1, h->stream));
+    if (fill_cco) CK(shell_copy(h->g, h->pnew, h->f.U[4], 1, h->stream));
     return MHD_OK;
   }
   SourceArgs a{};
@@ -664,11 +666,11 @@ int source_thermal(mhd_handle *h, double dt, bool rho_sp_filled = false, bool fi
   a.dt = dt; a.err = h->err; a.imc_count = h->dtred + 2; a.skip = nullptr;
   a.pin = h->f.U[4]; a.pold = h->f.U[4]; a.pout = h->pnew; a.pass = 0;
   CK(source_pass(a, h->stream));
-  CK(shell_copy(h->g, h->f.U[4], h->pnew, 2, h->stream));
+  if (fill_cco) CK(shell_copy(h->g, h->f.U[4], h->pnew, 2, h->stream));
   TRY(fill(h, {h->pnew}, 7, 1, 0, {IN_P}));   // :2526-2528
   a.pin = h->pnew; a.pold = h->f.U[4]; a.pout = h->f.U[4]; a.pass = 1;
   CK(source_pass(a, h->stream));
-  CK(shell_copy(h->g, h->pnew, h->f.U[4], 1, h->stream));
+  if (fill_cco) CK(shell_copy(h->g, h->pnew, h->f.U[4], 1, h->stream));
   return MHD_OK;
 }
 }  // namespace
